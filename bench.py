@@ -1,0 +1,328 @@
+"""Benchmark of the DVS hot path on one GB300 (or N, one rank per GPU).
+
+Workload (default "precision"): Prophesee 1280x720 (fx=fy=1000, cx=640,
+cy=360) over a seeded 4096x4096-vertex fBm+crater heightfield (33.5M
+triangles, 10 m spacing), supersample 16 (config/prophesee.yaml), a 2 s
+descent from 3 km to 500 m, 1 us horizons and circuit cells.  A step is one
+native batch of 64 horizons (apps/main_dvs.cpp:294-296) = 64 us of simulated
+time.  The scene (several GB) is far larger than L2, so no flush is needed.
+
+value  = primary + shadow rays traced per second of device time (CUDA events
+         on the sensor's stream around K enqueued steps; inputs resident).
+e2e    = the same metric through dvs_sensor_process_events with host
+         intervals in and host events out (copies and readout included).
+cpu_baseline / --impl reference = the oracle port (the reference has no CPU
+         renderer) timed with all host threads on a bounded sample of the
+         same workload's pixel-cells.
+Multi-GPU: one rank per GPU, each an independent job (the reference runs one
+sequence per GPU, tools/run_sequences.py:247-256): weak scaling, no
+collective on the data path.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # configs: precision (1280x720), small (346x260 DAVIS, plain method)
+    "precision": dict(grid=4096, seed=20260003, camera=dict(width=1280, height=720, fx=1000.0, fy=1000.0, cx=640.0,
+                                                            cy=360.0),
+                      ss=16, z0=3000.0, z1=500.0, duration=2.0, ground_speed=80.0, sun_elevation=30.0,
+                      intensity=1000.0, time_resolution=1e-6, batch=64),
+    "small": dict(grid=256, seed=20260001, camera=dict(width=346, height=260, fx=300.0, fy=300.0, cx=173.0, cy=130.0),
+                  ss=1, z0=1000.0, z1=1000.0, duration=0.49, ground_speed=50.0, sun_elevation=30.0, intensity=1.0,
+                  time_resolution=1e-5, batch=64),
+}
+HAPKE = dict(b=0.3, c=0.4, hS=0.06, hC=1.0, thetap=0.349066, w=0.25, B_S0=1.0, B_C0=0.0, phi=0.3)
+PHYSIC = dict(threshold_pos=0.2, threshold_neg=0.2, refractory_time=200e-6, readout_bandwidth=5e6,
+              readout_latency=18e-9, threshold_std=0.03, threshold_min=0.01, wavelength_nm=550,
+              quantum_efficiency=0.3, pixel_pitch_um=15, fill_factor=0.2, f_number=2.0, lens_transmission=0.8,
+              radiance_scale=0.001, temperature_k=300, subthreshold_kappa=0.8, receptor_capacitance_f=1e-15,
+              reset_capacitance_f=20e-15, dark_current_a=1e-18, reset_leakage_a=0, circuit_step=1e-6,
+              photon_shot_noise=1, reset_thermal_noise=0, random_seed=114514, max_events_per_step=16,
+              readout_queue_capacity=1000000)
+METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency vs plain path"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+def make_workload(name, rank=0):
+    from dvsrender4deepspace_gb300 import terrain, trajectory
+    w = WORKLOADS[name]
+    V, N, I = terrain.terrain_mesh(w["grid"], w["seed"])
+    light = trajectory.sun_direction(w["sun_elevation"], 35.0)
+    # each rank flies its own job over the same terrain (offset start)
+    x0 = -2000.0 + 1000.0 * rank if w["grid"] >= 1024 else 0.0
+    traj = trajectory.Descent((x0, 0.0), w["z0"], w["z1"], w["duration"], w["ground_speed"], light, w["intensity"])
+    return w, V, N, I, traj
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(name, V, N, I, traj, w, budget_s=15.0, threads=0):
+    """Oracle port (reference arithmetic, FP32 rays) on a bounded sample of the
+    workload's pixel-cells; returns Mrays/s and the sample description."""
+    from oracle import oracle as O
+    cam = w["camera"]
+    t_build = time.time()
+    osc = O.OracleScene(V, N, I, cam, w["ss"], HAPKE, max_leaf=64)
+    build_s = time.time() - t_build
+    rng = np.random.default_rng(7)
+    n_pix = cam["width"] * cam["height"]
+    nthreads = threads or os.cpu_count()
+    total_rays, total_t, cells = 0, 0.0, 0
+    batch = max(64, 2048 // max(1, w["ss"] * w["ss"] // 16))
+    while total_t < budget_s and cells < 50:
+        t = cells * w["time_resolution"]
+        pix = rng.choice(n_pix, size=batch, replace=False).astype(np.int32)
+        t0 = time.perf_counter()
+        _, _, prim, shad = osc.render_pixels(traj.state(t), pix, nthreads)
+        total_t += time.perf_counter() - t0
+        total_rays += prim + shad
+        cells += 1
+    return {"value": total_rays / total_t / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+            "sample": "%d pixel-cells (%d random pixels x %d cell times, ss=%d), %.1f s of CPU work; oracle "
+                      "binary BVH (leaf 64) built in %.1f s" % (batch * cells, batch, cells, w["ss"], total_t, build_s)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    w, V, N, I, traj = make_workload(args.workload)
+    res = []
+    for step in range(args.warmup + args.steps):
+        cb = cpu_baseline(args.workload, V, N, I, traj, w, budget_s=max(2.0, 60.0 / (args.warmup + args.steps)))
+        if step >= args.warmup:
+            res.append(cb)
+    value = statistics.median(r["value"] for r in res)
+    cbl = dict(res[-1])
+    cbl["value"] = value
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, **{k: v for k, v in w.items() if k != "camera"},
+                       "camera": w["camera"]},
+            "cpu_baseline": cbl, "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gb300(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from dvsrender4deepspace_gb300 import DeviceScene, EventSensor, interval_array, trajectory
+    from dvsrender4deepspace_gb300.build import build
+    if rank == 0:
+        build()
+    if world > 1:
+        torch.distributed.barrier()
+    w, V, N, I, traj = make_workload(args.workload, rank)
+    t_setup = time.time()
+    scene = DeviceScene(V, N, I, w["camera"], w["ss"], HAPKE, leaf_size=args.leaf)
+    info = scene.info()
+    sensor = EventSensor(scene, PHYSIC, timing=True, cells_per_chunk=args.chunk, cells_per_warp=args.cw)
+    sensor.initialize(traj.state(0.0), 0.0)
+    setup_s = time.time() - t_setup
+    dt, B = w["time_resolution"], w["batch"]
+    t_cursor = [0.0]
+
+    def next_batch():
+        ivs = trajectory.horizons(traj, t_cursor[0], dt, B)
+        t_cursor[0] = ivs[-1][3]
+        return interval_array(ivs)
+
+    for _ in range(args.warmup):
+        sensor.process_many(next_batch())
+    # ---- device-resident timed region (value)
+    batches = [next_batch() for _ in range(args.steps)]
+    stream = torch.cuda.ExternalStream(sensor.stream())
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sensor.reset_stats()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for b in batches:
+            sensor.enqueue(b)
+        stop.record(stream)
+        torch.cuda.synchronize()
+    dev_ms = start.elapsed_time(stop)
+    st = sensor.stats()
+    sensor.collect()  # the last batch's events (readout kept consistent)
+    rays = st["primary_rays"] + st["shadow_rays"]
+    # ---- end to end through the C-ABI with host buffers (e2e)
+    e2e_batches = [next_batch() for _ in range(args.steps)]
+    events_total, d2h = 0, 0
+    torch.cuda.synchronize()
+    sensor.reset_stats()
+    t0 = time.perf_counter()
+    for b in e2e_batches:
+        ev = sensor.process_many(b)
+        events_total += len(ev)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    st2 = sensor.stats()
+    rays2 = st2["primary_rays"] + st2["shadow_rays"]
+    gen2 = st2["events_generated"]
+    # max over ranks
+    vals = torch.tensor([dev_ms, e2e_s, rays, rays2, st2["events_delivered"]], dtype=torch.float64, device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+        mx = vals.clone()
+        dist.all_reduce(mx[:2], op=dist.ReduceOp.MAX)
+        sm = vals.clone()
+        dist.all_reduce(sm[2:], op=dist.ReduceOp.SUM)
+        vals = torch.cat([mx[:2], sm[2:]])
+    dev_ms, e2e_s, rays_all, rays2_all, delivered_all = vals.tolist()
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+    value = rays_all / (dev_ms / 1e3) / 1e6
+    e2e_value = rays2_all / e2e_s / 1e6
+    n_pix = w["camera"]["width"] * w["camera"]["height"]
+    optics_ms = st["optics_ms"] / max(1, st["optics_launches"])
+    # dominant kernel: trace_cells (optics).  Algorithmic bytes per launch: the
+    # per-pixel-cell radiance it must write (8 B) -- the HBM-minimal traffic of
+    # a latency/ALU-bound traversal; see the design doc for the accounting.
+    cells_per_launch = st["circuit_cells"] / max(1, st["circuit_launches"]) / max(1, n_pix)
+    alg_bytes = n_pix * cells_per_launch * 8.0
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (optics_ms / 1e3) / 1e9 if optics_ms > 0 else None
+    circuit_ms = st["circuit_ms"] / max(1, st["circuit_launches"])
+    circuit_bytes = n_pix * cells_per_launch * 8.0 + n_pix * (5 * 8 + 1 + 48) * 2 + n_pix * 4 * 2
+    cb = None
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline(args.workload, V, N, I, traj, w, budget_s=15.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": args.workload, "pixels": n_pix, "width": w["camera"]["width"],
+                   "height": w["camera"]["height"], "supersample": w["ss"], "terrain_grid": w["grid"],
+                   "triangles": int(info["triangles"]), "horizons_per_step": B, "time_resolution": dt,
+                   "circuit_step": PHYSIC["circuit_step"], "shot_noise": "curand_xorwow", "sun_elevation_deg":
+                   w["sun_elevation"], "intensity": w["intensity"], "l2": "inputs larger than L2 (scene %.1f GB)"
+                   % (info["device_bytes"] / 1e9), "parallelism": "dp%d (independent jobs)" % world,
+                   "bvh": "4-wide Morton radix, leaf %d, depth %d" % (args.leaf, info["depth"])},
+        "rays_per_step": rays / args.steps, "events_per_s": delivered_all / e2e_s,
+        "events_generated_per_step": gen2 / args.steps,
+        "e2e": {"value": e2e_value, "unit": "Mrays/s",
+                "h2d_bytes_per_step": B * 176, "d2h_bytes_per_step": int(events_total * 24 / args.steps)},
+        "gpu_launches": int(st["launches"]),
+        "kernel_ms": {"optics_per_launch": optics_ms, "circuit_per_launch": circuit_ms,
+                      "events_total": st["events_ms"]},
+        "roofline": {"bound": "hbm", "kernel": "trace_cells_kernel", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "peak_source": "measured" if peaks else "fallback",
+                     "note": "traversal is L1-broadcast/ALU bound; bytes = radiance written per launch"},
+        "roofline_circuit": {"bound": "hbm", "kernel": "circuit_kernel",
+                             "achieved": circuit_bytes / (circuit_ms / 1e3) / 1e9 if circuit_ms > 0 else None,
+                             "peak": peak, "unit": "GB/s"},
+        "clocks": clocks.summary(), "setup_s": setup_s, "bvh_build_s": info["build_seconds"],
+        "cpu_baseline": cb,
+    }
+    if line["roofline_circuit"]["achieved"]:
+        line["roofline_circuit"]["frac"] = line["roofline_circuit"]["achieved"] / peak
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="precision", choices=sorted(WORKLOADS))
+    ap.add_argument("--leaf", type=int, default=4)
+    ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--cw", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,167 @@
+"""ctypes binding of libdvs_gb300.so (the C-ABI in include/dvs_gb300.h).
+
+The library is built in-tree (dvsrender4deepspace_gb300/build.py).  Loading
+fails loudly when it is missing or has no CUDA device behind it: there is no
+CPU fallback for the hot path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libdvs_gb300.so")
+
+DVS_OK = 0
+DVS_ERR_CAPACITY = 1
+DVS_ERR_OPTICAL = 2
+DVS_ERR_INVALID = 3
+DVS_ERR_CUDA = 4
+DVS_ERR_STALLED = 5
+DVS_ERR_OUTPUT_SMALL = 6
+
+# Layout-identical to OpticalState / OpticalInterval / Event of the reference
+# (include/dvs/optical_sensor.hpp:148-153, include/dvs/dvs_base.hpp:9-18).
+STATE_DTYPE = np.dtype({"names": ["position", "velocity", "light", "light_rate", "rotation", "intensity",
+                                  "intensity_rate"],
+                        "formats": [("<f4", 3), ("<f4", 3), ("<f4", 3), ("<f4", 3), ("<f4", 4), "<f4", "<f4"],
+                        "offsets": [0, 12, 24, 36, 48, 64, 68], "itemsize": 80})
+INTERVAL_DTYPE = np.dtype({"names": ["start", "end", "t0", "t1"], "formats": [STATE_DTYPE, STATE_DTYPE, "<f8", "<f8"],
+                           "offsets": [0, 80, 160, 168], "itemsize": 176})
+EVENT_DTYPE = np.dtype([("timestamp", "<f8"), ("x", "<i2"), ("y", "<i2"), ("polarity", "i1"), ("depth", "<f4")])
+assert EVENT_DTYPE.itemsize == 17
+
+
+class Camera(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float)]
+
+
+HAPKE_KEYS = ("b", "c", "hS", "hC", "thetap", "w", "B_S0", "B_C0", "phi")
+
+
+class Hapke(C.Structure):
+    _fields_ = [(k, C.c_float) for k in HAPKE_KEYS]
+
+
+PHYSIC_FLOAT_FIELDS = ("threshold_pos", "threshold_neg", "refractory_time", "readout_bandwidth",
+                       "readout_latency", "threshold_std", "threshold_min", "wavelength_nm",
+                       "quantum_efficiency", "pixel_pitch_um", "fill_factor", "f_number",
+                       "lens_transmission", "radiance_scale", "temperature_k", "subthreshold_kappa",
+                       "receptor_capacitance_f", "reset_capacitance_f", "dark_current_a",
+                       "reset_leakage_a", "circuit_step")
+PHYSIC_INT_FIELDS = ("photon_shot_noise", "reset_thermal_noise", "random_seed", "max_events_per_step",
+                     "readout_queue_capacity")
+
+
+class Physic(C.Structure):
+    _fields_ = [(k, C.c_float) for k in PHYSIC_FLOAT_FIELDS] + [(k, C.c_int32) for k in PHYSIC_INT_FIELDS]
+
+
+class SensorOptions(C.Structure):
+    _fields_ = [("physic_effects", C.c_int32), ("aer_delay", C.c_int32), ("cells_per_chunk", C.c_int32),
+                ("cells_per_warp", C.c_int32), ("timing", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class BvhParams(C.Structure):
+    _fields_ = [("leaf_size", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("triangles", C.c_uint64), ("vertices", C.c_uint64), ("nodes", C.c_uint64), ("depth", C.c_int32),
+                ("root", C.c_int32), ("device_bytes", C.c_uint64), ("build_seconds", C.c_double)]
+
+
+class SensorStats(C.Structure):
+    _fields_ = [("primary_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("events_generated", C.c_uint64),
+                ("events_delivered", C.c_uint64), ("dropped", C.c_uint64), ("peak_queue", C.c_uint64),
+                ("circuit_cells", C.c_uint64), ("launches", C.c_uint64), ("optics_ms", C.c_double),
+                ("circuit_ms", C.c_double), ("events_ms", C.c_double), ("readout_ms", C.c_double),
+                ("optics_launches", C.c_uint64), ("circuit_launches", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# every symbol include/dvs_gb300.h declares
+EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_derive_parameters",
+           "dvs_scene_create", "dvs_scene_destroy", "dvs_scene_info_get", "dvs_cam_render", "dvs_sensor_create",
+           "dvs_sensor_destroy", "dvs_sensor_initialize", "dvs_sensor_process", "dvs_sensor_read",
+           "dvs_sensor_process_events", "dvs_sensor_enqueue", "dvs_sensor_collect", "dvs_sensor_drain", "dvs_sensor_stats_get", "dvs_sensor_stats_reset",
+           "dvs_sensor_stream", "dvs_sensor_read_state")
+
+_LIB = None
+
+
+def _declare(lib):
+    vp, sz, f_p = C.c_void_p, C.c_size_t, C.POINTER(C.c_float)
+    lib.dvs_last_error.restype = C.c_char_p
+    lib.dvs_version.restype = C.c_char_p
+    lib.dvs_sensor_options_default.argtypes = [C.POINTER(SensorOptions)]
+    lib.dvs_sensor_options_default.restype = None
+    lib.dvs_derive_parameters.argtypes = [C.POINTER(Physic), C.c_int32, C.POINTER(C.c_double)]
+    lib.dvs_scene_create.argtypes = [f_p, f_p, C.POINTER(C.c_uint32), f_p, sz, sz, C.POINTER(Camera), C.c_int32,
+                                     C.POINTER(Hapke), C.POINTER(BvhParams), C.POINTER(vp)]
+    lib.dvs_scene_destroy.argtypes = [vp]
+    lib.dvs_scene_info_get.argtypes = [vp, C.POINTER(SceneInfo)]
+    lib.dvs_cam_render.argtypes = [vp, vp, f_p, f_p]
+    lib.dvs_sensor_create.argtypes = [vp, C.POINTER(Physic), C.POINTER(SensorOptions), C.POINTER(vp)]
+    lib.dvs_sensor_destroy.argtypes = [vp]
+    lib.dvs_sensor_initialize.argtypes = [vp, vp, C.c_double]
+    lib.dvs_sensor_process.argtypes = [vp, vp, sz, C.POINTER(sz)]
+    lib.dvs_sensor_read.argtypes = [vp, vp, sz, C.POINTER(sz)]
+    lib.dvs_sensor_process_events.argtypes = [vp, vp, sz, vp, sz, C.POINTER(sz)]
+    lib.dvs_sensor_drain.argtypes = [vp, vp, sz, C.POINTER(sz)]
+    lib.dvs_sensor_enqueue.argtypes = [vp, vp, sz]
+    lib.dvs_sensor_collect.argtypes = [vp, C.POINTER(sz)]
+    lib.dvs_sensor_stats_get.argtypes = [vp, C.POINTER(SensorStats)]
+    lib.dvs_sensor_stats_reset.argtypes = [vp]
+    lib.dvs_sensor_stream.argtypes = [vp]
+    lib.dvs_sensor_stream.restype = vp
+    lib.dvs_sensor_read_state.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+    return lib
+
+
+def library_path():
+    return LIB_PATH
+
+
+def load(build_if_missing=True):
+    """Open the C-ABI library, building it first if it is absent."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            if not build_if_missing:
+                raise OSError("libdvs_gb300.so is not built; run dvsrender4deepspace_gb300.build")
+            from . import build
+            build.build()
+        _LIB = _declare(C.CDLL(LIB_PATH))
+    return _LIB
+
+
+class DvsError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(message)
+        self.code = code
+
+
+class CapacityError(DvsError):
+    pass
+
+
+class OpticalError(DvsError):
+    pass
+
+
+def check(status):
+    if status == DVS_OK:
+        return
+    msg = load().dvs_last_error().decode(errors="replace")
+    if status == DVS_ERR_CAPACITY:
+        raise CapacityError(status, msg)
+    if status == DVS_ERR_OPTICAL:
+        raise OpticalError(status, msg)
+    if status == DVS_ERR_INVALID:
+        err = DvsError(status, msg)
+        raise ValueError(msg) from err
+    raise DvsError(status, msg)

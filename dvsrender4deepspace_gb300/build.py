@@ -1,0 +1,85 @@
+"""Builds libdvs_gb300.so in-tree for sm_103a.
+
+Four translation units compile in parallel (two CUDA, two host C++) and link
+into one shared library exposing the C-ABI declared in include/dvs_gb300.h.
+Host code and device code are both compiled without floating-point
+contraction so that every expression rounds as written.
+
+    python -m dvsrender4deepspace_gb300.build        (or build() from Python)
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OUT_DIR = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libdvs_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HOST_FLAGS = ["-O3", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c++17", "-Wall", "-Wno-unused-function"]
+
+
+def nvcc():
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    path = os.path.join(cuda, "bin", "nvcc")
+    return path if os.path.exists(path) else (shutil.which("nvcc") or "nvcc")
+
+
+def _sources():
+    return [os.path.join(CSRC, f) for f in ("kernels.cu", "capi.cu", "bvh4_build.cpp", "readout.cpp")]
+
+
+def _headers():
+    return [os.path.join(CSRC, f) for f in ("kernels.h", "dvs_internal.h")] + [
+        os.path.join(ROOT, "include", "dvs_gb300.h")]
+
+
+def up_to_date():
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(p) <= t for p in _sources() + _headers() + [__file__])
+
+
+def build(force=False, verbose=False):
+    """Compile the library unless it is newer than every source."""
+    if not force and up_to_date():
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    inc = ["-I", CSRC, "-I", os.path.join(ROOT, "include")]
+    xhost = ",".join(HOST_FLAGS)
+    cmds = []
+    for src in _sources():
+        obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
+        if src.endswith(".cu"):
+            cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-Xcompiler", xhost, *inc,
+                   "-c", src, "-o", obj]
+        else:
+            cmd = [os.environ.get("CXX", "g++"), *HOST_FLAGS, *inc, "-I",
+                   os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include"), "-c", src, "-o", obj]
+        cmds.append((cmd, obj))
+    procs = [(subprocess.Popen(c, stdout=subprocess.PIPE, stderr=subprocess.STDOUT), c, o) for c, o in cmds]
+    failed = []
+    for p, c, o in procs:
+        out = p.communicate()[0].decode(errors="replace")
+        if p.returncode != 0:
+            failed.append((" ".join(c), out))
+        elif verbose and out.strip():
+            print(out)
+    if failed:
+        msg = "\n\n".join("%s\n%s" % f for f in failed)
+        raise RuntimeError("building libdvs_gb300.so failed:\n" + msg)
+    tmp = LIB + ".tmp"
+    link = [nvcc(), *ARCH, "-shared", "-o", tmp, *[o for _, o in cmds], "-Xcompiler", "-fopenmp", "-lgomp"]
+    r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("linking libdvs_gb300.so failed:\n" + r.stdout.decode(errors="replace"))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)
+    print(LIB)

@@ -1,0 +1,307 @@
+// Host builder of the 4-wide BVH.
+//
+// Replaces the reference's single-threaded recursive binned-SAH builder
+// (src/bvh/build.cpp:27-174, src/bvh/bining.cpp:9-182).  Design:
+//   1. triangle centroids -> 63-bit Morton codes on one uniform grid (so a
+//      flat terrain splits on x/y first, not on its thin z range);
+//   2. parallel LSD radix sort of (code, triangle);
+//   3. top-down radix splits at the highest differing code bit, giving a
+//      binary tree over contiguous leaf ranges (<= leaf_size triangles);
+//   4. collapse to 4-wide nodes by repeatedly opening the largest-area inner
+//      child; nodes are numbered breadth-first so the top levels are first.
+// All passes are O(n) or O(n log n) and OpenMP-parallel.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "dvs_internal.h"
+
+namespace dvsgb {
+namespace {
+
+struct Box {
+  float lo[3], hi[3];
+};
+inline Box empty_box() {
+  const float inf = std::numeric_limits<float>::infinity();
+  return Box{{inf, inf, inf}, {-inf, -inf, -inf}};
+}
+inline void grow(Box &b, const Box &o) {
+  for (int d = 0; d < 3; ++d) {
+    b.lo[d] = std::min(b.lo[d], o.lo[d]);
+    b.hi[d] = std::max(b.hi[d], o.hi[d]);
+  }
+}
+inline float half_area(const Box &b) {
+  float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+
+// Spreads the low 21 bits of v so that two zero bits separate each.
+inline uint64_t spread21(uint64_t v) {
+  v &= 0x1fffffull;
+  v = (v | (v << 32)) & 0x001f00000000ffffull;
+  v = (v | (v << 16)) & 0x001f0000ff0000ffull;
+  v = (v | (v << 8)) & 0x100f00f00f00f00full;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
+
+int thread_count() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+// LSD radix sort of 64-bit keys with 32-bit payloads, 11-bit digits.
+void radix_sort(std::vector<uint64_t> &keys, std::vector<uint32_t> &vals) {
+  const size_t n = keys.size();
+  std::vector<uint64_t> k2(n);
+  std::vector<uint32_t> v2(n);
+  const int bits = 11, buckets = 1 << bits;
+  const int nt = std::max(1, std::min(thread_count(), int(n / 65536) + 1));
+  std::vector<size_t> hist((size_t)nt * buckets);
+  uint64_t all_or = 0, all_and = ~0ull;
+  for (size_t i = 0; i < n; ++i) { all_or |= keys[i]; all_and &= keys[i]; }
+  for (int shift = 0; shift < 64; shift += bits) {
+    const uint64_t digit_mask = (uint64_t(buckets) - 1) << shift;
+    if (((all_or ^ all_and) & digit_mask) == 0) continue;  // digit identical everywhere
+    std::fill(hist.begin(), hist.end(), 0);
+#pragma omp parallel num_threads(nt)
+    {
+#ifdef _OPENMP
+      const int t = omp_get_thread_num();
+#else
+      const int t = 0;
+#endif
+      const size_t b = n * t / nt, e = n * (t + 1) / nt;
+      size_t *h = &hist[(size_t)t * buckets];
+      for (size_t i = b; i < e; ++i) h[(keys[i] >> shift) & (buckets - 1)]++;
+#pragma omp barrier
+#pragma omp single
+      {
+        size_t sum = 0;
+        for (int d = 0; d < buckets; ++d)
+          for (int tt = 0; tt < nt; ++tt) {
+            size_t c = hist[(size_t)tt * buckets + d];
+            hist[(size_t)tt * buckets + d] = sum;
+            sum += c;
+          }
+      }
+      for (size_t i = b; i < e; ++i) {
+        size_t pos = h[(keys[i] >> shift) & (buckets - 1)]++;
+        k2[pos] = keys[i];
+        v2[pos] = vals[i];
+      }
+    }
+    keys.swap(k2);
+    vals.swap(v2);
+  }
+}
+
+struct BinNode {
+  Box box;
+  int32_t left, right;  // -1 for leaves
+  int32_t start, count;
+  float area;
+};
+
+struct TreeBuilder {
+  const std::vector<uint64_t> &codes;
+  const std::vector<Box> &tri_boxes;  // in sorted order
+  std::vector<BinNode> &nodes;
+  std::atomic<int32_t> next{0};
+  int leaf_size;
+
+  int32_t build(int32_t b, int32_t e) {
+    const int32_t id = next.fetch_add(1);
+    BinNode &n = nodes[id];
+    if (e - b <= leaf_size) {
+      Box box = empty_box();
+      for (int32_t i = b; i < e; ++i) grow(box, tri_boxes[i]);
+      n.box = box;
+      n.left = n.right = -1;
+      n.start = b;
+      n.count = e - b;
+      n.area = half_area(box);
+      return id;
+    }
+    int32_t m;
+    const uint64_t a = codes[b], z = codes[e - 1];
+    if (a == z) {
+      m = b + (e - b) / 2;
+    } else {
+      const int h = 63 - __builtin_clzll(a ^ z);
+      // first index in [b, e) whose bit h is set (codes are sorted)
+      int32_t lo = b, hi = e - 1;
+      while (lo < hi) {
+        int32_t mid = lo + (hi - lo) / 2;
+        if ((codes[mid] >> h) & 1) hi = mid; else lo = mid + 1;
+      }
+      m = lo;
+    }
+    int32_t l, r;
+    if (e - b > 32768) {
+#pragma omp task shared(l)
+      l = build(b, m);
+#pragma omp task shared(r)
+      r = build(m, e);
+#pragma omp taskwait
+    } else {
+      l = build(b, m);
+      r = build(m, e);
+    }
+    BinNode &nn = nodes[id];
+    nn.box = nodes[l].box;
+    grow(nn.box, nodes[r].box);
+    nn.left = l;
+    nn.right = r;
+    nn.start = 0;
+    nn.count = 0;
+    nn.area = half_area(nn.box);
+    return id;
+  }
+};
+
+}  // namespace
+
+bool build_bvh4(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf_size, Bvh4Build &out,
+                std::string &error) {
+  const auto t_start = std::chrono::steady_clock::now();
+  if (nt == 0 || nv == 0) { error = "empty mesh"; return false; }
+  if (nt > (size_t(1) << 28)) { error = "mesh exceeds 2^28 triangles"; return false; }
+  if (leaf_size < 1 || leaf_size > 8) { error = "leaf_size must be 1..8"; return false; }
+  for (size_t i = 0; i < 3 * nt; ++i)
+    if (I[i] >= nv) { error = "mesh triangle index outside vertex array"; return false; }
+
+  // 1. bounds and Morton codes
+  std::vector<Box> boxes(nt);
+  Box scene = empty_box();
+  const long long ntl = (long long)nt;
+#pragma omp parallel
+  {
+    Box local = empty_box();
+#pragma omp for schedule(static)
+    for (long long i = 0; i < ntl; ++i) {
+      Box b = empty_box();
+      for (int k = 0; k < 3; ++k) {
+        const float *p = V + 3 * (size_t)I[3 * i + k];
+        for (int d = 0; d < 3; ++d) { b.lo[d] = std::min(b.lo[d], p[d]); b.hi[d] = std::max(b.hi[d], p[d]); }
+      }
+      boxes[i] = b;
+      Box c;
+      for (int d = 0; d < 3; ++d) c.lo[d] = c.hi[d] = 0.5f * (b.lo[d] + b.hi[d]);
+      grow(local, c);
+    }
+#pragma omp critical
+    grow(scene, local);
+  }
+  float extent = std::max({scene.hi[0] - scene.lo[0], scene.hi[1] - scene.lo[1], scene.hi[2] - scene.lo[2]});
+  if (!(extent > 0) || !std::isfinite(extent)) extent = 1.0f;
+  const double scale = double((1u << 21) - 1) / double(extent);
+  std::vector<uint64_t> codes(nt);
+  std::vector<uint32_t> order(nt);
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < ntl; ++i) {
+    uint64_t q[3];
+    for (int d = 0; d < 3; ++d) {
+      double c = 0.5 * (double(boxes[i].lo[d]) + double(boxes[i].hi[d]));
+      double v = (c - scene.lo[d]) * scale;
+      v = std::min(std::max(v, 0.0), double((1u << 21) - 1));
+      q[d] = uint64_t(v);
+    }
+    codes[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+    order[i] = uint32_t(i);
+  }
+
+  // 2. sort
+  radix_sort(codes, order);
+  std::vector<Box> sorted_boxes(nt);
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < ntl; ++i) sorted_boxes[i] = boxes[order[i]];
+  std::vector<Box>().swap(boxes);
+
+  // 3. binary radix tree
+  std::vector<BinNode> bin(2 * nt + 1);
+  TreeBuilder tb{codes, sorted_boxes, bin, {}, leaf_size};
+  int32_t root = 0;
+#pragma omp parallel
+#pragma omp single
+  root = tb.build(0, (int32_t)nt);
+  bin.resize(tb.next.load());
+
+  // 4. collapse to 4-wide, breadth first
+  std::vector<Bvh4Node> nodes;
+  nodes.reserve(bin.size() / 2 + 2);
+  std::vector<int32_t> queue;  // binary node per 4-wide node
+  std::vector<int32_t> level;
+  queue.push_back(root);
+  level.push_back(1);
+  int depth = 1;
+  for (size_t qi = 0; qi < queue.size(); ++qi) {
+    const int32_t b = queue[qi];
+    int32_t kids[4];
+    int nk = 0;
+    if (bin[b].count > 0) {
+      kids[nk++] = b;  // a leaf root: one leaf child
+    } else {
+      kids[nk++] = bin[b].left;
+      kids[nk++] = bin[b].right;
+      while (nk < 4) {
+        int best = -1;
+        float best_area = -1;
+        for (int k = 0; k < nk; ++k)
+          if (bin[kids[k]].count == 0 && bin[kids[k]].area > best_area) { best = k; best_area = bin[kids[k]].area; }
+        if (best < 0) break;
+        const int32_t open = kids[best];
+        kids[best] = bin[open].left;
+        kids[nk++] = bin[open].right;
+      }
+    }
+    Bvh4Node node;
+    std::memset(&node, 0, sizeof(node));
+    for (int k = 0; k < 4; ++k) {
+      if (k >= nk) {
+        node.child[k] = -1;
+        node.count[k] = -1;
+        continue;
+      }
+      const BinNode &c = bin[kids[k]];
+      node.lo_x[k] = c.box.lo[0]; node.hi_x[k] = c.box.hi[0];
+      node.lo_y[k] = c.box.lo[1]; node.hi_y[k] = c.box.hi[1];
+      node.lo_z[k] = c.box.lo[2]; node.hi_z[k] = c.box.hi[2];
+      if (c.count > 0) {
+        node.child[k] = c.start;
+        node.count[k] = c.count;
+      } else {
+        node.child[k] = (int32_t)queue.size();
+        node.count[k] = 0;
+        queue.push_back(kids[k]);
+        level.push_back(level[qi] + 1);
+        depth = std::max(depth, level[qi] + 1);
+      }
+    }
+    nodes.push_back(node);
+  }
+  if (3 * depth + 1 > kStackSlots) {
+    error = "BVH too deep for the traversal stack (depth " + std::to_string(depth) + ")";
+    return false;
+  }
+  out.nodes.swap(nodes);
+  out.order.swap(order);
+  out.depth = depth;
+  out.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  return true;
+}
+
+}  // namespace dvsgb

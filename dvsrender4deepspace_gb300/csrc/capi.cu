@@ -1,0 +1,798 @@
+// Host orchestration and C-ABI of the GB300 DVS path.
+//
+// dvs_scene  replaces BVHBuilder::build + DeviceScene (src/bvh/build.cpp:27-76,
+//            src/cuda/device_scene.cu:15-37): one device arena holds the
+//            4-wide BVH, the leaf-order triangle and shading records and the
+//            Morton pixel order.
+// dvs_sensor replaces EventSensor (src/cuda/event_sensor.cu:244-305): circuit
+//            state in structure-of-arrays form, cuRAND XORWOW per pixel,
+//            per-pixel event slabs, and the optics -> circuit chunk pipeline.
+// Readout follows EventReadout (src/event_readout.cpp:6-34) on the host.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "dvs_gb300.h"
+#include "kernels.h"
+
+using namespace dvsgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr, what)                                                            \
+  do {                                                                                  \
+    cudaError_t e__ = (expr);                                                           \
+    if (e__ != cudaSuccess)                                                             \
+      return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in ") + (what) + " : " +      \
+                                    cudaGetErrorString(e__));                           \
+  } while (0)
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// parameters() and photo_parameters() (src/cuda/event_sensor.cu:151-176),
+// with the compile-time switch ENABLE_PHYSIC_EFFECTS as a runtime flag.
+void derive(const dvs_physic &c, bool effects, PixelParams &p, PhotoParams &photo) {
+  const double q = 1.602176634e-19, k = 1.380649e-23, h = 6.62607015e-34, cl = 299792458;
+  p.threshold_pos = c.threshold_pos;
+  p.threshold_neg = c.threshold_neg;
+  const double voltage = k * c.temperature_k / (q * c.subthreshold_kappa);
+  p.charge_scale = c.receptor_capacitance_f * voltage / q;
+  p.reference_leak = 0;
+  p.reset_noise_std = 0;
+  if (effects) {
+    p.refractory_time = c.refractory_time;
+    p.reference_leak = c.reset_leakage_a / (c.reset_capacitance_f * voltage);
+    p.reset_noise_std = c.reset_thermal_noise ? std::sqrt(k * c.temperature_k / c.reset_capacitance_f) / voltage : 0;
+  } else {
+    p.refractory_time = 0;
+  }
+  const double pitch = c.pixel_pitch_um * 1e-6;
+  const float fnum2 = 4 * c.f_number * c.f_number;  // float product, as event_sensor.cu:167
+  photo.electrons_per_radiance = c.radiance_scale * 3.141592653589793 / fnum2 * c.lens_transmission * pitch * pitch *
+                                 c.fill_factor * c.quantum_efficiency * (c.wavelength_nm * 1e-9) / (h * cl);
+  photo.integration_step = c.circuit_step;
+  if (effects) {
+    photo.dark_electrons = c.dark_current_a / q;
+    photo.shot_noise = c.photon_shot_noise;
+  } else {
+    photo.dark_electrons = 0;
+    photo.shot_noise = 0;
+  }
+}
+
+float material_albedo(float value, float fallback) {  // device_optics.cuh:30-33
+  return std::isfinite(value) && value >= 0 && value <= 1 ? value : fallback;
+}
+
+// Morton order of the image pixels: consecutive ranks form compact 2-D tiles.
+std::vector<int32_t> morton_pixel_order(int w, int h) {
+  auto part = [](uint32_t v) {
+    v &= 0xffff;
+    v = (v | (v << 8)) & 0x00ff00ff;
+    v = (v | (v << 4)) & 0x0f0f0f0f;
+    v = (v | (v << 2)) & 0x33333333;
+    v = (v | (v << 1)) & 0x55555555;
+    return v;
+  };
+  std::vector<std::pair<uint32_t, int32_t>> keys((size_t)w * h);
+  for (int y = 0; y < h; ++y)
+    for (int x = 0; x < w; ++x) keys[(size_t)y * w + x] = {part(x) | (part(y) << 1), y * w + x};
+  std::sort(keys.begin(), keys.end());
+  std::vector<int32_t> order(keys.size());
+  for (size_t i = 0; i < keys.size(); ++i) order[i] = keys[i].second;
+  return order;
+}
+
+template <class T>
+cudaError_t grow_device(T *&ptr, size_t &cap, size_t need) {
+  if (need <= cap) return cudaSuccess;
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc(&ptr, sizeof(T) * need);
+  if (e == cudaSuccess) cap = need;
+  return e;
+}
+template <class T>
+cudaError_t grow_pinned(T *&ptr, size_t &cap, size_t need) {
+  if (need <= cap) return cudaSuccess;
+  if (ptr) cudaFreeHost(ptr);
+  ptr = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMallocHost(&ptr, sizeof(T) * std::max<size_t>(need, 1));
+  if (e == cudaSuccess) cap = need;
+  return e;
+}
+
+}  // namespace
+
+// ---- handles --------------------------------------------------------------------
+struct dvs_scene {
+  int device = 0;
+  dvs_camera camera{};
+  int samples = 1;
+  dvs_hapke hapke{};
+  bool has_albedo = false;
+  void *arena = nullptr;
+  size_t arena_bytes = 0;
+  Bvh4Node *nodes = nullptr;
+  TriRecord *tris = nullptr;
+  ShadeRecord *shade = nullptr;
+  int32_t *pixel_of_rank = nullptr;
+  size_t n_nodes = 0, n_tris = 0, n_vertices = 0;
+  int depth = 0;
+  double build_seconds = 0;
+  // camera render buffers
+  cudaStream_t stream = nullptr;
+  double *cam_radiance = nullptr;
+  float *cam_depth = nullptr, *cam_image = nullptr, *cam_depth_image = nullptr;
+  CellPose *cam_pose = nullptr;
+  dvs_optical_state *cam_state = nullptr;
+  dvs_optical_state *h_state = nullptr;
+
+  SceneView view() const {
+    SceneView v;
+    v.nodes = nodes;
+    v.tris = tris;
+    v.shade = shade;
+    v.pixel_of_rank = pixel_of_rank;
+    v.width = camera.width;
+    v.height = camera.height;
+    v.samples = samples;
+    v.has_albedo = has_albedo ? 1 : 0;
+    v.fx = camera.fx;
+    v.fy = camera.fy;
+    v.cx = camera.cx;
+    v.cy = camera.cy;
+    v.hapke = hapke;
+    return v;
+  }
+  int pixels() const { return camera.width * camera.height; }
+};
+
+struct dvs_sensor {
+  dvs_scene *scene = nullptr;
+  int device = 0;
+  dvs_physic physic{};
+  dvs_sensor_options opt{};
+  PixelParams p{};
+  PhotoParams photo{};
+  double threshold_std = 0, threshold_min = 0;
+  int max_events = 16;
+  unsigned seed = 0;
+  Readout *readout = nullptr;
+  bool initialized = false;
+  double last_time = 0;
+  bool pending = false;  // an enqueued batch awaits collect
+  double pending_end = 0;
+  cudaStream_t stream = nullptr;
+  // device state
+  CircuitState st{};
+  int32_t *ev_count = nullptr, *error_word = nullptr, *event_total = nullptr;
+  double *slab_t = nullptr;
+  int8_t *slab_p = nullptr;
+  DevEvent *events = nullptr;
+  unsigned long long *counters = nullptr;
+  double *radiance = nullptr;
+  size_t radiance_cap = 0;
+  dvs_optical_interval *ivs = nullptr;
+  size_t ivs_cap = 0;
+  Cell *cells = nullptr;
+  size_t cells_cap = 0;
+  CellPose *poses = nullptr;
+  size_t poses_cap = 0;
+  dvs_optical_state *d_state = nullptr;
+  // pinned staging
+  dvs_optical_interval *h_ivs = nullptr;
+  size_t h_ivs_cap = 0;
+  Cell *h_cells = nullptr;
+  size_t h_cells_cap = 0;
+  DevEvent *h_events = nullptr;
+  size_t h_events_cap = 0;
+  int32_t *h_status = nullptr;  // [event_total, error]
+  dvs_optical_state *h_state = nullptr;
+  // results
+  std::vector<HostEvent> ready;
+  size_t ready_head = 0;
+  dvs_sensor_stats stats{};
+  // timing
+  std::vector<cudaEvent_t> timers;
+  size_t timers_used = 0;
+  std::vector<int> timer_kind;  // 0 optics, 1 circuit, 2 events
+};
+
+extern "C" {
+
+const char *dvs_last_error(void) { return g_last_error.c_str(); }
+const char *dvs_version(void) { return "dvs_gb300 1.0 (sm_103a)"; }
+
+void dvs_sensor_options_default(dvs_sensor_options *out) {
+  if (!out) return;
+  std::memset(out, 0, sizeof(*out));
+  out->physic_effects = 1;
+  out->aer_delay = 1;
+}
+
+int dvs_derive_parameters(const dvs_physic *physic, int32_t physic_effects, double *out9) {
+  if (!physic || !out9) return fail(DVS_ERR_INVALID, "null argument");
+  PixelParams p;
+  PhotoParams ph;
+  derive(*physic, physic_effects != 0, p, ph);
+  const double v[9] = {p.threshold_pos, p.threshold_neg, p.charge_scale, p.refractory_time, p.reference_leak,
+                       p.reset_noise_std, ph.electrons_per_radiance, ph.dark_electrons, ph.integration_step};
+  std::memcpy(out9, v, sizeof(v));
+  return DVS_OK;
+}
+
+// ---- scene ----------------------------------------------------------------------
+int dvs_scene_create(const float *vertices, const float *normals, const uint32_t *indices, const float *albedos,
+                     size_t n_vertices, size_t n_triangles, const dvs_camera *camera, int32_t supersample,
+                     const dvs_hapke *hapke, const dvs_bvh_params *params, dvs_scene **out) {
+  if (!out) return fail(DVS_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (!vertices || !normals || !indices || !camera || !hapke || n_vertices == 0 || n_triangles == 0)
+    return fail(DVS_ERR_INVALID, "invalid indexed mesh/BVH/material dimensions");
+  if (camera->width <= 0 || camera->height <= 0 || camera->width > 32767 || camera->height > 32767 ||
+      !(camera->fx > 0) || !(camera->fy > 0) || !std::isfinite(camera->cx) || !std::isfinite(camera->cy))
+    return fail(DVS_ERR_INVALID, "invalid scene or camera range");
+  if (supersample < 1 || supersample > 64 ||
+      double(camera->width) * camera->height * supersample * supersample > std::numeric_limits<int>::max())
+    return fail(DVS_ERR_INVALID, "too many aperture samples");
+  for (size_t i = 0; i < 3 * n_vertices; ++i)
+    if (!std::isfinite(vertices[i])) return fail(DVS_ERR_INVALID, "nonfinite mesh vertex");
+  for (size_t i = 0; i < 3 * n_vertices; ++i)
+    if (!std::isfinite(normals[i])) return fail(DVS_ERR_INVALID, "nonfinite mesh normal");
+  const int leaf = params && params->leaf_size > 0 ? params->leaf_size : 4;
+
+  Bvh4Build bvh;
+  std::string err;
+  if (!build_bvh4(vertices, n_vertices, indices, n_triangles, leaf, bvh, err)) return fail(DVS_ERR_INVALID, err);
+
+  // leaf-order records
+  std::vector<TriRecord> tris(n_triangles);
+  std::vector<ShadeRecord> shade(n_triangles);
+  const long long nt = (long long)n_triangles;
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < nt; ++i) {
+    const uint32_t src = bvh.order[i];
+    const uint32_t a = indices[3 * (size_t)src], b = indices[3 * (size_t)src + 1], c = indices[3 * (size_t)src + 2];
+    TriRecord &t = tris[i];
+    std::memset(&t, 0, sizeof(t));
+    for (int d = 0; d < 3; ++d) {
+      t.v0[d] = vertices[3 * (size_t)a + d];
+      t.e1[d] = vertices[3 * (size_t)b + d] - vertices[3 * (size_t)a + d];
+      t.e2[d] = vertices[3 * (size_t)c + d] - vertices[3 * (size_t)a + d];
+    }
+    t.original = src;
+    ShadeRecord &s = shade[i];
+    std::memset(&s, 0, sizeof(s));
+    for (int d = 0; d < 3; ++d) {
+      s.n0[d] = normals[3 * (size_t)a + d];
+      s.n1[d] = normals[3 * (size_t)b + d];
+      s.n2[d] = normals[3 * (size_t)c + d];
+    }
+    if (albedos) {
+      s.a0 = material_albedo(albedos[a], hapke->w);
+      s.a1 = material_albedo(albedos[b], hapke->w);
+      s.a2 = material_albedo(albedos[c], hapke->w);
+    }
+  }
+  const std::vector<int32_t> order = morton_pixel_order(camera->width, camera->height);
+
+  dvs_scene *s = new dvs_scene;
+  s->camera = *camera;
+  s->samples = supersample;
+  s->hapke = *hapke;
+  s->has_albedo = albedos != nullptr;
+  s->n_nodes = bvh.nodes.size();
+  s->n_tris = n_triangles;
+  s->n_vertices = n_vertices;
+  s->depth = bvh.depth;
+  s->build_seconds = bvh.seconds;
+  cudaGetDevice(&s->device);
+  const size_t off_nodes = 0;
+  const size_t off_tris = align_up(off_nodes + sizeof(Bvh4Node) * s->n_nodes, 256);
+  const size_t off_shade = align_up(off_tris + sizeof(TriRecord) * n_triangles, 256);
+  const size_t off_pix = align_up(off_shade + sizeof(ShadeRecord) * n_triangles, 256);
+  const size_t total = align_up(off_pix + sizeof(int32_t) * order.size(), 256);
+  cudaError_t e = cudaMalloc(&s->arena, total);
+  if (e != cudaSuccess) {
+    delete s;
+    return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in allocate scene arena : ") + cudaGetErrorString(e));
+  }
+  s->arena_bytes = total;
+  char *base = static_cast<char *>(s->arena);
+  s->nodes = reinterpret_cast<Bvh4Node *>(base + off_nodes);
+  s->tris = reinterpret_cast<TriRecord *>(base + off_tris);
+  s->shade = reinterpret_cast<ShadeRecord *>(base + off_shade);
+  s->pixel_of_rank = reinterpret_cast<int32_t *>(base + off_pix);
+  e = cudaMemcpy(s->nodes, bvh.nodes.data(), sizeof(Bvh4Node) * s->n_nodes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(s->tris, tris.data(), sizeof(TriRecord) * n_triangles, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(s->shade, shade.data(), sizeof(ShadeRecord) * n_triangles, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(s->pixel_of_rank, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    dvs_scene_destroy(s);
+    return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in upload scene array : ") + cudaGetErrorString(e));
+  }
+  *out = s;
+  return DVS_OK;
+}
+
+int dvs_scene_destroy(dvs_scene *s) {
+  if (!s) return DVS_OK;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  cudaFree(s->cam_radiance);
+  cudaFree(s->cam_depth);
+  cudaFree(s->cam_image);
+  cudaFree(s->cam_depth_image);
+  cudaFree(s->cam_pose);
+  cudaFree(s->cam_state);
+  if (s->h_state) cudaFreeHost(s->h_state);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  cudaFree(s->arena);
+  delete s;
+  return DVS_OK;
+}
+
+int dvs_scene_info_get(const dvs_scene *s, dvs_scene_info *out) {
+  if (!s || !out) return fail(DVS_ERR_INVALID, "null argument");
+  out->triangles = s->n_tris;
+  out->vertices = s->n_vertices;
+  out->nodes = s->n_nodes;
+  out->depth = s->depth;
+  out->root = 0;
+  out->device_bytes = s->arena_bytes;
+  out->build_seconds = s->build_seconds;
+  return DVS_OK;
+}
+
+int dvs_cam_render(dvs_scene *s, const dvs_optical_state *pose, float *radiance, float *depth) {
+  if (!s || !pose || !radiance) return fail(DVS_ERR_INVALID, "invalid parallel optical request");
+  CUDA_TRY(cudaSetDevice(s->device), "select device");
+  const int n = s->pixels();
+  if (!s->cam_radiance) {
+    CUDA_TRY(cudaMalloc(&s->cam_radiance, sizeof(double) * n), "allocate optical values");
+    CUDA_TRY(cudaMalloc(&s->cam_depth, sizeof(float) * n), "allocate optical depth");
+    CUDA_TRY(cudaMalloc(&s->cam_image, sizeof(float) * n), "allocate image");
+    CUDA_TRY(cudaMalloc(&s->cam_depth_image, sizeof(float) * n), "allocate depth image");
+    CUDA_TRY(cudaMalloc(&s->cam_pose, sizeof(CellPose)), "allocate optical pose");
+    CUDA_TRY(cudaMalloc(&s->cam_state, sizeof(dvs_optical_state)), "allocate optical state");
+    CUDA_TRY(cudaMallocHost(&s->h_state, sizeof(dvs_optical_state)), "allocate pose staging");
+  }
+  *s->h_state = *pose;
+  CUDA_TRY(cudaMemcpyAsync(s->cam_state, s->h_state, sizeof(dvs_optical_state), cudaMemcpyHostToDevice, s->stream),
+           "upload optical poses");
+  CUDA_TRY(launch_pose_from_state(s->cam_state, s->cam_pose, s->stream), "pose");
+  CUDA_TRY(launch_trace_cells(s->view(), n, s->cam_pose, 0, 1, 0, s->cam_radiance, s->cam_depth, nullptr, s->stream),
+           "parallel optical launch");
+  CUDA_TRY(launch_radiance_to_float(n, s->pixel_of_rank, s->cam_radiance, s->cam_depth, s->cam_image,
+                                    s->cam_depth_image, s->stream),
+           "image layout");
+  CUDA_TRY(cudaMemcpyAsync(radiance, s->cam_image, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream),
+           "download optical values");
+  if (depth)
+    CUDA_TRY(cudaMemcpyAsync(depth, s->cam_depth_image, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream),
+             "download optical depth");
+  CUDA_TRY(cudaStreamSynchronize(s->stream), "parallel optical status");
+  for (int i = 0; i < n; ++i)
+    if (!std::isfinite(radiance[i])) return fail(DVS_ERR_OPTICAL, "invalid optical sample/BVH stack overflow");
+  return DVS_OK;
+}
+
+// ---- sensor ---------------------------------------------------------------------
+int dvs_sensor_destroy(dvs_sensor *s);
+
+int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sensor_options *options,
+                      dvs_sensor **out) {
+  if (!out) return fail(DVS_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (!scene || !physic) return fail(DVS_ERR_INVALID, "null scene or physic configuration");
+  const int n = scene->pixels();
+  if (physic->max_events_per_step < 1 || physic->max_events_per_step > 64 ||
+      (long long)n * physic->max_events_per_step > std::numeric_limits<int>::max())
+    return fail(DVS_ERR_INVALID, "invalid sensor capacity");
+  if (!(physic->circuit_step > 0)) return fail(DVS_ERR_INVALID, "invalid optical/circuit model parameter range");
+  dvs_sensor *s = new dvs_sensor;
+  s->scene = scene;
+  s->physic = *physic;
+  if (options) s->opt = *options; else dvs_sensor_options_default(&s->opt);
+  derive(*physic, s->opt.physic_effects != 0, s->p, s->photo);
+  s->threshold_std = s->opt.physic_effects ? physic->threshold_std : 0;
+  s->threshold_min = physic->threshold_min;
+  s->max_events = physic->max_events_per_step;
+  s->seed = (unsigned)physic->random_seed;
+  s->readout = new Readout(s->opt.aer_delay ? (double)physic->readout_bandwidth : 0,
+                           s->opt.aer_delay ? (double)physic->readout_latency : 0,
+                           (size_t)std::max(1, physic->readout_queue_capacity));
+  cudaGetDevice(&s->device);
+  auto bail = [&](cudaError_t e, const char *what) {
+    dvs_sensor_destroy(s);
+    return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in ") + what + " : " + cudaGetErrorString(e));
+  };
+  cudaError_t e;
+#define ALLOC(ptr, bytes, what)                 \
+  if ((e = cudaMalloc(&(ptr), (bytes))) != cudaSuccess) return bail(e, what);
+  ALLOC(s->st.receptor_log, sizeof(double) * n, "pixel states");
+  ALLOC(s->st.reference_log, sizeof(double) * n, "pixel states");
+  ALLOC(s->st.refractory_until, sizeof(double) * n, "pixel states");
+  ALLOC(s->st.threshold_pos, sizeof(double) * n, "pixel states");
+  ALLOC(s->st.threshold_neg, sizeof(double) * n, "pixel states");
+  ALLOC(s->st.reset_pending, sizeof(int8_t) * n, "pixel states");
+  ALLOC(s->st.rng, sizeof(curandStateXORWOW_t) * n, "pixel RNG");
+  ALLOC(s->ev_count, sizeof(int32_t) * n, "event counts");
+  ALLOC(s->slab_t, sizeof(double) * (size_t)n * s->max_events, "event slabs");
+  ALLOC(s->slab_p, sizeof(int8_t) * (size_t)n * s->max_events, "event slabs");
+  ALLOC(s->events, sizeof(DevEvent) * (size_t)n * s->max_events, "events");
+  ALLOC(s->counters, sizeof(unsigned long long) * kCntSlots, "counters");
+  ALLOC(s->error_word, sizeof(int32_t), "error flag");
+  ALLOC(s->event_total, sizeof(int32_t), "event count");
+  ALLOC(s->d_state, sizeof(dvs_optical_state), "pose");
+#undef ALLOC
+  if ((e = cudaMallocHost(&s->h_status, sizeof(int32_t) * 4)) != cudaSuccess) return bail(e, "status staging");
+  if ((e = cudaMallocHost(&s->h_state, sizeof(dvs_optical_state))) != cudaSuccess) return bail(e, "pose staging");
+  if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+  if ((e = cudaMemsetAsync(s->counters, 0, sizeof(unsigned long long) * kCntSlots, s->stream)) != cudaSuccess)
+    return bail(e, "clear counters");
+  *out = s;
+  return DVS_OK;
+}
+
+int dvs_sensor_destroy(dvs_sensor *s) {
+  if (!s) return DVS_OK;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  cudaFree(s->st.receptor_log);
+  cudaFree(s->st.reference_log);
+  cudaFree(s->st.refractory_until);
+  cudaFree(s->st.threshold_pos);
+  cudaFree(s->st.threshold_neg);
+  cudaFree(s->st.reset_pending);
+  cudaFree(s->st.rng);
+  cudaFree(s->ev_count);
+  cudaFree(s->slab_t);
+  cudaFree(s->slab_p);
+  cudaFree(s->events);
+  cudaFree(s->counters);
+  cudaFree(s->error_word);
+  cudaFree(s->event_total);
+  cudaFree(s->radiance);
+  cudaFree(s->ivs);
+  cudaFree(s->cells);
+  cudaFree(s->poses);
+  cudaFree(s->d_state);
+  if (s->h_ivs) cudaFreeHost(s->h_ivs);
+  if (s->h_cells) cudaFreeHost(s->h_cells);
+  if (s->h_events) cudaFreeHost(s->h_events);
+  if (s->h_status) cudaFreeHost(s->h_status);
+  if (s->h_state) cudaFreeHost(s->h_state);
+  for (cudaEvent_t ev : s->timers) cudaEventDestroy(ev);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s->readout;
+  delete s;
+  return DVS_OK;
+}
+
+void *dvs_sensor_stream(dvs_sensor *s) { return s ? (void *)s->stream : nullptr; }
+
+static int map_error(int32_t word) {
+  if (word & kErrCapacity) return fail(DVS_ERR_CAPACITY, "pixel event capacity exceeded; reduce numerical window");
+  if (word & kErrOptical) return fail(DVS_ERR_OPTICAL, "invalid optical sample or BVH traversal overflow");
+  if (word & kErrStalled) return fail(DVS_ERR_STALLED, "pixel circuit root solve made no progress");
+  return DVS_OK;
+}
+
+static cudaError_t ensure_radiance(dvs_sensor *s, size_t cells) {
+  return grow_device(s->radiance, s->radiance_cap, cells * (size_t)s->scene->pixels());
+}
+
+int dvs_sensor_initialize(dvs_sensor *s, const dvs_optical_state *pose, double timestamp) {
+  // EventSensor::initialize (event_sensor.cu:262-270)
+  if (!s || !pose || !std::isfinite(timestamp) || s->initialized)
+    return fail(DVS_ERR_INVALID, "invalid sensor initialization");
+  CUDA_TRY(cudaSetDevice(s->device), "select device");
+  const int n = s->scene->pixels();
+  CUDA_TRY(ensure_radiance(s, 1), "initial radiance");
+  CUDA_TRY(grow_device(s->poses, s->poses_cap, 1), "pose buffer");
+  *s->h_state = *pose;
+  CUDA_TRY(cudaMemcpyAsync(s->d_state, s->h_state, sizeof(dvs_optical_state), cudaMemcpyHostToDevice, s->stream),
+           "upload pose");
+  CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream), "clear initialization error");
+  CUDA_TRY(launch_pose_from_state(s->d_state, s->poses, s->stream), "pose");
+  CUDA_TRY(launch_trace_cells(s->scene->view(), n, s->poses, 0, 1, 0, s->radiance, nullptr, s->counters, s->stream),
+           "initial optics");
+  CUDA_TRY(launch_init_pixels(n, s->scene->pixel_of_rank, s->radiance, s->p, s->photo, s->threshold_std,
+                              s->threshold_min, s->seed, s->st, s->error_word, s->stream),
+           "initialize circuit");
+  CUDA_TRY(cudaMemcpyAsync(s->h_status + 1, s->error_word, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream),
+           "initialize circuit status");
+  CUDA_TRY(cudaStreamSynchronize(s->stream), "initialize circuit status");
+  if (s->h_status[1]) return fail(DVS_ERR_OPTICAL, "invalid optical sample during initialization");
+  s->stats.launches += 3;
+  s->last_time = timestamp;
+  s->initialized = true;
+  return DVS_OK;
+}
+
+static void record_timer(dvs_sensor *s, int kind) {
+  if (!s->opt.timing) return;
+  if (s->timers_used == s->timers.size()) {
+    cudaEvent_t ev;
+    cudaEventCreate(&ev);
+    s->timers.push_back(ev);
+    s->timer_kind.push_back(kind);
+  }
+  s->timer_kind[s->timers_used] = kind;
+  cudaEventRecord(s->timers[s->timers_used++], s->stream);
+}
+
+// Validates and uploads the batch, then enqueues every kernel of the hot path
+// on the sensor stream without waiting (upload_intervals + generate_pixels).
+static int enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count) {
+  if (!s || !s->initialized || !ivs || count == 0) return fail(DVS_ERR_INVALID, "sensor not initialized or no intervals");
+  if (count > (size_t)std::numeric_limits<int>::max()) return fail(DVS_ERR_INVALID, "too many intervals");
+  // upload_intervals (event_sensor.cu:274-289)
+  double previous = s->last_time, cells_f = 0;
+  for (size_t i = 0; i < count; ++i) {
+    const dvs_optical_interval &iv = ivs[i];
+    if (!std::isfinite(iv.t0) || !std::isfinite(iv.t1) || iv.t0 != previous || iv.t1 <= iv.t0)
+      return fail(DVS_ERR_INVALID, "sensor intervals must be positive and contiguous");
+    cells_f += (iv.t1 - iv.t0) / s->photo.integration_step;
+    previous = iv.t1;
+  }
+  if (cells_f > 1000000) return fail(DVS_ERR_INVALID, "optical horizon too long; reduce batch size");
+  CUDA_TRY(cudaSetDevice(s->device), "select device");
+  // circuit cells, generate_pixels' loop bounds (event_sensor.cu:37-40)
+  size_t n_cells = 0;
+  for (size_t i = 0; i < count; ++i) n_cells += (size_t)std::ceil((ivs[i].t1 - ivs[i].t0) / s->photo.integration_step);
+  CUDA_TRY(grow_pinned(s->h_cells, s->h_cells_cap, n_cells), "cell staging");
+  CUDA_TRY(grow_pinned(s->h_ivs, s->h_ivs_cap, count), "interval staging");
+  size_t c = 0;
+  for (size_t i = 0; i < count; ++i) {
+    const dvs_optical_interval &iv = ivs[i];
+    const int steps = static_cast<int>(std::ceil((iv.t1 - iv.t0) / s->photo.integration_step));
+    const double dt = (iv.t1 - iv.t0) / steps;
+    for (int step = 0; step < steps; ++step) {
+      Cell &cell = s->h_cells[c++];
+      cell.t0 = iv.t0 + step * dt;
+      cell.t1 = step + 1 == steps ? iv.t1 : iv.t0 + (step + 1) * dt;
+      cell.interval = (int32_t)i;
+      cell.pad = 0;
+    }
+  }
+  std::memcpy(s->h_ivs, ivs, sizeof(dvs_optical_interval) * count);
+  const int n = s->scene->pixels();
+  size_t chunk = s->opt.cells_per_chunk > 0 ? (size_t)s->opt.cells_per_chunk
+                                             : std::max<size_t>(1, std::min<size_t>(2048, (size_t(512) << 20) / (8 * (size_t)n)));
+  chunk = std::min(chunk, n_cells);
+  int cw_log2;
+  if (s->opt.cells_per_warp > 0) {
+    cw_log2 = 0;
+    while ((2 << cw_log2) <= std::min(32, s->opt.cells_per_warp)) ++cw_log2;
+  } else {
+    cw_log2 = 0;
+    while (cw_log2 < 5 && (size_t(2) << cw_log2) <= chunk) ++cw_log2;
+  }
+  CUDA_TRY(grow_device(s->ivs, s->ivs_cap, count), "trajectory interval allocation");
+  CUDA_TRY(grow_device(s->cells, s->cells_cap, n_cells), "cell allocation");
+  CUDA_TRY(grow_device(s->poses, s->poses_cap, n_cells), "pose allocation");
+  CUDA_TRY(ensure_radiance(s, chunk), "radiance chunk allocation");
+  CUDA_TRY(cudaMemcpyAsync(s->ivs, s->h_ivs, sizeof(dvs_optical_interval) * count, cudaMemcpyHostToDevice, s->stream),
+           "trajectory interval upload");
+  CUDA_TRY(cudaMemcpyAsync(s->cells, s->h_cells, sizeof(Cell) * n_cells, cudaMemcpyHostToDevice, s->stream),
+           "cell upload");
+  CUDA_TRY(cudaMemsetAsync(s->ev_count, 0, sizeof(int32_t) * n, s->stream), "clear events");
+  CUDA_TRY(cudaMemsetAsync(s->event_total, 0, sizeof(int32_t), s->stream), "clear events");
+  CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream), "clear status");
+  CUDA_TRY(launch_cell_poses(s->ivs, s->cells, (int)n_cells, s->poses, s->stream), "cell poses");
+  const SceneView view = s->scene->view();
+  for (size_t c0 = 0; c0 < n_cells; c0 += chunk) {
+    const int nc = (int)std::min(chunk, n_cells - c0);
+    record_timer(s, 0);
+    CUDA_TRY(launch_trace_cells(view, n, s->poses, (int)c0, nc, cw_log2, s->radiance, nullptr, s->counters, s->stream),
+             "trace circuit cells");
+    record_timer(s, 1);
+    CUDA_TRY(launch_circuit(n, s->cells, (int)c0, nc, s->radiance, s->p, s->photo, s->max_events, s->st, s->ev_count,
+                            s->slab_t, s->slab_p, s->error_word, s->counters, s->stream),
+             "integrate circuits");
+    s->stats.launches += 2;
+    s->stats.optics_launches += 1;
+    s->stats.circuit_launches += 1;
+  }
+  record_timer(s, 2);
+  CUDA_TRY(launch_emit_events(n, s->scene->pixel_of_rank, s->scene->camera.width, s->max_events, s->ev_count,
+                              s->slab_t, s->slab_p, s->events, s->event_total, s->stream),
+           "compact events");
+  CUDA_TRY(launch_event_depth(view, s->ivs, (int)count, s->events, s->event_total, s->error_word, s->counters,
+                              s->stream),
+           "event depth");
+  record_timer(s, 3);
+  s->stats.launches += 3;
+  s->last_time = ivs[count - 1].t1;
+  return DVS_OK;
+}
+
+static void collect_timers(dvs_sensor *s) {
+  if (!s->opt.timing) return;
+  for (size_t i = 0; i + 1 < s->timers_used; ++i) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, s->timers[i], s->timers[i + 1]) != cudaSuccess) continue;
+    switch (s->timer_kind[i]) {
+      case 0: s->stats.optics_ms += ms; break;
+      case 1: s->stats.circuit_ms += ms; break;
+      case 2: s->stats.events_ms += ms; break;
+      default: break;
+    }
+  }
+  s->timers_used = 0;
+}
+
+// collect_events (event_sensor.cu:296-305): status, events, readout.
+static int collect(dvs_sensor *s, double end, size_t *n_ready) {
+  CUDA_TRY(cudaMemcpyAsync(s->h_status, s->event_total, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream), "copy count");
+  CUDA_TRY(cudaMemcpyAsync(s->h_status + 1, s->error_word, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream),
+           "copy status");
+  CUDA_TRY(cudaStreamSynchronize(s->stream), "copy status");
+  collect_timers(s);
+  const int32_t count = s->h_status[0], word = s->h_status[1];
+  if (word) return map_error(word);
+  auto t0 = std::chrono::steady_clock::now();
+  if (count > 0) {
+    CUDA_TRY(grow_pinned(s->h_events, s->h_events_cap, (size_t)count), "event staging");
+    CUDA_TRY(cudaMemcpyAsync(s->h_events, s->events, sizeof(DevEvent) * count, cudaMemcpyDeviceToHost, s->stream),
+             "copy events");
+    CUDA_TRY(cudaStreamSynchronize(s->stream), "copy events");
+  }
+  std::vector<HostEvent> batch((size_t)count);
+  for (int32_t i = 0; i < count; ++i) {
+    const DevEvent &d = s->h_events[i];
+    batch[i] = HostEvent{d.t, d.x, d.y, d.polarity, d.depth};
+  }
+  if (s->ready_head > 0 && s->ready_head == s->ready.size()) {
+    s->ready.clear();
+    s->ready_head = 0;
+  }
+  const size_t before = s->ready.size();
+  s->readout->submit(batch, end, s->ready);
+  s->stats.events_generated += (uint64_t)count;
+  s->stats.events_delivered += s->ready.size() - before;
+  s->stats.dropped = s->readout->dropped();
+  s->stats.peak_queue = s->readout->peak();
+  s->stats.readout_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (n_ready) *n_ready = s->ready.size() - s->ready_head;
+  return DVS_OK;
+}
+
+int dvs_sensor_process(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, size_t *n_ready) {
+  if (n_ready) *n_ready = 0;
+  int r = enqueue(s, ivs, count);
+  if (r) return r;
+  s->pending = false;
+  return collect(s, ivs[count - 1].t1, n_ready);
+}
+
+int dvs_sensor_enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count) {
+  int r = enqueue(s, ivs, count);
+  if (r) return r;
+  s->pending = true;
+  s->pending_end = ivs[count - 1].t1;
+  return DVS_OK;
+}
+
+int dvs_sensor_collect(dvs_sensor *s, size_t *n_ready) {
+  if (n_ready) *n_ready = 0;
+  if (!s || !s->pending) return fail(DVS_ERR_INVALID, "no enqueued batch to collect");
+  s->pending = false;
+  return collect(s, s->pending_end, n_ready);
+}
+
+int dvs_sensor_read(dvs_sensor *s, dvs_event *out, size_t capacity, size_t *n_out) {
+  if (!s || !n_out) return fail(DVS_ERR_INVALID, "null argument");
+  const size_t avail = s->ready.size() - s->ready_head;
+  const size_t m = std::min(avail, capacity);
+  if (m && !out) return fail(DVS_ERR_INVALID, "null output buffer");
+  for (size_t i = 0; i < m; ++i) {
+    const HostEvent &e = s->ready[s->ready_head + i];
+    dvs_event &o = out[i];
+    o.timestamp = e.t;
+    o.x = e.x;
+    o.y = e.y;
+    o.polarity = e.p;
+    o.depth = e.depth;
+  }
+  s->ready_head += m;
+  *n_out = m;
+  if (s->ready_head == s->ready.size()) {
+    s->ready.clear();
+    s->ready_head = 0;
+  }
+  return DVS_OK;
+}
+
+int dvs_sensor_process_events(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, dvs_event *out,
+                              size_t capacity, size_t *n_out) {
+  if (!n_out) return fail(DVS_ERR_INVALID, "null argument");
+  *n_out = 0;
+  size_t n_ready = 0;
+  int r = dvs_sensor_process(s, ivs, count, &n_ready);
+  if (r) return r;
+  if (n_ready > capacity) {
+    *n_out = n_ready;
+    return fail(DVS_ERR_OUTPUT_SMALL, "event output buffer too small; events remain readable");
+  }
+  return dvs_sensor_read(s, out, capacity, n_out);
+}
+
+int dvs_sensor_drain(dvs_sensor *s, dvs_event *out, size_t capacity, size_t *n_out) {
+  if (!s || !n_out) return fail(DVS_ERR_INVALID, "null argument");
+  s->readout->drain(s->ready);
+  return dvs_sensor_read(s, out, capacity, n_out);
+}
+
+int dvs_sensor_stats_get(const dvs_sensor *s, dvs_sensor_stats *out) {
+  if (!s || !out) return fail(DVS_ERR_INVALID, "null argument");
+  unsigned long long c[kCntSlots] = {0, 0, 0, 0};
+  CUDA_TRY(cudaSetDevice(s->device), "select device");
+  CUDA_TRY(cudaMemcpyAsync(c, s->counters, sizeof(c), cudaMemcpyDeviceToHost, s->stream), "copy counters");
+  CUDA_TRY(cudaStreamSynchronize(s->stream), "copy counters");
+  *out = s->stats;
+  out->primary_rays = c[kCntPrimary];
+  out->shadow_rays = c[kCntShadow];
+  out->circuit_cells = c[kCntCells];
+  return DVS_OK;
+}
+
+int dvs_sensor_stats_reset(dvs_sensor *s) {
+  if (!s) return fail(DVS_ERR_INVALID, "null argument");
+  CUDA_TRY(cudaSetDevice(s->device), "select device");
+  CUDA_TRY(cudaMemsetAsync(s->counters, 0, sizeof(unsigned long long) * kCntSlots, s->stream), "clear counters");
+  CUDA_TRY(cudaStreamSynchronize(s->stream), "clear counters");
+  const uint64_t dropped = s->stats.dropped, peak = s->stats.peak_queue;
+  s->stats = dvs_sensor_stats{};
+  s->stats.dropped = dropped;
+  s->stats.peak_queue = peak;
+  return DVS_OK;
+}
+
+int dvs_sensor_read_state(dvs_sensor *s, double *state5, int32_t *reset_pending) {
+  if (!s) return fail(DVS_ERR_INVALID, "null argument");
+  CUDA_TRY(cudaSetDevice(s->device), "select device");
+  const int n = s->scene->pixels();
+  std::vector<double> buf((size_t)5 * n);
+  std::vector<int8_t> rp(n);
+  std::vector<int32_t> order(n);
+  double *src[5] = {s->st.receptor_log, s->st.reference_log, s->st.refractory_until, s->st.threshold_pos,
+                    s->st.threshold_neg};
+  for (int f = 0; f < 5; ++f)
+    CUDA_TRY(cudaMemcpyAsync(buf.data() + (size_t)f * n, src[f], sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream),
+             "download state");
+  CUDA_TRY(cudaMemcpyAsync(rp.data(), s->st.reset_pending, n, cudaMemcpyDeviceToHost, s->stream), "download state");
+  CUDA_TRY(cudaMemcpyAsync(order.data(), s->scene->pixel_of_rank, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                           s->stream),
+           "download order");
+  CUDA_TRY(cudaStreamSynchronize(s->stream), "download state");
+  for (int k = 0; k < n; ++k) {
+    const int pix = order[k];
+    if (state5)
+      for (int f = 0; f < 5; ++f) state5[(size_t)pix * 5 + f] = buf[(size_t)f * n + k];
+    if (reset_pending) reset_pending[pix] = rp[k];
+  }
+  return DVS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// Internal data layout of the GB300 DVS path, shared by host C++ and device
+// code.  Nothing here is part of the C-ABI.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "dvs_gb300.h"
+
+namespace dvsgb {
+
+// ---- wide BVH --------------------------------------------------------------
+// A 4-wide node, 128 bytes = 8 x 16-byte vector loads.  Child bounds are
+// stored per axis so one float4 load yields the same coordinate of all four
+// children.  child[c]: inner node index when count[c]==0, first triangle
+// (leaf order) when count[c]>0; count[c]<0 marks an empty slot.
+struct alignas(16) Bvh4Node {
+  float lo_x[4], hi_x[4], lo_y[4], hi_y[4], lo_z[4], hi_z[4];
+  int32_t child[4];
+  int32_t count[4];
+};
+static_assert(sizeof(Bvh4Node) == 128, "Bvh4Node layout");
+
+// Intersection record in leaf order, 48 bytes = 3 x 16-byte loads.  Edges are
+// precomputed with the same float subtraction the reference performs per test
+// (include/dvs/device_ray.hpp:58-59), so the Moller-Trumbore inputs are
+// bit-identical.
+struct alignas(16) TriRecord {
+  float v0[3];
+  float e1[3];
+  float e2[3];
+  uint32_t original;  // triangle index in the caller's mesh
+  uint32_t pad[2];
+};
+static_assert(sizeof(TriRecord) == 48, "TriRecord layout");
+
+// Shading record in leaf order, 64 bytes: vertex normals and per-vertex
+// material albedo (already passed through the fallback rule of
+// include/dvs/device_optics.cuh:30-33).
+struct alignas(16) ShadeRecord {
+  float n0[3], a0;
+  float n1[3], a1;
+  float n2[3], a2;
+  float pad[4];
+};
+static_assert(sizeof(ShadeRecord) == 64, "ShadeRecord layout");
+
+// Maximum warp-stack depth; the builder rejects trees that could exceed it.
+constexpr int kStackSlots = 96;
+
+struct Bvh4Build {
+  std::vector<Bvh4Node> nodes;
+  std::vector<uint32_t> order;  // leaf order -> original triangle index
+  int depth = 0;                // levels of 4-wide nodes
+  double seconds = 0;
+};
+
+// Morton-ordered radix-split binary tree collapsed to a 4-wide tree.
+// Returns false with a message on invalid input.
+bool build_bvh4(const float *vertices, size_t n_vertices, const uint32_t *indices, size_t n_triangles,
+                int leaf_size, Bvh4Build &out, std::string &error);
+
+// ---- FIFO readout (src/event_readout.cpp:6-34 semantics) ---------------------
+struct HostEvent {
+  double t;
+  int16_t x, y;
+  int8_t p;
+  float depth;
+};
+
+class Readout {
+ public:
+  Readout(double bandwidth, double latency, size_t capacity)
+      : bandwidth_(bandwidth), latency_(latency), capacity_(capacity) {}
+  // Orders a batch by (t, y, x), queues it and appends the events whose
+  // delivery time is <= now to `ready`.
+  void submit(std::vector<HostEvent> &batch, double now, std::vector<HostEvent> &ready);
+  void drain(std::vector<HostEvent> &ready);
+  size_t dropped() const { return dropped_; }
+  size_t peak() const { return peak_; }
+
+ private:
+  struct Pending {
+    double ready_time;
+    HostEvent event;
+  };
+  double bandwidth_, latency_, available_ = 0;
+  size_t capacity_, dropped_ = 0, peak_ = 0;
+  std::vector<Pending> queue_;
+  size_t head_ = 0;
+};
+
+}  // namespace dvsgb

@@ -1,0 +1,289 @@
+"""Host-side mirror of the reference's renderer facade over the C-ABI.
+
+Class and method names follow include/dvs/raycast.hpp:23-86,
+include/dvs/event_sensor.hpp:40-79 and include/dvs/device_scene.hpp:5-15 so
+code written against the reference reads the same; arguments are numpy
+arrays and plain dicts instead of Eigen/CUDA vector types.  Errors raise the
+reference's exception kinds: ValueError for std::invalid_argument, and
+CapacityError / OpticalError (RuntimeError) for device status 1 / 2.
+
+An optical state is a dict with keys position, velocity, light, light_rate
+(3 floats each), rotation (quaternion x, y, z, w), intensity,
+intensity_rate -- the fields of OpticalState (optical_sensor.hpp:148-152).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import EVENT_DTYPE, INTERVAL_DTYPE, STATE_DTYPE, check
+
+HAPKE_DEFAULT = dict(b=0.24, c=0.305, hS=0.08, hC=1.0, thetap=26.0 * float(np.float32(3.14159265358979323846)) / 180.0,
+                     w=0.324, B_S0=2.42, B_C0=0.0, phi=0.3)  # HapkeConfig defaults, scene_types.hpp:204-214
+
+
+def state_array(states):
+    """Packs one or more optical-state dicts into the OpticalState layout."""
+    if isinstance(states, dict):
+        states = [states]
+    out = np.zeros(len(states), STATE_DTYPE)
+    for i, st in enumerate(states):
+        for k in ("position", "velocity", "light", "light_rate"):
+            out[i][k] = st.get(k, (0.0, 0.0, 0.0))
+        out[i]["rotation"] = st.get("rotation", (0.0, 0.0, 0.0, 1.0))
+        out[i]["intensity"] = st.get("intensity", 0.0)
+        out[i]["intensity_rate"] = st.get("intensity_rate", 0.0)
+    return out
+
+
+def interval_array(intervals):
+    """[(start_state, end_state, t0, t1), ...] -> OpticalInterval layout."""
+    if isinstance(intervals, np.ndarray) and intervals.dtype == INTERVAL_DTYPE:
+        return np.ascontiguousarray(intervals)
+    out = np.zeros(len(intervals), INTERVAL_DTYPE)
+    for i, (a, b, t0, t1) in enumerate(intervals):
+        out[i]["start"] = state_array(a)[0]
+        out[i]["end"] = state_array(b)[0]
+        out[i]["t0"] = t0
+        out[i]["t1"] = t1
+    return out
+
+
+def camera_struct(camera):
+    return _capi.Camera(int(camera["width"]), int(camera["height"]), float(camera["fx"]), float(camera["fy"]),
+                        float(camera["cx"]), float(camera["cy"]))
+
+
+def hapke_struct(h):
+    return _capi.Hapke(*[float(h[k]) for k in _capi.HAPKE_KEYS])
+
+
+def physic_struct(p):
+    s = _capi.Physic()
+    for k in _capi.PHYSIC_FLOAT_FIELDS:
+        setattr(s, k, float(p[k]))
+    for k in _capi.PHYSIC_INT_FIELDS:
+        setattr(s, k, int(p[k]))
+    return s
+
+
+def derive_parameters(physic, physic_effects=True):
+    """parameters()/photo_parameters() (event_sensor.cu:151-176) as a dict."""
+    out = (C.c_double * 9)()
+    check(_capi.load().dvs_derive_parameters(C.byref(physic_struct(physic)), int(physic_effects), out))
+    keys = ("threshold_pos", "threshold_neg", "charge_scale", "refractory_time", "reference_leak",
+            "reset_noise_std", "electrons_per_radiance", "dark_electrons", "integration_step")
+    return dict(zip(keys, list(out)))
+
+
+class DeviceScene:
+    """Owner of the device-resident wide BVH, triangle and shading records
+    (replaces BVHBuilder::build + DeviceScene)."""
+
+    def __init__(self, vertices, normals, indices, camera, supersample, hapke=None, albedos=None, leaf_size=4):
+        lib = _capi.load()
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+        a = None if albedos is None else np.ascontiguousarray(albedos, np.float32).reshape(-1)
+        if n.shape != v.shape or (a is not None and a.size != v.shape[0]):
+            raise ValueError("invalid indexed mesh/BVH/material dimensions")
+        self.camera = dict(camera)
+        self.samples = int(supersample)
+        self.hapke = dict(hapke or HAPKE_DEFAULT)
+        h = C.c_void_p()
+        fp = C.POINTER(C.c_float)
+        check(lib.dvs_scene_create(v.ctypes.data_as(fp), n.ctypes.data_as(fp), i.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                   a.ctypes.data_as(fp) if a is not None else None, v.shape[0], i.shape[0],
+                                   C.byref(camera_struct(camera)), self.samples, C.byref(hapke_struct(self.hapke)),
+                                   C.byref(_capi.BvhParams(int(leaf_size))), C.byref(h)))
+        self.handle = h
+        self.width = int(camera["width"])
+        self.height = int(camera["height"])
+
+    @property
+    def pixels(self):
+        return self.width * self.height
+
+    def info(self):
+        out = _capi.SceneInfo()
+        check(_capi.load().dvs_scene_info_get(self.handle, C.byref(out)))
+        return {k: getattr(out, k) for k, _ in out._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _capi.load().dvs_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class EventSensor:
+    """EventSensor (include/dvs/event_sensor.hpp:40-79) on the GB300 path."""
+
+    def __init__(self, scene, physic, physic_effects=True, aer_delay=True, cells_per_chunk=0, cells_per_warp=0,
+                 timing=False):
+        lib = _capi.load()
+        self.scene = scene
+        self.physic = dict(physic)
+        opt = _capi.SensorOptions()
+        lib.dvs_sensor_options_default(C.byref(opt))
+        opt.physic_effects = int(physic_effects)
+        opt.aer_delay = int(aer_delay)
+        opt.cells_per_chunk = int(cells_per_chunk)
+        opt.cells_per_warp = int(cells_per_warp)
+        opt.timing = int(timing)
+        h = C.c_void_p()
+        check(lib.dvs_sensor_create(scene.handle, C.byref(physic_struct(physic)), C.byref(opt), C.byref(h)))
+        self.handle = h
+        self.max_events = int(physic["max_events_per_step"])
+
+    def initialize(self, pose, timestamp):
+        st = state_array(pose)
+        check(_capi.load().dvs_sensor_initialize(self.handle, st.ctypes.data, float(timestamp)))
+
+    def process(self, interval):
+        return self.process_many([interval])
+
+    def process_many(self, intervals):
+        ivs = interval_array(intervals)
+        n = C.c_size_t()
+        check(_capi.load().dvs_sensor_process(self.handle, ivs.ctypes.data, len(ivs), C.byref(n)))
+        return self._read(n.value)
+
+    def enqueue(self, intervals):
+        """Launches a batch without waiting; events stay on the device."""
+        ivs = interval_array(intervals)
+        check(_capi.load().dvs_sensor_enqueue(self.handle, ivs.ctypes.data, len(ivs)))
+
+    def collect(self):
+        n = C.c_size_t()
+        check(_capi.load().dvs_sensor_collect(self.handle, C.byref(n)))
+        return self._read(n.value)
+
+    def _read(self, count):
+        out = np.zeros(max(count, 1), EVENT_DTYPE)
+        got = C.c_size_t()
+        check(_capi.load().dvs_sensor_read(self.handle, out.ctypes.data, len(out), C.byref(got)))
+        return out[: got.value].copy()
+
+    def drain(self):
+        cap = 1 << 20
+        chunks = []
+        while True:
+            out = np.zeros(cap, EVENT_DTYPE)
+            got = C.c_size_t()
+            check(_capi.load().dvs_sensor_drain(self.handle, out.ctypes.data, cap, C.byref(got)))
+            chunks.append(out[: got.value].copy())
+            if got.value < cap:
+                break
+        return np.concatenate(chunks)
+
+    def stats(self):
+        out = _capi.SensorStats()
+        check(_capi.load().dvs_sensor_stats_get(self.handle, C.byref(out)))
+        return out.as_dict()
+
+    def reset_stats(self):
+        check(_capi.load().dvs_sensor_stats_reset(self.handle))
+
+    def dropped(self):
+        return self.stats()["dropped"]
+
+    def peak_queue(self):
+        return self.stats()["peak_queue"]
+
+    def stream(self):
+        return _capi.load().dvs_sensor_stream(self.handle)
+
+    def read_state(self):
+        n = self.scene.pixels
+        st = np.zeros((n, 5), np.float64)
+        rp = np.zeros(n, np.int32)
+        check(_capi.load().dvs_sensor_read_state(self.handle, st.ctypes.data_as(C.POINTER(C.c_double)),
+                                                 rp.ctypes.data_as(C.POINTER(C.c_int32))))
+        return st, rp
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _capi.load().dvs_sensor_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DvsRayCaster:
+    """DvsRayCaster (include/dvs/raycast.hpp:23-62)."""
+
+    def __init__(self, scene, physic, **options):
+        self.scene = scene
+        self.sensor = EventSensor(scene, physic, **options)
+
+    def initialize(self, state, timestamp):
+        self.sensor.initialize(state, timestamp)
+
+    def advance(self, start, end, t0, t1):
+        return self.sensor.process((start, end, t0, t1))
+
+    def advance_many(self, intervals):
+        return self.sensor.process_many(intervals)
+
+    def drain(self):
+        return self.sensor.drain()
+
+    def dropped_events(self):
+        return self.sensor.dropped()
+
+    def peak_queue(self):
+        return self.sensor.peak_queue()
+
+
+def quaternion_from_matrix(m):
+    """Unit quaternion (x, y, z, w) of a 3x3 rotation matrix (Shepperd's method)."""
+    m = np.asarray(m, np.float64).reshape(3, 3)
+    tr = m[0, 0] + m[1, 1] + m[2, 2]
+    if tr > 0:
+        s = np.sqrt(tr + 1.0) * 2
+        w, x, y, z = 0.25 * s, (m[2, 1] - m[1, 2]) / s, (m[0, 2] - m[2, 0]) / s, (m[1, 0] - m[0, 1]) / s
+    elif m[0, 0] > m[1, 1] and m[0, 0] > m[2, 2]:
+        s = np.sqrt(1.0 + m[0, 0] - m[1, 1] - m[2, 2]) * 2
+        w, x, y, z = (m[2, 1] - m[1, 2]) / s, 0.25 * s, (m[0, 1] + m[1, 0]) / s, (m[0, 2] + m[2, 0]) / s
+    elif m[1, 1] > m[2, 2]:
+        s = np.sqrt(1.0 + m[1, 1] - m[0, 0] - m[2, 2]) * 2
+        w, x, y, z = (m[0, 2] - m[2, 0]) / s, (m[0, 1] + m[1, 0]) / s, 0.25 * s, (m[1, 2] + m[2, 1]) / s
+    else:
+        s = np.sqrt(1.0 + m[2, 2] - m[0, 0] - m[1, 1]) * 2
+        w, x, y, z = (m[1, 0] - m[0, 1]) / s, (m[0, 2] + m[2, 0]) / s, (m[1, 2] + m[2, 1]) / s, 0.25 * s
+    q = np.array([x, y, z, w])
+    return tuple(float(v) for v in (q / np.linalg.norm(q)).astype(np.float32))
+
+
+class CamRayCaster:
+    """CamRayCaster (include/dvs/raycast.hpp:64-86): image and depth frames."""
+
+    def __init__(self, scene):
+        self.scene = scene
+
+    def render_state(self, state):
+        st = state_array(state)
+        n = self.scene.pixels
+        img = np.zeros(n, np.float32)
+        dep = np.zeros(n, np.float32)
+        fp = C.POINTER(C.c_float)
+        check(_capi.load().dvs_cam_render(self.scene.handle, st.ctypes.data, img.ctypes.data_as(fp),
+                                          dep.ctypes.data_as(fp)))
+        return img, dep
+
+    def render_main(self, camera_origin, camera_world, light_dir, light_intensity):
+        """camera_world: 3x3 rotation (row-major here); light_dir: world light direction."""
+        q = quaternion_from_matrix(camera_world)
+        return self.render_state(dict(position=camera_origin, rotation=q, light=light_dir,
+                                      intensity=light_intensity))

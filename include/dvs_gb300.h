@@ -1,0 +1,199 @@
+/*
+ * dvs_gb300 -- C-ABI of the GB300-native DVS hot path.
+ *
+ * Plain pointers and sizes only.  The structs are layout-identical to the
+ * reference's device PODs so a caller can hand over the reference's own
+ * vectors unchanged:
+ *   dvs_optical_state    == OpticalState     (include/dvs/optical_sensor.hpp:148-152), 80 bytes
+ *   dvs_optical_interval == OpticalInterval  (include/dvs/optical_sensor.hpp:153),     176 bytes
+ *   dvs_event            == Event            (include/dvs/dvs_base.hpp:9-18),           17 bytes packed
+ *   dvs_camera           == CameraConfig     (include/dvs/scene_types.hpp:174-177)
+ *   dvs_physic           == PhysicConfig     (include/dvs/scene_types.hpp:179-194)
+ *   dvs_hapke            == HapkeConfig      (include/dvs/scene_types.hpp:204-214)
+ *
+ * Every entry point returns a status code (DVS_OK on success); the text of the
+ * last failure on the calling thread is available from dvs_last_error().  The
+ * reference reports the same conditions as C++ exceptions
+ * (src/cuda/event_sensor.cu:300-301, include/dvs/math_types.hpp:6-14).
+ *
+ * Threading: one CUDA stream per handle.  A handle is not thread-safe;
+ * different handles are.  A scene may be shared by several sensors and
+ * cameras (the reference shares one DeviceScene through shared_ptr) and must
+ * outlive them.
+ */
+#ifndef DVS_GB300_H
+#define DVS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define DVS_ALIGN16 alignas(16)
+extern "C" {
+#else
+#define DVS_ALIGN16 _Alignas(16)
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define DVS_OK 0
+#define DVS_ERR_CAPACITY 1      /* "pixel event capacity exceeded; reduce numerical window" */
+#define DVS_ERR_OPTICAL 2       /* "invalid optical sample or BVH traversal overflow" */
+#define DVS_ERR_INVALID 3       /* invalid argument or state (std::invalid_argument) */
+#define DVS_ERR_CUDA 4          /* CUDA runtime failure (std::runtime_error via CUDA_CHECK) */
+#define DVS_ERR_STALLED 5       /* circuit root solve made no progress (bounded-loop guard) */
+#define DVS_ERR_OUTPUT_SMALL 6  /* caller's output buffer too small; nothing was lost */
+
+/* ---- PODs ---------------------------------------------------------------- */
+typedef struct { float x, y, z; } dvs_float3;
+typedef struct { DVS_ALIGN16 float x; float y, z, w; } dvs_float4; /* quaternion (x,y,z,w) */
+
+typedef struct {
+  dvs_float3 position, velocity, light, light_rate;
+  dvs_float4 rotation;
+  float intensity, intensity_rate;
+} dvs_optical_state;
+
+typedef struct {
+  dvs_optical_state start, end;
+  double t0, t1;
+} dvs_optical_interval;
+
+#pragma pack(push, 1)
+typedef struct {
+  double timestamp; /* seconds */
+  int16_t x, y;
+  int8_t polarity;  /* 1 ON, 0 OFF */
+  float depth;      /* mean hit range at the event time, -1 for background */
+} dvs_event;
+#pragma pack(pop)
+
+typedef struct { int32_t width, height; float fx, fy, cx, cy; } dvs_camera;
+
+typedef struct {
+  float b, c, hS, hC, thetap, w, B_S0, B_C0, phi;
+} dvs_hapke;
+
+typedef struct {
+  float threshold_pos, threshold_neg, refractory_time;
+  float readout_bandwidth, readout_latency;
+  float threshold_std, threshold_min;
+  float wavelength_nm, quantum_efficiency, pixel_pitch_um;
+  float fill_factor, f_number, lens_transmission;
+  float radiance_scale;
+  float temperature_k, subthreshold_kappa;
+  float receptor_capacitance_f;
+  float reset_capacitance_f, dark_current_a;
+  float reset_leakage_a, circuit_step;
+  int32_t photon_shot_noise, reset_thermal_noise;
+  int32_t random_seed, max_events_per_step;
+  int32_t readout_queue_capacity;
+} dvs_physic;
+
+/* Runtime forms of the reference's compile-time switches
+ * ENABLE_PHYSIC_EFFECTS and ENABLE_AER_DELAY (CMakeLists.txt:21-35), plus
+ * the tunables of this implementation.  dvs_sensor_options_default() gives
+ * the reference's defaults (both switches on). */
+typedef struct {
+  int32_t physic_effects;     /* shot noise, dark current, mismatch, refractory, leak, kTC */
+  int32_t aer_delay;          /* finite FIFO readout */
+  int32_t cells_per_chunk;    /* circuit cells traced per optics launch (0 = automatic) */
+  int32_t cells_per_warp;     /* 1,2,4,8,16,32: cells sharing one warp packet (0 = automatic) */
+  int32_t timing;             /* record per-kernel CUDA-event timings */
+  int32_t reserved[3];
+} dvs_sensor_options;
+
+typedef struct {
+  int32_t leaf_size;          /* triangles per BVH leaf, 1..8 (default 4) */
+  int32_t reserved[3];
+} dvs_bvh_params;
+
+typedef struct {
+  uint64_t triangles, vertices, nodes;
+  int32_t depth, root;
+  uint64_t device_bytes;
+  double build_seconds;
+} dvs_scene_info;
+
+typedef struct {
+  uint64_t primary_rays, shadow_rays;      /* traced on the device, counted there */
+  uint64_t events_generated, events_delivered;
+  uint64_t dropped, peak_queue;            /* readout FIFO (EventReadout::dropped/peak_queue) */
+  uint64_t circuit_cells;                  /* pixel x cell integrations */
+  uint64_t launches;                       /* kernels launched by this handle */
+  double optics_ms, circuit_ms, events_ms, readout_ms; /* with options.timing */
+  uint64_t optics_launches, circuit_launches;
+} dvs_sensor_stats;
+
+typedef struct dvs_scene dvs_scene;
+typedef struct dvs_sensor dvs_sensor;
+
+/* ---- library --------------------------------------------------------------- */
+const char *dvs_last_error(void);
+const char *dvs_version(void);
+/* Fills a default option block (reference behaviour). */
+void dvs_sensor_options_default(dvs_sensor_options *out);
+/* Derived per-pixel parameters, parameters()/photo_parameters()
+ * (src/cuda/event_sensor.cu:151-176): out[0..5] = threshold_pos, threshold_neg,
+ * charge_scale, refractory_time, reference_leak, reset_noise_std;
+ * out[6..8] = electrons_per_radiance, dark_electrons, integration_step. */
+int dvs_derive_parameters(const dvs_physic *physic, int32_t physic_effects, double *out9);
+
+/* ---- scene: replaces BVHBuilder::build + DeviceScene (src/bvh/build.cpp:27-76,
+ *      src/cuda/device_scene.cu:15-37) ----------------------------------------- */
+/* vertices/normals: n_vertices x 3 floats; indices: n_triangles x 3 uint32;
+ * albedos: n_vertices floats or NULL.  Builds the wide BVH and uploads it. */
+int dvs_scene_create(const float *vertices, const float *normals, const uint32_t *indices,
+                     const float *albedos, size_t n_vertices, size_t n_triangles,
+                     const dvs_camera *camera, int32_t supersample, const dvs_hapke *hapke,
+                     const dvs_bvh_params *params, dvs_scene **out);
+int dvs_scene_destroy(dvs_scene *scene);
+int dvs_scene_info_get(const dvs_scene *scene, dvs_scene_info *out);
+
+/* ---- camera image: replaces CamRayCaster::render_main / OpticalSampler::evaluate
+ *      (src/cuda/cam_render.cu:16-28, src/cuda/optical_sampler.cu:8-23,154-168) -- */
+/* radiance and depth: width*height floats each (host pointers); depth may be NULL. */
+int dvs_cam_render(dvs_scene *scene, const dvs_optical_state *pose, float *radiance, float *depth);
+
+/* ---- event sensor: replaces EventSensor (src/cuda/event_sensor.cu:244-305) ---- */
+int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sensor_options *options,
+                      dvs_sensor **out);
+int dvs_sensor_destroy(dvs_sensor *sensor);
+/* EventSensor::initialize (event_sensor.cu:262-270). */
+int dvs_sensor_initialize(dvs_sensor *sensor, const dvs_optical_state *pose, double timestamp);
+/* EventSensor::process_many (event_sensor.cu:290-305): traces, integrates and
+ * reads out a batch of contiguous intervals.  The ready events are kept in the
+ * handle; *n_ready receives their count.  Fetch them with dvs_sensor_read. */
+int dvs_sensor_process(dvs_sensor *sensor, const dvs_optical_interval *intervals, size_t n_intervals,
+                       size_t *n_ready);
+/* The two halves of dvs_sensor_process, for callers that overlap host work
+ * with the device or time the device path alone:
+ *   dvs_sensor_enqueue  validates and uploads the batch and launches every
+ *                       kernel on the handle's stream without waiting; the
+ *                       circuit state advances and the generated events stay
+ *                       on the device;
+ *   dvs_sensor_collect  waits, reports device errors, downloads the events
+ *                       and runs the readout (*n_ready as in process).
+ * An enqueue that is not collected before the next enqueue discards that
+ * batch's events (the circuit state still advanced). */
+int dvs_sensor_enqueue(dvs_sensor *sensor, const dvs_optical_interval *intervals, size_t n_intervals);
+int dvs_sensor_collect(dvs_sensor *sensor, size_t *n_ready);
+/* Copies up to `capacity` ready events into `out` and removes them. */
+int dvs_sensor_read(dvs_sensor *sensor, dvs_event *out, size_t capacity, size_t *n_out);
+/* process + read in one call; DVS_ERR_OUTPUT_SMALL leaves the events readable. */
+int dvs_sensor_process_events(dvs_sensor *sensor, const dvs_optical_interval *intervals,
+                              size_t n_intervals, dvs_event *out, size_t capacity, size_t *n_out);
+/* EventSensor::drain / EventReadout::drain (event_readout.cpp:31-34). */
+int dvs_sensor_drain(dvs_sensor *sensor, dvs_event *out, size_t capacity, size_t *n_out);
+int dvs_sensor_stats_get(const dvs_sensor *sensor, dvs_sensor_stats *out);
+int dvs_sensor_stats_reset(dvs_sensor *sensor);
+/* The CUDA stream (cudaStream_t) the handle launches on, for external timing. */
+void *dvs_sensor_stream(dvs_sensor *sensor);
+/* Per-pixel circuit state, row-major pixel order: 5 doubles per pixel
+ * (receptor_log, reference_log, refractory_until, threshold_pos, threshold_neg)
+ * and one int32 reset flag.  Either pointer may be NULL. */
+int dvs_sensor_read_state(dvs_sensor *sensor, double *state5, int32_t *reset_pending);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DVS_GB300_H */

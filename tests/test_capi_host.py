@@ -1,0 +1,93 @@
+"""C-ABI library checks that need no GPU: it loads, exports every symbol the
+header declares, keeps the reference's struct layouts, derives the pixel
+parameters exactly as the oracle does, and rejects invalid arguments before
+touching the device."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from dvsrender4deepspace_gb300 import _capi
+from dvsrender4deepspace_gb300 import build as dvs_build
+from dvsrender4deepspace_gb300.raycast import camera_struct, hapke_struct, physic_struct
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    dvs_build.build()
+    return _capi.load()
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "dvs_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(dvs_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_symbols()
+    assert len(names) >= 19
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(_capi.EXPORTS)
+
+
+def test_struct_layouts_match_reference():
+    assert _capi.STATE_DTYPE.itemsize == 80      # OpticalState with float4 alignment
+    assert _capi.INTERVAL_DTYPE.itemsize == 176  # OpticalInterval
+    assert _capi.EVENT_DTYPE.itemsize == 17      # packed Event
+    assert C.sizeof(_capi.Physic) == 26 * 4
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.dvs_version()
+
+
+def test_derive_parameters_matches_oracle(lib):
+    from oracle import oracle as O
+    from tests.test_oracle_golden import davis_physic
+    ol = O.load()
+    for effects in (0, 1):
+        for over in ({}, dict(reset_leakage_a=1e-16, reset_thermal_noise=1), dict(f_number=1.4, circuit_step=0.5e-6)):
+            phys = davis_physic(**over)
+            out = (C.c_double * 9)()
+            assert lib.dvs_derive_parameters(C.byref(physic_struct(phys)), effects, out) == 0
+            p, ph = O.opixel_params(), O.ophoto()
+            ol.oracle_derive_parameters(C.byref(O.physic_struct(phys)), effects, C.byref(p), C.byref(ph))
+            want = [p.threshold_pos, p.threshold_neg, p.charge_scale, p.refractory_time, p.reference_leak,
+                    p.reset_noise_std, ph.electrons_per_radiance, ph.dark_electrons, ph.integration_step]
+            assert list(out) == want
+
+
+def test_scene_create_rejects_invalid_arguments_on_host(lib):
+    V = np.zeros((3, 3), np.float32)
+    I = np.array([[0, 1, 5]], np.uint32)  # index outside the vertex array
+    cam = camera_struct(dict(width=4, height=4, fx=1, fy=1, cx=2, cy=2))
+    h = C.c_void_p()
+    fp = C.POINTER(C.c_float)
+    hap = hapke_struct(dict(b=.24, c=.3, hS=.08, hC=1, thetap=.4, w=.3, B_S0=2, B_C0=0, phi=.3))
+    r = lib.dvs_scene_create(V.ctypes.data_as(fp), V.ctypes.data_as(fp), I.ctypes.data_as(C.POINTER(C.c_uint32)),
+                             None, 3, 1, C.byref(cam), 1, C.byref(hap), None, C.byref(h))
+    assert r == _capi.DVS_ERR_INVALID and b"index" in lib.dvs_last_error()
+    bad = camera_struct(dict(width=0, height=4, fx=1, fy=1, cx=2, cy=2))
+    I = np.array([[0, 1, 2]], np.uint32)
+    r = lib.dvs_scene_create(V.ctypes.data_as(fp), V.ctypes.data_as(fp), I.ctypes.data_as(C.POINTER(C.c_uint32)),
+                             None, 3, 1, C.byref(bad), 1, C.byref(hap), None, C.byref(h))
+    assert r == _capi.DVS_ERR_INVALID
+    V[1, 0] = np.nan
+    r = lib.dvs_scene_create(V.ctypes.data_as(fp), V.ctypes.data_as(fp), I.ctypes.data_as(C.POINTER(C.c_uint32)),
+                             None, 3, 1, C.byref(cam), 1, C.byref(hap), None, C.byref(h))
+    assert r == _capi.DVS_ERR_INVALID and b"nonfinite" in lib.dvs_last_error()
+
+
+def test_sensor_calls_reject_null_handles(lib):
+    h = C.c_void_p()
+    assert lib.dvs_sensor_create(None, None, None, C.byref(h)) == _capi.DVS_ERR_INVALID
+    n = C.c_size_t()
+    assert lib.dvs_sensor_process(None, None, 0, C.byref(n)) == _capi.DVS_ERR_INVALID
+    assert lib.dvs_sensor_initialize(None, None, 0.0) == _capi.DVS_ERR_INVALID
+    assert lib.dvs_cam_render(None, None, None, None) == _capi.DVS_ERR_INVALID
