@@ -77,8 +77,14 @@ class Orbit:
                     rotation=yaw_quaternion(psi), intensity=self.intensity, intensity_rate=0.0)
 
 
-def horizons(trajectory, t_start, step, count):
-    """`count` contiguous intervals [t_k, t_k+1] with t_k = t_start + k*step."""
+def horizons(trajectory, t_start, step, count, float_step=True):
+    """`count` contiguous intervals [t_k, t_k+1] with t_k = t_start + k*step.
+
+    With float_step the step is first rounded to float, as the reference app
+    holds scene.time_resolution in a float (apps/main_dvs.cpp:302), so a
+    1e-6 s horizon spans exactly one 1e-6 circuit cell (also a float)."""
+    if float_step:
+        step = float(np.float32(step))
     out = []
     prev = trajectory.state(t_start)
     t_prev = float(t_start)

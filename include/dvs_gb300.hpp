@@ -1,0 +1,133 @@
+// C++17 facade over the dvs_gb300 C-ABI with the reference's class names and
+// call shapes, so that the reference's apps (apps/main_dvs.cpp,
+// apps/main_cam.cpp) and tests keep their structure when they switch to the
+// GB300 path.  Header-only; link against libdvs_gb300.so.
+//
+//   reference                                   here
+//   DeviceScene(bundle, config, root)            dvs_gb300::DeviceScene(mesh arrays, camera, ss, hapke)
+//     (include/dvs/device_scene.hpp:5-15)          -- builds the BVH itself; no BVHBuilder::build call
+//   EventSensor / DvsRayCaster                   dvs_gb300::DvsRayCaster
+//     initialize, advance, advance_many,           same names; events come back as std::vector<dvs_event>
+//     drain, dropped_events, peak_queue            (include/dvs/raycast.hpp:23-62)
+//   CamRayCaster::render_main                    dvs_gb300::CamRayCaster::render_main
+//     (include/dvs/raycast.hpp:64-86)              (quaternion pose instead of an Eigen matrix)
+//
+// Failures throw what the reference throws: std::invalid_argument for bad
+// inputs, std::runtime_error for device status and CUDA errors.
+#pragma once
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "dvs_gb300.h"
+
+namespace dvs_gb300 {
+
+inline void check(int status) {
+  if (status == DVS_OK) return;
+  const std::string msg = dvs_last_error();
+  if (status == DVS_ERR_INVALID) throw std::invalid_argument(msg);
+  throw std::runtime_error(msg);
+}
+
+class DeviceScene {
+ public:
+  DeviceScene(const std::vector<float> &vertices, const std::vector<float> &normals,
+              const std::vector<uint32_t> &indices, const dvs_camera &camera, int supersample,
+              const dvs_hapke &hapke, const std::vector<float> *albedos = nullptr, int leaf_size = 4) {
+    if (vertices.size() % 3 || normals.size() != vertices.size() || indices.size() % 3 ||
+        (albedos && albedos->size() * 3 != vertices.size()))
+      throw std::invalid_argument("invalid indexed mesh/BVH/material dimensions");
+    dvs_bvh_params params{};
+    params.leaf_size = leaf_size;
+    dvs_scene *s = nullptr;
+    check(dvs_scene_create(vertices.data(), normals.data(), indices.data(), albedos ? albedos->data() : nullptr,
+                           vertices.size() / 3, indices.size() / 3, &camera, supersample, &hapke, &params, &s));
+    scene_.reset(s);
+    camera_ = camera;
+  }
+  dvs_scene *get() const { return scene_.get(); }
+  const dvs_camera &camera() const { return camera_; }
+  dvs_scene_info info() const {
+    dvs_scene_info i{};
+    check(dvs_scene_info_get(scene_.get(), &i));
+    return i;
+  }
+
+ private:
+  struct Deleter {
+    void operator()(dvs_scene *s) const { dvs_scene_destroy(s); }
+  };
+  std::unique_ptr<dvs_scene, Deleter> scene_;
+  dvs_camera camera_{};
+};
+
+class DvsRayCaster {
+ public:
+  DvsRayCaster(std::shared_ptr<DeviceScene> scene, const dvs_physic &physic, const dvs_sensor_options *options = nullptr)
+      : scene_(std::move(scene)) {
+    dvs_sensor *s = nullptr;
+    check(dvs_sensor_create(scene_->get(), &physic, options, &s));
+    sensor_.reset(s);
+  }
+  void initialize(const dvs_optical_state &state, double timestamp) {
+    check(dvs_sensor_initialize(sensor_.get(), &state, timestamp));
+  }
+  void advance(const dvs_optical_state &start, const dvs_optical_state &end, double t0, double t1,
+               std::vector<dvs_event> &events) {
+    dvs_optical_interval iv{start, end, t0, t1};
+    advance_many(std::vector<dvs_optical_interval>{iv}, events);
+  }
+  void advance_many(const std::vector<dvs_optical_interval> &intervals, std::vector<dvs_event> &events) {
+    size_t n = 0;
+    check(dvs_sensor_process(sensor_.get(), intervals.data(), intervals.size(), &n));
+    read(n, events);
+  }
+  void drain(std::vector<dvs_event> &events) {
+    events.clear();
+    std::vector<dvs_event> chunk(1 << 16);
+    for (;;) {
+      size_t got = 0;
+      check(dvs_sensor_drain(sensor_.get(), chunk.data(), chunk.size(), &got));
+      events.insert(events.end(), chunk.begin(), chunk.begin() + got);
+      if (got < chunk.size()) break;
+    }
+  }
+  dvs_sensor_stats stats() const {
+    dvs_sensor_stats st{};
+    check(dvs_sensor_stats_get(sensor_.get(), &st));
+    return st;
+  }
+  std::size_t dropped_events() const { return stats().dropped; }
+  std::size_t peak_queue() const { return stats().peak_queue; }
+
+ private:
+  void read(size_t n, std::vector<dvs_event> &events) {
+    events.resize(n);
+    size_t got = 0;
+    if (n) check(dvs_sensor_read(sensor_.get(), events.data(), n, &got));
+    events.resize(got);
+  }
+  struct Deleter {
+    void operator()(dvs_sensor *s) const { dvs_sensor_destroy(s); }
+  };
+  std::shared_ptr<DeviceScene> scene_;
+  std::unique_ptr<dvs_sensor, Deleter> sensor_;
+};
+
+class CamRayCaster {
+ public:
+  explicit CamRayCaster(std::shared_ptr<DeviceScene> scene) : scene_(std::move(scene)) {}
+  void render_main(const dvs_optical_state &pose, std::vector<float> &light_frame, std::vector<float> &depth_map) {
+    const size_t n = size_t(scene_->camera().width) * scene_->camera().height;
+    light_frame.resize(n);
+    depth_map.resize(n);
+    check(dvs_cam_render(scene_->get(), &pose, light_frame.data(), depth_map.data()));
+  }
+
+ private:
+  std::shared_ptr<DeviceScene> scene_;
+};
+
+}  // namespace dvs_gb300

@@ -84,6 +84,36 @@ def test_scene_create_rejects_invalid_arguments_on_host(lib):
     assert r == _capi.DVS_ERR_INVALID and b"nonfinite" in lib.dvs_last_error()
 
 
+def test_cpp_facade_compiles_links_and_throws(lib, tmp_path):
+    """The C++17 facade (include/dvs_gb300.hpp) builds against the library and
+    maps an invalid argument to std::invalid_argument, as the reference does."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "facade.cpp"
+    src.write_text(r'''
+#include "dvs_gb300.hpp"
+#include <cstdio>
+int main() {
+  dvs_camera cam{4, 4, 1.f, 1.f, 2.f, 2.f};
+  dvs_hapke hap{.24f, .3f, .08f, 1.f, .4f, .3f, 2.f, 0.f, .3f};
+  std::vector<float> v(9, 0.f), n(9, 0.f);
+  std::vector<uint32_t> i{0, 1, 7};
+  try { dvs_gb300::DeviceScene s(v, n, i, cam, 1, hap); }
+  catch (const std::invalid_argument &e) { std::printf("invalid_argument: %s\n", e.what()); return 0; }
+  return 1;
+}
+''')
+    exe = tmp_path / "facade"
+    r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                        _capi.library_path(), "-Wl,-rpath," + os.path.dirname(_capi.library_path())],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "index" in r.stdout, r.stdout + r.stderr
+
+
 def test_sensor_calls_reject_null_handles(lib):
     h = C.c_void_p()
     assert lib.dvs_sensor_create(None, None, None, C.byref(h)) == _capi.DVS_ERR_INVALID
