@@ -88,7 +88,7 @@ EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_d
            "dvs_scene_create", "dvs_scene_destroy", "dvs_scene_info_get", "dvs_cam_render", "dvs_sensor_create",
            "dvs_sensor_destroy", "dvs_sensor_initialize", "dvs_sensor_process", "dvs_sensor_read",
            "dvs_sensor_process_events", "dvs_sensor_enqueue", "dvs_sensor_collect", "dvs_sensor_drain", "dvs_sensor_stats_get", "dvs_sensor_stats_reset",
-           "dvs_sensor_stream", "dvs_sensor_read_state")
+           "dvs_sensor_stream", "dvs_sensor_read_state", "dvs_cam_render_noalloc")
 
 _LIB = None
 
@@ -119,6 +119,7 @@ def _declare(lib):
     lib.dvs_sensor_stream.argtypes = [vp]
     lib.dvs_sensor_stream.restype = vp
     lib.dvs_sensor_read_state.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+    lib.dvs_cam_render_noalloc.argtypes = [vp, vp, vp, vp, vp]
     return lib
 
 

@@ -28,7 +28,7 @@ def nvcc():
 
 
 def _sources():
-    return [os.path.join(CSRC, f) for f in ("kernels.cu", "capi.cu", "bvh4_build.cpp", "readout.cpp")]
+    return [os.path.join(CSRC, f) for f in ("kernels.cu", "capi.cu", "noalloc.cu", "bvh4_build.cpp", "readout.cpp")]
 
 
 def _headers():

@@ -213,6 +213,11 @@ struct dvs_sensor {
   std::vector<int> timer_kind;  // 0 optics, 1 circuit, 2 events
 };
 
+// Accessors for the no-allocation entry point (noalloc.cu).
+SceneView dvsgb_scene_view(const dvs_scene *scene) { return scene->view(); }
+int dvsgb_scene_device(const dvs_scene *scene) { return scene->device; }
+int dvsgb_set_error(int code, const char *message) { return fail(code, message); }
+
 extern "C" {
 
 const char *dvs_last_error(void) { return g_last_error.c_str(); }

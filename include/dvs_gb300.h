@@ -154,6 +154,24 @@ int dvs_scene_info_get(const dvs_scene *scene, dvs_scene_info *out);
 /* radiance and depth: width*height floats each (host pointers); depth may be NULL. */
 int dvs_cam_render(dvs_scene *scene, const dvs_optical_state *pose, float *radiance, float *depth);
 
+/* Camera render that allocates no memory.  No counterpart in the reference.
+ * For callers that cannot allocate device memory while rendering: a frame
+ * loop under a fixed device-memory budget, a host framework that owns all
+ * device memory through its own pool, or a latency-critical path where
+ * cudaMalloc/cudaFree may stall or synchronize the device.
+ * radiance and depth are DEVICE pointers of width*height floats (row-major;
+ * depth may be NULL); the work is enqueued on `stream` (a cudaStream_t, NULL
+ * for the default stream) and the call returns without waiting.  Samples that
+ * could not be traced are NaN in `radiance`.
+ * Intermediates live in one library-owned static device array sized for at
+ * most 1280x720 pixels (about 11 MB, held on every GPU that loads the library
+ * until the process exits); larger images are rejected with DVS_ERR_INVALID.
+ * The first call on a device looks up that array's device address (once per
+ * device), so make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race on it. */
+int dvs_cam_render_noalloc(dvs_scene *scene, const dvs_optical_state *pose, float *radiance, float *depth,
+                           void *stream);
+
 /* ---- event sensor: replaces EventSensor (src/cuda/event_sensor.cu:244-305) ---- */
 int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sensor_options *options,
                       dvs_sensor **out);
