@@ -60,7 +60,8 @@ class Physic(C.Structure):
 
 class SensorOptions(C.Structure):
     _fields_ = [("physic_effects", C.c_int32), ("aer_delay", C.c_int32), ("cells_per_chunk", C.c_int32),
-                ("cells_per_warp", C.c_int32), ("timing", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("cells_per_warp", C.c_int32), ("timing", C.c_int32), ("row_begin", C.c_int32),
+                ("row_end", C.c_int32), ("reserved", C.c_int32)]
 
 
 class BvhParams(C.Structure):
@@ -88,7 +89,26 @@ EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_d
            "dvs_scene_create", "dvs_scene_destroy", "dvs_scene_info_get", "dvs_cam_render", "dvs_sensor_create",
            "dvs_sensor_destroy", "dvs_sensor_initialize", "dvs_sensor_process", "dvs_sensor_read",
            "dvs_sensor_process_events", "dvs_sensor_enqueue", "dvs_sensor_collect", "dvs_sensor_drain", "dvs_sensor_stats_get", "dvs_sensor_stats_reset",
-           "dvs_sensor_stream", "dvs_sensor_read_state", "dvs_cam_render_noalloc")
+           "dvs_sensor_stream", "dvs_sensor_read_state", "dvs_cam_render_noalloc", "dvs_sensor_process_adaptive",
+           "dvs_sensor_refinement_stats", "dvs_sensor_last_convergence", "dvs_sensor_adaptive_capacity",
+           "dvs_readout_create", "dvs_readout_destroy", "dvs_readout_submit", "dvs_readout_drain", "dvs_readout_read",
+           "dvs_readout_counters")
+
+
+class RefinementStats(C.Structure):
+    _fields_ = [("traced_pixel_samples", C.c_uint64), ("fallback_pixels", C.c_int32), ("maximum_knots", C.c_int32),
+                ("exact_segments", C.c_int32), ("native_cell_queries", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ReceptorProbe(C.Structure):
+    _fields_ = [("maximum_log_voltage_error", C.c_double), ("p99_log_voltage_error", C.c_double),
+                ("mean_log_voltage_error", C.c_double), ("pixels", C.c_int32), ("circuit_cells", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 _LIB = None
 
@@ -120,6 +140,17 @@ def _declare(lib):
     lib.dvs_sensor_stream.restype = vp
     lib.dvs_sensor_read_state.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
     lib.dvs_cam_render_noalloc.argtypes = [vp, vp, vp, vp, vp]
+    lib.dvs_sensor_process_adaptive.argtypes = [vp, vp, sz, C.c_double, C.c_int32, C.POINTER(C.c_int32),
+                                                C.POINTER(sz)]
+    lib.dvs_sensor_refinement_stats.argtypes = [vp, C.POINTER(RefinementStats)]
+    lib.dvs_sensor_last_convergence.argtypes = [vp, C.POINTER(ReceptorProbe)]
+    lib.dvs_sensor_adaptive_capacity.argtypes = [vp, C.POINTER(C.c_int32)]
+    lib.dvs_readout_create.argtypes = [C.c_double, C.c_double, sz, C.POINTER(vp)]
+    lib.dvs_readout_destroy.argtypes = [vp]
+    lib.dvs_readout_submit.argtypes = [vp, vp, sz, C.c_double, C.POINTER(sz)]
+    lib.dvs_readout_drain.argtypes = [vp, C.POINTER(sz)]
+    lib.dvs_readout_read.argtypes = [vp, vp, sz, C.POINTER(sz)]
+    lib.dvs_readout_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     return lib
 
 

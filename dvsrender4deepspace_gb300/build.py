@@ -28,11 +28,11 @@ def nvcc():
 
 
 def _sources():
-    return [os.path.join(CSRC, f) for f in ("kernels.cu", "capi.cu", "noalloc.cu", "bvh4_build.cpp", "readout.cpp")]
+    return [os.path.join(CSRC, f) for f in ("kernels.cu", "adaptive.cu", "capi.cu", "noalloc.cu", "bvh_build.cpp", "readout.cpp")]
 
 
 def _headers():
-    return [os.path.join(CSRC, f) for f in ("kernels.h", "dvs_internal.h")] + [
+    return [os.path.join(CSRC, f) for f in ("kernels.h", "dvs_internal.h", "device_optics.cuh", "device_circuit.cuh")] + [
         os.path.join(ROOT, "include", "dvs_gb300.h")]
 
 

@@ -1,4 +1,4 @@
-// Host builder of the 4-wide BVH.
+// Host builder of the 8-wide BVH.
 //
 // Replaces the reference's single-threaded recursive binned-SAH builder
 // (src/bvh/build.cpp:27-174, src/bvh/bining.cpp:9-182).  Design:
@@ -7,7 +7,7 @@
 //   2. parallel LSD radix sort of (code, triangle);
 //   3. top-down radix splits at the highest differing code bit, giving a
 //      binary tree over contiguous leaf ranges (<= leaf_size triangles);
-//   4. collapse to 4-wide nodes by repeatedly opening the largest-area inner
+//   4. collapse to 8-wide nodes by repeatedly opening the largest-area inner
 //      child; nodes are numbered breadth-first so the top levels are first.
 // All passes are O(n) or O(n log n) and OpenMP-parallel.
 #include <algorithm>
@@ -175,7 +175,7 @@ struct TreeBuilder {
 
 }  // namespace
 
-bool build_bvh4(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf_size, Bvh4Build &out,
+bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf_size, BvhBuild &out,
                 std::string &error) {
   const auto t_start = std::chrono::steady_clock::now();
   if (nt == 0 || nv == 0) { error = "empty mesh"; return false; }
@@ -240,24 +240,24 @@ bool build_bvh4(const float *V, size_t nv, const uint32_t *I, size_t nt, int lea
   root = tb.build(0, (int32_t)nt);
   bin.resize(tb.next.load());
 
-  // 4. collapse to 4-wide, breadth first
-  std::vector<Bvh4Node> nodes;
-  nodes.reserve(bin.size() / 2 + 2);
-  std::vector<int32_t> queue;  // binary node per 4-wide node
+  // 4. collapse to kBvhWidth-wide, breadth first
+  std::vector<BvhNode> nodes;
+  nodes.reserve(bin.size() / (kBvhWidth - 1) + 2);
+  std::vector<int32_t> queue;  // binary node per wide node
   std::vector<int32_t> level;
   queue.push_back(root);
   level.push_back(1);
   int depth = 1;
   for (size_t qi = 0; qi < queue.size(); ++qi) {
     const int32_t b = queue[qi];
-    int32_t kids[4];
+    int32_t kids[kBvhWidth];
     int nk = 0;
     if (bin[b].count > 0) {
       kids[nk++] = b;  // a leaf root: one leaf child
     } else {
       kids[nk++] = bin[b].left;
       kids[nk++] = bin[b].right;
-      while (nk < 4) {
+      while (nk < kBvhWidth) {
         int best = -1;
         float best_area = -1;
         for (int k = 0; k < nk; ++k)
@@ -268,24 +268,23 @@ bool build_bvh4(const float *V, size_t nv, const uint32_t *I, size_t nt, int lea
         kids[nk++] = bin[open].right;
       }
     }
-    Bvh4Node node;
+    BvhNode node;
     std::memset(&node, 0, sizeof(node));
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < kBvhWidth; ++k) {
+      BvhChild &out_child = node.c[k];
       if (k >= nk) {
-        node.child[k] = -1;
-        node.count[k] = -1;
+        out_child.child = -1;
+        out_child.count = -1;
         continue;
       }
       const BinNode &c = bin[kids[k]];
-      node.lo_x[k] = c.box.lo[0]; node.hi_x[k] = c.box.hi[0];
-      node.lo_y[k] = c.box.lo[1]; node.hi_y[k] = c.box.hi[1];
-      node.lo_z[k] = c.box.lo[2]; node.hi_z[k] = c.box.hi[2];
+      for (int d = 0; d < 3; ++d) { out_child.lo[d] = c.box.lo[d]; out_child.hi[d] = c.box.hi[d]; }
       if (c.count > 0) {
-        node.child[k] = c.start;
-        node.count[k] = c.count;
+        out_child.child = c.start;
+        out_child.count = c.count;
       } else {
-        node.child[k] = (int32_t)queue.size();
-        node.count[k] = 0;
+        out_child.child = (int32_t)queue.size();
+        out_child.count = 0;
         queue.push_back(kids[k]);
         level.push_back(level[qi] + 1);
         depth = std::max(depth, level[qi] + 1);
@@ -293,7 +292,7 @@ bool build_bvh4(const float *V, size_t nv, const uint32_t *I, size_t nt, int lea
     }
     nodes.push_back(node);
   }
-  if (3 * depth + 1 > kStackSlots) {
+  if ((kBvhWidth - 1) * depth + 1 > kStackSlots) {
     error = "BVH too deep for the traversal stack (depth " + std::to_string(depth) + ")";
     return false;
   }

@@ -127,13 +127,15 @@ struct dvs_scene {
   bool has_albedo = false;
   void *arena = nullptr;
   size_t arena_bytes = 0;
-  Bvh4Node *nodes = nullptr;
+  BvhNode *nodes = nullptr;
   TriRecord *tris = nullptr;
   ShadeRecord *shade = nullptr;
   int32_t *pixel_of_rank = nullptr;
+  std::vector<int32_t> rank_of_pixel;  // host inverse of pixel_of_rank
   size_t n_nodes = 0, n_tris = 0, n_vertices = 0;
   int depth = 0;
   double build_seconds = 0;
+  float coherent_span = 1.0f;  // 0.5 % of the scene's largest extent
   // camera render buffers
   cudaStream_t stream = nullptr;
   double *cam_radiance = nullptr;
@@ -156,6 +158,7 @@ struct dvs_scene {
     v.fy = camera.fy;
     v.cx = camera.cx;
     v.cy = camera.cy;
+    v.coherent_span = coherent_span;
     v.hapke = hapke;
     return v;
   }
@@ -211,6 +214,31 @@ struct dvs_sensor {
   std::vector<cudaEvent_t> timers;
   size_t timers_used = 0;
   std::vector<int> timer_kind;  // 0 optics, 1 circuit, 2 events
+  // adaptive optics (OpticalSampler caches, optical_sampler.hpp:305-313)
+  int knot_capacity = 0;  // chosen from free memory on first use
+  OpticalKnot *knots = nullptr;
+  int32_t *knot_counts = nullptr, *exact_cells = nullptr, *exact_counts = nullptr, *exact_queue = nullptr;
+  int32_t *exact_total = nullptr, *fallback_list = nullptr, *fallback_total = nullptr;
+  double *exact_radiance = nullptr;
+  unsigned long long *ref_stats = nullptr, *h_ref = nullptr;
+  int32_t *probe_ranks = nullptr;
+  double *probe_state = nullptr;
+  int n_probes = 0;
+  dvs_refinement_stats refine{};
+  dvs_receptor_probe convergence{};
+  // pixels this sensor owns: the whole image, or rows [row_begin, row_end)
+  // (one GPU's share when several GPUs split a sensor), in Morton order
+  int n_pix = 0;
+  int row_begin = 0;
+  const int32_t *order = nullptr;    // device: rank -> row-major pixel of the full image
+  int32_t *own_order = nullptr;      // allocated when the sensor covers a row band
+  std::vector<int32_t> band_rank_of_pixel;  // band-local row-major pixel -> rank
+  int pixels() const { return n_pix; }
+  SceneView view() const {
+    SceneView v = scene->view();
+    v.pixel_of_rank = order;
+    return v;
+  }
 };
 
 // Accessors for the no-allocation entry point (noalloc.cu).
@@ -261,9 +289,9 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
     if (!std::isfinite(normals[i])) return fail(DVS_ERR_INVALID, "nonfinite mesh normal");
   const int leaf = params && params->leaf_size > 0 ? params->leaf_size : 4;
 
-  Bvh4Build bvh;
+  BvhBuild bvh;
   std::string err;
-  if (!build_bvh4(vertices, n_vertices, indices, n_triangles, leaf, bvh, err)) return fail(DVS_ERR_INVALID, err);
+  if (!build_bvh(vertices, n_vertices, indices, n_triangles, leaf, bvh, err)) return fail(DVS_ERR_INVALID, err);
 
   // leaf-order records
   std::vector<TriRecord> tris(n_triangles);
@@ -306,9 +334,18 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   s->n_vertices = n_vertices;
   s->depth = bvh.depth;
   s->build_seconds = bvh.seconds;
+  {
+    float lo[3] = {vertices[0], vertices[1], vertices[2]}, hi[3] = {vertices[0], vertices[1], vertices[2]};
+    for (size_t i = 0; i < n_vertices; ++i)
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = std::min(lo[d], vertices[3 * i + d]);
+        hi[d] = std::max(hi[d], vertices[3 * i + d]);
+      }
+    s->coherent_span = 0.005f * std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1.0f});
+  }
   cudaGetDevice(&s->device);
   const size_t off_nodes = 0;
-  const size_t off_tris = align_up(off_nodes + sizeof(Bvh4Node) * s->n_nodes, 256);
+  const size_t off_tris = align_up(off_nodes + sizeof(BvhNode) * s->n_nodes, 256);
   const size_t off_shade = align_up(off_tris + sizeof(TriRecord) * n_triangles, 256);
   const size_t off_pix = align_up(off_shade + sizeof(ShadeRecord) * n_triangles, 256);
   const size_t total = align_up(off_pix + sizeof(int32_t) * order.size(), 256);
@@ -319,11 +356,13 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   }
   s->arena_bytes = total;
   char *base = static_cast<char *>(s->arena);
-  s->nodes = reinterpret_cast<Bvh4Node *>(base + off_nodes);
+  s->nodes = reinterpret_cast<BvhNode *>(base + off_nodes);
   s->tris = reinterpret_cast<TriRecord *>(base + off_tris);
   s->shade = reinterpret_cast<ShadeRecord *>(base + off_shade);
   s->pixel_of_rank = reinterpret_cast<int32_t *>(base + off_pix);
-  e = cudaMemcpy(s->nodes, bvh.nodes.data(), sizeof(Bvh4Node) * s->n_nodes, cudaMemcpyHostToDevice);
+  s->rank_of_pixel.assign(order.size(), 0);
+  for (size_t r = 0; r < order.size(); ++r) s->rank_of_pixel[order[r]] = (int32_t)r;
+  e = cudaMemcpy(s->nodes, bvh.nodes.data(), sizeof(BvhNode) * s->n_nodes, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->tris, tris.data(), sizeof(TriRecord) * n_triangles, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(s->shade, shade.data(), sizeof(ShadeRecord) * n_triangles, cudaMemcpyHostToDevice);
@@ -408,7 +447,13 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
   if (!out) return fail(DVS_ERR_INVALID, "null output handle");
   *out = nullptr;
   if (!scene || !physic) return fail(DVS_ERR_INVALID, "null scene or physic configuration");
-  const int n = scene->pixels();
+  dvs_sensor_options opt;
+  if (options) opt = *options; else dvs_sensor_options_default(&opt);
+  const int H = scene->camera.height, W = scene->camera.width;
+  const bool band = opt.row_end > opt.row_begin;
+  if (band && (opt.row_begin < 0 || opt.row_end > H))
+    return fail(DVS_ERR_INVALID, "sensor row band outside the image");
+  const int n = band ? (opt.row_end - opt.row_begin) * W : scene->pixels();
   if (physic->max_events_per_step < 1 || physic->max_events_per_step > 64 ||
       (long long)n * physic->max_events_per_step > std::numeric_limits<int>::max())
     return fail(DVS_ERR_INVALID, "invalid sensor capacity");
@@ -416,7 +461,9 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
   dvs_sensor *s = new dvs_sensor;
   s->scene = scene;
   s->physic = *physic;
-  if (options) s->opt = *options; else dvs_sensor_options_default(&s->opt);
+  s->opt = opt;
+  s->n_pix = n;
+  s->order = scene->pixel_of_rank;
   derive(*physic, s->opt.physic_effects != 0, s->p, s->photo);
   s->threshold_std = s->opt.physic_effects ? physic->threshold_std : 0;
   s->threshold_min = physic->threshold_min;
@@ -433,6 +480,23 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
   cudaError_t e;
 #define ALLOC(ptr, bytes, what)                 \
   if ((e = cudaMalloc(&(ptr), (bytes))) != cudaSuccess) return bail(e, what);
+  if (band) {
+    // the band's pixels in the scene's Morton order; RNG subsequences and ray
+    // geometry stay those of the full-image pixel
+    s->row_begin = opt.row_begin;
+    std::vector<int32_t> mine;
+    mine.reserve(n);
+    std::vector<int32_t> order_host(scene->pixels());
+    for (int p = 0; p < scene->pixels(); ++p) order_host[scene->rank_of_pixel[p]] = p;
+    for (int32_t p : order_host)
+      if (p / W >= opt.row_begin && p / W < opt.row_end) mine.push_back(p);
+    s->band_rank_of_pixel.assign(n, 0);
+    for (size_t r = 0; r < mine.size(); ++r) s->band_rank_of_pixel[mine[r] - opt.row_begin * W] = (int32_t)r;
+    ALLOC(s->own_order, sizeof(int32_t) * n, "sensor pixel order");
+    if ((e = cudaMemcpy(s->own_order, mine.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return bail(e, "sensor pixel order");
+    s->order = s->own_order;
+  }
   ALLOC(s->st.receptor_log, sizeof(double) * n, "pixel states");
   ALLOC(s->st.reference_log, sizeof(double) * n, "pixel states");
   ALLOC(s->st.refractory_until, sizeof(double) * n, "pixel states");
@@ -487,6 +551,20 @@ int dvs_sensor_destroy(dvs_sensor *s) {
   if (s->h_status) cudaFreeHost(s->h_status);
   if (s->h_state) cudaFreeHost(s->h_state);
   for (cudaEvent_t ev : s->timers) cudaEventDestroy(ev);
+  cudaFree(s->own_order);
+  cudaFree(s->knots);
+  cudaFree(s->knot_counts);
+  cudaFree(s->exact_cells);
+  cudaFree(s->exact_counts);
+  cudaFree(s->exact_queue);
+  cudaFree(s->exact_total);
+  cudaFree(s->exact_radiance);
+  cudaFree(s->fallback_list);
+  cudaFree(s->fallback_total);
+  cudaFree(s->ref_stats);
+  cudaFree(s->probe_ranks);
+  cudaFree(s->probe_state);
+  if (s->h_ref) cudaFreeHost(s->h_ref);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s->readout;
   delete s;
@@ -503,7 +581,7 @@ static int map_error(int32_t word) {
 }
 
 static cudaError_t ensure_radiance(dvs_sensor *s, size_t cells) {
-  return grow_device(s->radiance, s->radiance_cap, cells * (size_t)s->scene->pixels());
+  return grow_device(s->radiance, s->radiance_cap, cells * (size_t)s->pixels());
 }
 
 int dvs_sensor_initialize(dvs_sensor *s, const dvs_optical_state *pose, double timestamp) {
@@ -511,7 +589,7 @@ int dvs_sensor_initialize(dvs_sensor *s, const dvs_optical_state *pose, double t
   if (!s || !pose || !std::isfinite(timestamp) || s->initialized)
     return fail(DVS_ERR_INVALID, "invalid sensor initialization");
   CUDA_TRY(cudaSetDevice(s->device), "select device");
-  const int n = s->scene->pixels();
+  const int n = s->pixels();
   CUDA_TRY(ensure_radiance(s, 1), "initial radiance");
   CUDA_TRY(grow_device(s->poses, s->poses_cap, 1), "pose buffer");
   *s->h_state = *pose;
@@ -519,9 +597,9 @@ int dvs_sensor_initialize(dvs_sensor *s, const dvs_optical_state *pose, double t
            "upload pose");
   CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream), "clear initialization error");
   CUDA_TRY(launch_pose_from_state(s->d_state, s->poses, s->stream), "pose");
-  CUDA_TRY(launch_trace_cells(s->scene->view(), n, s->poses, 0, 1, 0, s->radiance, nullptr, s->counters, s->stream),
+  CUDA_TRY(launch_trace_cells(s->view(), n, s->poses, 0, 1, 0, s->radiance, nullptr, s->counters, s->stream),
            "initial optics");
-  CUDA_TRY(launch_init_pixels(n, s->scene->pixel_of_rank, s->radiance, s->p, s->photo, s->threshold_std,
+  CUDA_TRY(launch_init_pixels(n, s->order, s->radiance, s->p, s->photo, s->threshold_std,
                               s->threshold_min, s->seed, s->st, s->error_word, s->stream),
            "initialize circuit");
   CUDA_TRY(cudaMemcpyAsync(s->h_status + 1, s->error_word, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream),
@@ -546,9 +624,9 @@ static void record_timer(dvs_sensor *s, int kind) {
   cudaEventRecord(s->timers[s->timers_used++], s->stream);
 }
 
-// Validates and uploads the batch, then enqueues every kernel of the hot path
-// on the sensor stream without waiting (upload_intervals + generate_pixels).
-static int enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count) {
+// Validates the batch, builds its circuit cells, uploads both and launches
+// the per-cell pose kernel (upload_intervals, event_sensor.cu:274-289).
+static int upload_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, size_t &n_cells_out) {
   if (!s || !s->initialized || !ivs || count == 0) return fail(DVS_ERR_INVALID, "sensor not initialized or no intervals");
   if (count > (size_t)std::numeric_limits<int>::max()) return fail(DVS_ERR_INVALID, "too many intervals");
   // upload_intervals (event_sensor.cu:274-289)
@@ -581,31 +659,53 @@ static int enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count)
     }
   }
   std::memcpy(s->h_ivs, ivs, sizeof(dvs_optical_interval) * count);
-  const int n = s->scene->pixels();
-  size_t chunk = s->opt.cells_per_chunk > 0 ? (size_t)s->opt.cells_per_chunk
-                                             : std::max<size_t>(1, std::min<size_t>(2048, (size_t(512) << 20) / (8 * (size_t)n)));
-  chunk = std::min(chunk, n_cells);
-  int cw_log2;
-  if (s->opt.cells_per_warp > 0) {
-    cw_log2 = 0;
-    while ((2 << cw_log2) <= std::min(32, s->opt.cells_per_warp)) ++cw_log2;
-  } else {
-    cw_log2 = 0;
-    while (cw_log2 < 5 && (size_t(2) << cw_log2) <= chunk) ++cw_log2;
-  }
   CUDA_TRY(grow_device(s->ivs, s->ivs_cap, count), "trajectory interval allocation");
   CUDA_TRY(grow_device(s->cells, s->cells_cap, n_cells), "cell allocation");
   CUDA_TRY(grow_device(s->poses, s->poses_cap, n_cells), "pose allocation");
-  CUDA_TRY(ensure_radiance(s, chunk), "radiance chunk allocation");
   CUDA_TRY(cudaMemcpyAsync(s->ivs, s->h_ivs, sizeof(dvs_optical_interval) * count, cudaMemcpyHostToDevice, s->stream),
            "trajectory interval upload");
   CUDA_TRY(cudaMemcpyAsync(s->cells, s->h_cells, sizeof(Cell) * n_cells, cudaMemcpyHostToDevice, s->stream),
            "cell upload");
+  CUDA_TRY(launch_cell_poses(s->ivs, s->cells, (int)n_cells, s->poses, s->stream), "cell poses");
+  s->stats.launches += 1;
+  n_cells_out = n_cells;
+  return DVS_OK;
+}
+
+// Cells per optics launch and cells per warp packet for a batch.
+static void chunk_shape(const dvs_sensor *s, size_t n_cells, size_t rows, size_t &chunk, int &cw_log2) {
+  chunk = s->opt.cells_per_chunk > 0 ? (size_t)s->opt.cells_per_chunk
+                                     : std::max<size_t>(1, std::min<size_t>(2048, (size_t(512) << 20) / (8 * rows)));
+  chunk = std::min(chunk, n_cells);
+  cw_log2 = 0;
+  if (s->opt.cells_per_warp > 0) {
+    while ((2 << cw_log2) <= std::min(32, s->opt.cells_per_warp)) ++cw_log2;
+  } else {
+    while (cw_log2 < 5 && (size_t(2) << cw_log2) <= chunk) ++cw_log2;
+  }
+}
+
+static int clear_batch_outputs(dvs_sensor *s) {
+  const int n = s->pixels();
   CUDA_TRY(cudaMemsetAsync(s->ev_count, 0, sizeof(int32_t) * n, s->stream), "clear events");
   CUDA_TRY(cudaMemsetAsync(s->event_total, 0, sizeof(int32_t), s->stream), "clear events");
   CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream), "clear status");
-  CUDA_TRY(launch_cell_poses(s->ivs, s->cells, (int)n_cells, s->poses, s->stream), "cell poses");
-  const SceneView view = s->scene->view();
+  return DVS_OK;
+}
+
+// Validates and uploads the batch, then enqueues every kernel of the hot path
+// on the sensor stream without waiting (upload_intervals + generate_pixels).
+static int enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count) {
+  size_t n_cells = 0;
+  int r = upload_batch(s, ivs, count, n_cells);
+  if (r) return r;
+  const int n = s->pixels();
+  size_t chunk;
+  int cw_log2;
+  chunk_shape(s, n_cells, (size_t)n, chunk, cw_log2);
+  CUDA_TRY(ensure_radiance(s, chunk), "radiance chunk allocation");
+  if ((r = clear_batch_outputs(s))) return r;
+  const SceneView view = s->view();
   for (size_t c0 = 0; c0 < n_cells; c0 += chunk) {
     const int nc = (int)std::min(chunk, n_cells - c0);
     record_timer(s, 0);
@@ -620,14 +720,14 @@ static int enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count)
     s->stats.circuit_launches += 1;
   }
   record_timer(s, 2);
-  CUDA_TRY(launch_emit_events(n, s->scene->pixel_of_rank, s->scene->camera.width, s->max_events, s->ev_count,
+  CUDA_TRY(launch_emit_events(n, s->order, s->scene->camera.width, s->max_events, s->ev_count,
                               s->slab_t, s->slab_p, s->events, s->event_total, s->stream),
            "compact events");
   CUDA_TRY(launch_event_depth(view, s->ivs, (int)count, s->events, s->event_total, s->error_word, s->counters,
                               s->stream),
            "event depth");
   record_timer(s, 3);
-  s->stats.launches += 3;
+  s->stats.launches += 2;
   s->last_time = ivs[count - 1].t1;
   return DVS_OK;
 }
@@ -696,6 +796,229 @@ int dvs_sensor_enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t co
   if (r) return r;
   s->pending = true;
   s->pending_end = ivs[count - 1].t1;
+  return DVS_OK;
+}
+
+// ---- adaptive optics (EventSensor::process_adaptive, event_sensor.cu:306-374) ----
+// Cache capacity from free memory as OpticalSampler::OpticalSampler does
+// (optical_sampler.cu:141-152): 512, 256 or 128 knots per pixel.
+static int ensure_adaptive(dvs_sensor *s) {
+  if (s->knot_capacity) return DVS_OK;
+  const size_t n = (size_t)s->pixels();
+  size_t available = 0, total = 0;
+  CUDA_TRY(cudaMemGetInfo(&available, &total), "query optical cache memory budget");
+  int cap = 128;
+  for (int candidate : {512, 256, 128}) {
+    const size_t needed = n * candidate * (16 + 24 + 8 + 4);  // knot, exact cell, radiance, queue slot
+    if (available > needed + (size_t(1) << 30)) {
+      cap = candidate;
+      break;
+    }
+  }
+  CUDA_TRY(cudaMalloc(&s->knots, sizeof(OpticalKnot) * n * cap), "allocate pixel optical knots");
+  CUDA_TRY(cudaMalloc(&s->knot_counts, sizeof(int32_t) * n), "allocate optical knot counts");
+  CUDA_TRY(cudaMalloc(&s->exact_counts, sizeof(int32_t) * n), "allocate local exact cell counts");
+  CUDA_TRY(cudaMalloc(&s->exact_total, sizeof(int32_t)), "allocate exact query count");
+  CUDA_TRY(cudaMalloc(&s->fallback_list, sizeof(int32_t) * n), "allocate exact fallback pixel IDs");
+  CUDA_TRY(cudaMalloc(&s->fallback_total, sizeof(int32_t)), "allocate exact fallback count");
+  CUDA_TRY(cudaMalloc(&s->ref_stats, sizeof(unsigned long long) * kRefSlots), "allocate refinement statistics");
+  CUDA_TRY(cudaMallocHost(&s->h_ref, sizeof(unsigned long long) * (kRefSlots + 4)), "refinement staging");
+  // receptor-convergence probes: 1024 hashed pixels (event_sensor.cu:359-360)
+  s->n_probes = (int)std::min<size_t>(1024, n);
+  std::vector<int32_t> ranks(s->n_probes);
+  for (int i = 0; i < s->n_probes; ++i) {
+    // the sensor's i-th hashed pixel in row-major order of its own rows
+    const size_t local = (size_t)((uint64_t(i) * 2654435761ULL) % n);
+    const size_t pixel = (size_t)s->row_begin * s->scene->camera.width + local;
+    ranks[i] = s->band_rank_of_pixel.empty() ? s->scene->rank_of_pixel[pixel]
+                                             : s->band_rank_of_pixel[local];
+  }
+  CUDA_TRY(cudaMalloc(&s->probe_ranks, sizeof(int32_t) * s->n_probes), "allocate mean receptor probes");
+  CUDA_TRY(cudaMalloc(&s->probe_state, sizeof(double) * 2 * s->n_probes), "allocate mean receptor probes");
+  CUDA_TRY(cudaMemcpy(s->probe_ranks, ranks.data(), sizeof(int32_t) * s->n_probes, cudaMemcpyHostToDevice),
+           "upload mean receptor probe IDs");
+  s->knot_capacity = cap;
+  return DVS_OK;
+}
+
+static int ensure_exact(dvs_sensor *s) {
+  if (s->exact_cells) return DVS_OK;
+  const size_t n = (size_t)s->pixels(), cap = (size_t)s->knot_capacity;
+  CUDA_TRY(cudaMalloc(&s->exact_cells, sizeof(int32_t) * n * cap), "allocate local exact optical cells");
+  CUDA_TRY(cudaMalloc(&s->exact_radiance, sizeof(double) * n * cap), "allocate local exact radiance");
+  CUDA_TRY(cudaMalloc(&s->exact_queue, sizeof(int32_t) * n * cap), "allocate compact exact ray queue");
+  return DVS_OK;
+}
+
+// verify_receptor (event_sensor.cu:357-374): the probe pixels' receptors
+// driven by exactly traced and by interpolated light over every cell.
+static int verify_receptor(dvs_sensor *s, size_t n_cells, double start, double end) {
+  const SceneView view = s->view();
+  const int np = s->n_probes;
+  size_t chunk;
+  int cw_log2;
+  chunk_shape(s, n_cells, (size_t)np, chunk, cw_log2);
+  chunk = std::min(chunk, s->radiance_cap / (size_t)np);
+  if (chunk == 0) chunk = 1;
+  CUDA_TRY(grow_device(s->radiance, s->radiance_cap, chunk * (size_t)np), "probe radiance");
+  CUDA_TRY(launch_capture_probes(np, s->probe_ranks, s->st.receptor_log, s->probe_state, s->stream),
+           "capture mean receptor initial state");
+  for (size_t c0 = 0; c0 < n_cells; c0 += chunk) {
+    const int nc = (int)std::min(chunk, n_cells - c0);
+    CUDA_TRY(launch_trace_list(view, np, s->probe_ranks, s->poses, (int)c0, nc, cw_log2, s->radiance, nullptr,
+                               s->counters, s->stream),
+             "mean receptor probe optics");
+    CUDA_TRY(launch_advance_probes(np, s->probe_ranks, s->cells, (int)c0, nc, s->radiance, s->knots, s->knot_counts,
+                                   s->knot_capacity, start, end, s->photo, s->p.charge_scale, s->probe_state,
+                                   s->stream),
+             "mean receptor probe integration");
+    s->stats.launches += 2;
+  }
+  std::vector<double> states((size_t)2 * np);
+  CUDA_TRY(cudaMemcpyAsync(states.data(), s->probe_state, sizeof(double) * 2 * np, cudaMemcpyDeviceToHost, s->stream),
+           "download mean receptor convergence");
+  CUDA_TRY(cudaStreamSynchronize(s->stream), "download mean receptor convergence");
+  std::vector<double> errors(np);
+  dvs_receptor_probe r{};
+  r.pixels = np;
+  r.circuit_cells = (int32_t)n_cells;
+  for (int i = 0; i < np; ++i) {
+    errors[i] = std::fabs(states[2 * i] - states[2 * i + 1]);
+    r.mean_log_voltage_error += errors[i];
+  }
+  std::sort(errors.begin(), errors.end());
+  r.maximum_log_voltage_error = errors.back();
+  r.p99_log_voltage_error = errors[size_t(np * .99)];
+  r.mean_log_voltage_error /= np;
+  s->convergence = r;
+  return DVS_OK;
+}
+
+int dvs_sensor_process_adaptive(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, double tolerance,
+                                int32_t check_convergence, int32_t *accepted, size_t *n_ready) {
+  if (accepted) *accepted = 0;
+  if (n_ready) *n_ready = 0;
+  if (!s || !ivs || count == 0) return fail(DVS_ERR_INVALID, "empty adaptive optical horizon");
+  const double start = ivs[0].t0, end = ivs[count - 1].t1;
+  if (!std::isfinite(tolerance) || tolerance <= 0 || s->p.refractory_time <= 0 ||
+      (end - start) / s->p.refractory_time + 2 > s->max_events)
+    return fail(DVS_ERR_INVALID, "invalid adaptive tolerance or event capacity bound");
+  size_t n_cells = 0;
+  int r = upload_batch(s, ivs, count, n_cells);
+  if (r) return r;
+  if ((r = ensure_adaptive(s))) return r;
+  const int n = s->pixels(), cap = s->knot_capacity;
+  const SceneView view = s->view();
+  // all refinement completes and is checked before pixel/RNG state changes
+  CUDA_TRY(cudaMemsetAsync(s->ref_stats, 0, sizeof(unsigned long long) * kRefSlots, s->stream), "clear statistics");
+  CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream), "clear refinement errors");
+  record_timer(s, 0);
+  CUDA_TRY(launch_refine(view, n, s->ivs, (int)count, start, end, s->photo, tolerance, s->st, s->p.charge_scale, cap,
+                         s->knots, s->knot_counts, s->ref_stats, s->error_word, s->counters, s->stream),
+           "refine pixel optical launch");
+  s->stats.launches += 1;
+  CUDA_TRY(cudaMemcpyAsync(s->h_ref, s->ref_stats, sizeof(unsigned long long) * kRefSlots, cudaMemcpyDeviceToHost,
+                           s->stream),
+           "refinement statistics");
+  CUDA_TRY(cudaMemcpyAsync(s->h_status + 1, s->error_word, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream),
+           "refinement status");
+  CUDA_TRY(cudaStreamSynchronize(s->stream), "refinement status");
+  if (s->h_status[1]) return fail(DVS_ERR_OPTICAL, "invalid ray during optical refinement");
+  int32_t queries = 0;
+  if (s->h_ref[kRefExactSegments]) {
+    if ((r = ensure_exact(s))) return r;
+    CUDA_TRY(cudaMemsetAsync(s->exact_total, 0, sizeof(int32_t), s->stream), "clear exact query queue");
+    CUDA_TRY(launch_identify_exact(n, s->cells, (int)n_cells, start, end, s->knots, s->knot_counts, cap,
+                                   s->exact_cells, s->exact_counts, s->exact_queue, s->exact_total, s->ref_stats,
+                                   s->stream),
+             "identify local exact optical cells");
+    CUDA_TRY(launch_sample_exact(view, s->poses, s->exact_cells, s->exact_queue, s->exact_total, cap,
+                                 s->exact_radiance, s->error_word, s->counters, s->stream),
+             "trace local exact ray cells");
+    s->stats.launches += 2;
+    CUDA_TRY(cudaMemcpyAsync(s->h_ref, s->ref_stats, sizeof(unsigned long long) * kRefSlots, cudaMemcpyDeviceToHost,
+                             s->stream),
+             "local exact refinement statistics");
+    CUDA_TRY(cudaMemcpyAsync(s->h_status, s->exact_total, sizeof(int32_t) * 1, cudaMemcpyDeviceToHost, s->stream),
+             "local exact query count");
+    CUDA_TRY(cudaMemcpyAsync(s->h_status + 1, s->error_word, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream),
+             "local exact ray status");
+    CUDA_TRY(cudaStreamSynchronize(s->stream), "local exact ray status");
+    if (s->h_status[1]) return fail(DVS_ERR_OPTICAL, "invalid ray in local exact optical cell");
+    queries = s->h_status[0];
+  }
+  s->refine.traced_pixel_samples = s->h_ref[kRefTraced];
+  s->refine.fallback_pixels = (int32_t)s->h_ref[kRefFallback];
+  s->refine.maximum_knots = (int32_t)s->h_ref[kRefMaxKnots];
+  s->refine.exact_segments = (int32_t)s->h_ref[kRefExactSegments];
+  s->refine.native_cell_queries = queries;
+  if (check_convergence) {
+    if ((r = verify_receptor(s, n_cells, start, end))) return r;
+    const double threshold = std::min(s->p.threshold_pos, s->p.threshold_neg);
+    if (s->convergence.maximum_log_voltage_error > .02 * threshold ||
+        s->convergence.p99_log_voltage_error > .005 * threshold) {
+      collect_timers(s);
+      return DVS_OK;  // rejected: no pixel, RNG or time state changed
+    }
+  }
+  record_timer(s, 1);
+  if ((r = clear_batch_outputs(s))) return r;
+  CUDA_TRY(launch_integrate_knots(n, s->cells, (int)n_cells, start, end, s->knots, s->knot_counts, cap,
+                                  s->exact_cells, s->exact_radiance, queries ? s->exact_counts : nullptr, s->p,
+                                  s->photo, s->max_events, s->st, s->ev_count, s->slab_t, s->slab_p, s->error_word,
+                                  s->stream),
+           "adaptive circuit launch");
+  s->stats.launches += 1;
+  const int nf = s->refine.fallback_pixels;
+  if (nf > 0) {
+    CUDA_TRY(cudaMemsetAsync(s->fallback_total, 0, sizeof(int32_t), s->stream), "clear fallback ID counter");
+    CUDA_TRY(launch_compact_fallback(n, s->knot_counts, s->fallback_list, s->fallback_total, s->stream),
+             "compact exact fallback pixels");
+    size_t chunk;
+    int cw_log2;
+    chunk_shape(s, n_cells, (size_t)nf, chunk, cw_log2);
+    CUDA_TRY(grow_device(s->radiance, s->radiance_cap, chunk * (size_t)nf), "fallback optical tile");
+    for (size_t c0 = 0; c0 < n_cells; c0 += chunk) {
+      const int nc = (int)std::min(chunk, n_cells - c0);
+      CUDA_TRY(launch_trace_list(view, nf, s->fallback_list, s->poses, (int)c0, nc, cw_log2, s->radiance, nullptr,
+                                 s->counters, s->stream),
+               "parallel exact cell optics launch");
+      CUDA_TRY(launch_circuit_list(nf, s->fallback_list, s->cells, (int)c0, nc, s->radiance, s->p, s->photo,
+                                   s->max_events, s->st, s->ev_count, s->slab_t, s->slab_p, s->error_word,
+                                   s->counters, s->stream),
+               "exact fallback circuit tile launch");
+      s->stats.launches += 2;
+    }
+  }
+  record_timer(s, 2);
+  CUDA_TRY(launch_emit_events(n, s->order, s->scene->camera.width, s->max_events, s->ev_count,
+                              s->slab_t, s->slab_p, s->events, s->event_total, s->stream),
+           "compact events");
+  record_timer(s, 3);
+  s->stats.launches += 2;
+  s->last_time = end;
+  if (accepted) *accepted = 1;
+  return collect(s, end, n_ready);
+}
+
+int dvs_sensor_refinement_stats(const dvs_sensor *s, dvs_refinement_stats *out) {
+  if (!s || !out) return fail(DVS_ERR_INVALID, "null argument");
+  *out = s->refine;
+  return DVS_OK;
+}
+
+int dvs_sensor_last_convergence(const dvs_sensor *s, dvs_receptor_probe *out) {
+  if (!s || !out) return fail(DVS_ERR_INVALID, "null argument");
+  *out = s->convergence;
+  return DVS_OK;
+}
+
+int dvs_sensor_adaptive_capacity(dvs_sensor *s, int32_t *capacity) {
+  if (!s || !capacity) return fail(DVS_ERR_INVALID, "null argument");
+  CUDA_TRY(cudaSetDevice(s->device), "select device");
+  int r = ensure_adaptive(s);
+  if (r) return r;
+  *capacity = s->knot_capacity;
   return DVS_OK;
 }
 
@@ -777,7 +1100,7 @@ int dvs_sensor_stats_reset(dvs_sensor *s) {
 int dvs_sensor_read_state(dvs_sensor *s, double *state5, int32_t *reset_pending) {
   if (!s) return fail(DVS_ERR_INVALID, "null argument");
   CUDA_TRY(cudaSetDevice(s->device), "select device");
-  const int n = s->scene->pixels();
+  const int n = s->pixels();
   std::vector<double> buf((size_t)5 * n);
   std::vector<int8_t> rp(n);
   std::vector<int32_t> order(n);
@@ -787,16 +1110,93 @@ int dvs_sensor_read_state(dvs_sensor *s, double *state5, int32_t *reset_pending)
     CUDA_TRY(cudaMemcpyAsync(buf.data() + (size_t)f * n, src[f], sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream),
              "download state");
   CUDA_TRY(cudaMemcpyAsync(rp.data(), s->st.reset_pending, n, cudaMemcpyDeviceToHost, s->stream), "download state");
-  CUDA_TRY(cudaMemcpyAsync(order.data(), s->scene->pixel_of_rank, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+  CUDA_TRY(cudaMemcpyAsync(order.data(), s->order, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
                            s->stream),
            "download order");
   CUDA_TRY(cudaStreamSynchronize(s->stream), "download state");
+  const int first = s->row_begin * s->scene->camera.width;  // band sensors report their own rows
   for (int k = 0; k < n; ++k) {
-    const int pix = order[k];
+    const int pix = order[k] - first;
     if (state5)
       for (int f = 0; f < 5; ++f) state5[(size_t)pix * 5 + f] = buf[(size_t)f * n + k];
     if (reset_pending) reset_pending[pix] = rp[k];
   }
+  return DVS_OK;
+}
+
+}  // extern "C"
+
+// ---- standalone readout FIFO (host) -----------------------------------------------
+struct dvs_readout {
+  Readout fifo;
+  std::vector<HostEvent> ready;
+  size_t head = 0;
+  dvs_readout(double b, double l, size_t c) : fifo(b, l, c) {}
+};
+
+extern "C" {
+
+int dvs_readout_create(double bandwidth, double latency, size_t capacity, dvs_readout **out) {
+  if (!out) return fail(DVS_ERR_INVALID, "null output handle");
+  if (!std::isfinite(bandwidth) || !std::isfinite(latency) || capacity < 1)
+    return fail(DVS_ERR_INVALID, "invalid readout bandwidth, latency or capacity");
+  *out = new dvs_readout(bandwidth, latency, capacity);
+  return DVS_OK;
+}
+
+int dvs_readout_destroy(dvs_readout *r) {
+  delete r;
+  return DVS_OK;
+}
+
+static void compact_ready(dvs_readout *r) {
+  if (r->head && r->head == r->ready.size()) {
+    r->ready.clear();
+    r->head = 0;
+  }
+}
+
+int dvs_readout_submit(dvs_readout *r, const dvs_event *events, size_t n, double now, size_t *n_ready) {
+  if (!r || !n_ready || (n && !events)) return fail(DVS_ERR_INVALID, "null argument");
+  std::vector<HostEvent> batch(n);
+  for (size_t i = 0; i < n; ++i)
+    batch[i] = HostEvent{events[i].timestamp, events[i].x, events[i].y, events[i].polarity, events[i].depth};
+  compact_ready(r);
+  r->fifo.submit(batch, now, r->ready);
+  *n_ready = r->ready.size() - r->head;
+  return DVS_OK;
+}
+
+int dvs_readout_drain(dvs_readout *r, size_t *n_ready) {
+  if (!r || !n_ready) return fail(DVS_ERR_INVALID, "null argument");
+  compact_ready(r);
+  r->fifo.drain(r->ready);
+  *n_ready = r->ready.size() - r->head;
+  return DVS_OK;
+}
+
+int dvs_readout_read(dvs_readout *r, dvs_event *out, size_t capacity, size_t *n_out) {
+  if (!r || !n_out) return fail(DVS_ERR_INVALID, "null argument");
+  const size_t m = std::min(capacity, r->ready.size() - r->head);
+  if (m && !out) return fail(DVS_ERR_INVALID, "null output buffer");
+  for (size_t i = 0; i < m; ++i) {
+    const HostEvent &e = r->ready[r->head + i];
+    out[i].timestamp = e.t;
+    out[i].x = e.x;
+    out[i].y = e.y;
+    out[i].polarity = e.p;
+    out[i].depth = e.depth;
+  }
+  r->head += m;
+  *n_out = m;
+  compact_ready(r);
+  return DVS_OK;
+}
+
+int dvs_readout_counters(const dvs_readout *r, uint64_t *dropped, uint64_t *peak_queue) {
+  if (!r) return fail(DVS_ERR_INVALID, "null argument");
+  if (dropped) *dropped = r->fifo.dropped();
+  if (peak_queue) *peak_queue = r->fifo.peak();
   return DVS_OK;
 }
 

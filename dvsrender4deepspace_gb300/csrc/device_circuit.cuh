@@ -1,0 +1,114 @@
+// Device-side pixel circuit of the GB300 DVS path (include/dvs/pixel_model.hpp
+// semantics, FP64) and the cuRAND photon-count draw.  Internal linkage.
+#pragma once
+#include <cuda_runtime.h>
+#include <curand_kernel.h>
+
+#include "kernels.h"
+
+namespace dvsgb {
+namespace {
+// ---- pixel circuit (include/dvs/pixel_model.hpp:18-102), FP64 ------------------------
+__device__ __forceinline__ double receptor_log_at(double u, double rate, double dt, double charge) {
+  if (dt <= 0) return u;
+  rate = fmax(0.0, rate);
+  double x = exp(u);
+  if (rate == 0) return u - log1p(x * dt / charge);
+  double a = exp(-rate * dt / charge), b = -expm1(-rate * dt / charge);
+  return -log(a / x + b / rate);
+}
+
+struct PixelRegs {
+  double receptor_log, reference_log, refractory_until, threshold_pos, threshold_neg;
+  bool reset_pending;
+};
+
+// Returns events emitted, -1 at capacity, -2 when the loop stops making progress.
+__device__ int advance_pixel(PixelRegs &s, const PixelParams &p, double rate, double t0, double t1, double *out_t,
+                             int8_t *out_p, int capacity, curandStateXORWOW_t &rng) {
+  if (t1 <= t0) return 0;
+  int count = 0;
+  double cursor = t0, u = s.receptor_log;
+  int passes = 0;
+  while (cursor < t1) {
+    if (++passes > 4096) return -2;  // bounded: see kErrStalled
+    if (cursor < s.refractory_until) {
+      double end = fmin(t1, s.refractory_until);
+      u = receptor_log_at(u, rate, end - cursor, p.charge_scale);
+      cursor = end;
+      s.reference_log = u;
+      if (cursor < t1 || cursor == s.refractory_until) {
+        if (cursor >= s.refractory_until && s.reset_pending) {
+          if (p.reset_noise_std > 0) s.reference_log += p.reset_noise_std * curand_normal_double(&rng);
+          s.reset_pending = false;
+        }
+      }
+      if (cursor >= t1) break;
+    } else if (s.reset_pending) {
+      if (p.reset_noise_std > 0) s.reference_log += p.reset_noise_std * curand_normal_double(&rng);
+      s.reset_pending = false;
+    }
+    double remaining = t1 - cursor;
+    double c0 = u - s.reference_log;
+    double boundary = remaining;
+    double x = exp(u), target = rate + p.charge_scale * p.reference_leak;
+    if (p.reference_leak > 0 && x > target && target > rate) {
+      double extremum;
+      if (rate > 0) extremum = -p.charge_scale / rate * log((1.0 / target - 1.0 / rate) / (1.0 / x - 1.0 / rate));
+      else extremum = p.charge_scale * (1.0 / target - 1.0 / x);
+      if (extremum > 1e-15 && extremum < boundary) boundary = extremum;
+    }
+    double ub = receptor_log_at(u, rate, boundary, p.charge_scale);
+    double cb = ub - s.reference_log + p.reference_leak * boundary;
+    int polarity = -1;
+    double level = 0;
+    if (c0 >= s.threshold_pos) { polarity = 1; level = s.threshold_pos; }
+    else if (c0 <= -s.threshold_neg) { polarity = 0; level = -s.threshold_neg; }
+    else if (cb >= s.threshold_pos) { polarity = 1; level = s.threshold_pos; }
+    else if (cb <= -s.threshold_neg) { polarity = 0; level = -s.threshold_neg; }
+    if (polarity < 0) {
+      u = ub;
+      s.reference_log -= p.reference_leak * boundary;
+      cursor += boundary;
+      continue;
+    }
+    if (count == capacity) return -1;
+    double lo = 0, hi = boundary;
+    if (c0 >= s.threshold_pos || c0 <= -s.threshold_neg) hi = 0;
+    else if (p.reference_leak == 0) {
+      double target_inverse = exp(-(s.reference_log + level));
+      double initial_inverse = exp(-u);
+      if (rate > 0) {
+        double stationary_inverse = 1.0 / rate;
+        hi = -p.charge_scale / rate * log1p((target_inverse - initial_inverse) / (initial_inverse - stationary_inverse));
+      } else hi = p.charge_scale * (target_inverse - initial_inverse);
+      hi = fmin(boundary, fmax(0.0, hi));
+    } else
+      for (int j = 0; j < 48; ++j) {
+        double mid = (lo + hi) * .5;
+        double c = receptor_log_at(u, rate, mid, p.charge_scale) - s.reference_log + p.reference_leak * mid;
+        if (polarity ? c >= level : c <= level) hi = mid; else lo = mid;
+      }
+    u = receptor_log_at(u, rate, hi, p.charge_scale);
+    cursor += hi;
+    out_t[count] = cursor;
+    out_p[count] = (int8_t)polarity;
+    ++count;
+    s.reference_log = u;
+    s.refractory_until = cursor + p.refractory_time;
+    s.reset_pending = true;
+  }
+  s.receptor_log = u;
+  return count;
+}
+
+// poisson_electrons (include/dvs/photon_noise.cuh:4-9): cuRAND draws in the
+// reference's order so seeded streams match a reference build on the same toolkit.
+__device__ __forceinline__ double poisson_electrons(curandStateXORWOW_t &rng, double lambda) {
+  if (lambda <= 0) return 0;
+  if (lambda > 1e6) return fmax(0.0, floor(lambda + sqrt(lambda) * curand_normal_double(&rng) + .5));
+  return curand_poisson(&rng, lambda);
+}
+
+}  // namespace
+}  // namespace dvsgb

@@ -1,0 +1,587 @@
+// Device-side optics of the GB300 DVS path: float3 algebra, Hapke, pose
+// interpolation, the 8-wide warp-packet BVH traversal and the pixel sample.
+// Included by the CUDA translation units that trace rays; everything has
+// internal linkage.  Compiled with -fmad=false (see kernels.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace dvsgb {
+namespace {
+constexpr unsigned kFull = 0xffffffffu;
+constexpr float kRayEps = 1e-6f;          // include/helper_math.hpp:12
+constexpr float kPi = 3.14159265358979323846f;  // include/dvs/math_types.hpp:37
+__device__ __forceinline__ float kInf() { return __int_as_float(0x7f800000); }
+
+// ---- float3 algebra (include/helper_math.hpp:18-77) -------------------------
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator/(float3 a, float s) { return f3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross(float3 a, float3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 normalize(float3 v) {
+  float len = sqrtf(dot(v, v));
+  if (len > 0.0f) return v / len;
+  return f3(0.0f, 0.0f, 0.0f);
+}
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
+
+// ---- Hapke (include/dvs/hapke.hpp:14-157), FP32 --------------------------------
+__device__ __forceinline__ float safe_tan(float x) {
+  return tanf(clampf(x, -kPi / 2.0f + 1e-6f, kPi / 2.0f - 1e-6f));
+}
+__device__ __forceinline__ float safe_acos(float x) { return acosf(clampf(x, -1.0f, 1.0f)); }
+__device__ __forceinline__ float hg_double_lobe(float cosg, float b, float c) {
+  const float one_minus_bb = 1.0f - b * b;
+  const float term1 = ((1.0f + c) * 0.5f) * one_minus_bb / powf(1.0f - 2.0f * b * cosg + b * b, 1.5f);
+  const float term2 = ((1.0f - c) * 0.5f) * one_minus_bb / powf(1.0f + 2.0f * b * cosg + b * b, 1.5f);
+  return term1 + term2;
+}
+__device__ __forceinline__ float b_s(float tg, float h) {
+  if (h <= 0.0f) return tg <= 0.0f ? 1.0f : 0.0f;
+  return 1.0f / (1.0f + tg / h);
+}
+__device__ __forceinline__ float b_c(float tg, float h) {
+  if (h <= 0.0f) return tg <= 0.0f ? 1.0f : 0.0f;
+  const float T = tg / h;
+  if (T < 1e-8f) return 1.0f;
+  return (1.0f + (1.0f - expf(-T)) / T) / (2.0f * (1.0f + T) * (1.0f + T));
+}
+__device__ __forceinline__ float hfunc(float x, float w) {
+  if (x <= 1e-8f) return 1.0f;
+  const float root = sqrtf(fmaxf(0.0f, 1.0f - w));
+  const float r0 = (1.0f - root) / (1.0f + root);
+  const float term = r0 + (1.0f - 2.0f * r0 * x) * 0.5f * logf(1.0f + 1.0f / x);
+  return 1.0f / (1.0f - w * x * term);
+}
+__device__ __forceinline__ float porosity_k(float phi) {
+  if (phi <= 1e-8f) return 1.0f;
+  const float p = 1.209f * powf(phi, 2.0f / 3.0f);
+  return -logf(1.0f - p) / p;
+}
+__device__ __forceinline__ float chi_f(float thetap) {
+  const float t = tanf(thetap);
+  return 1.0f / sqrtf(1.0f + kPi * t * t);
+}
+__device__ __forceinline__ float e1_f(float thetap, float cosy, float siny) {
+  const float s = fmaxf(siny, 1e-6f);
+  return expf((-2.0f / kPi) * (1.0f / tanf(thetap)) * cosy / s);
+}
+__device__ __forceinline__ float e2_f(float thetap, float cosy, float siny) {
+  const float s = fmaxf(siny, 1e-6f);
+  const float v = (1.0f / tanf(thetap)) * cosy / s;
+  return expf((-1.0f / kPi) * v * v);
+}
+__device__ __forceinline__ float eta_f(float thetap, float cosy, float siny) {
+  const float ch = chi_f(thetap);
+  const float e1 = e1_f(thetap, cosy, siny);
+  const float e2 = e2_f(thetap, cosy, siny);
+  return ch * (cosy + siny * tanf(thetap) * e2 / (2.0f - e1));
+}
+__device__ __forceinline__ float f_psi(float psi) { return expf(-2.0f * tanf(psi * 0.5f)); }
+
+__device__ float hapke_reflectance(float cosi, float cose, float cosg, float albedo, const dvs_hapke &p) {
+  if (cosi <= 0 || cose <= 0) return 0;
+  cosi = clampf(cosi, 0, 1);
+  cose = clampf(cose, 0, 1);
+  cosg = clampf(cosg, -1, 1);
+  const float sini = sqrtf(fmaxf(0, 1 - cosi * cosi)), sine = sqrtf(fmaxf(0, 1 - cose * cose));
+  const float tg = safe_tan(safe_acos(cosg) * 0.5f);
+  const float psi = safe_acos((cosg - cosi * cose) / (sini * sine + 1e-6f));
+  const float p_g = hg_double_lobe(cosg, p.b, p.c);
+  const float BS = b_s(tg, p.hS);
+  const float BC = b_c(tg, p.hC);
+  const float K = porosity_k(p.phi);
+  float mu0, mue, S;
+  const float thetap = p.thetap;
+  if (thetap <= 1e-8f) {
+    mu0 = cosi; mue = cose; S = 1.0f;
+  } else {
+    const float ch = chi_f(thetap);
+    const float tan_thetap = tanf(thetap);
+    const float sh = sinf(psi * 0.5f);
+    const float s2 = sh * sh;
+    const float e2e = e2_f(thetap, cose, sine), e2i = e2_f(thetap, cosi, sini);
+    const float e1e = e1_f(thetap, cose, sine), e1i = e1_f(thetap, cosi, sini);
+    const float eta_e = eta_f(thetap, cose, sine), eta_i = eta_f(thetap, cosi, sini);
+    const float fp = f_psi(psi);
+    if (cosi >= cose) {
+      mu0 = ch * (cosi + sini * tan_thetap * (cosf(psi) * e2e + s2 * e2i) / (2.0f - e1e - (psi / kPi) * e1i));
+      mue = ch * (cose + sine * tan_thetap * (e2e - s2 * e2i) / (2.0f - e1e - (psi / kPi) * e1i));
+      S = mue / eta_e * cosi / eta_i * ch / (1.0f - fp + fp * ch * (cosi / eta_i));
+    } else {
+      mu0 = ch * (cosi + sini * tan_thetap * (e2i - s2 * e2e) / (2.0f - e1i - (psi / kPi) * e1e));
+      mue = ch * (cose + sine * tan_thetap * (cosf(psi) * e2i + s2 * e2e) / (2.0f - e1i - (psi / kPi) * e1e));
+      S = mue / eta_e * cosi / eta_i * ch / (1.0f - fp + fp * ch * (cose / eta_e));
+    }
+  }
+  const float M = hfunc(mu0 / K, albedo) * hfunc(mue / K, albedo) - 1.0f;
+  const float LS = mu0 / (mu0 + mue + 1e-6f);
+  return (albedo / (4.0f * kPi)) * LS * K * (p_g * (1.0f + BS * p.B_S0) + M) * (1.0f + BC * p.B_C0) * S;
+}
+
+// ---- pose interpolation (include/dvs/device_optics.cuh:6-29) ---------------------
+__device__ __forceinline__ float hermite(float a, float va, float b, float vb, float u, float dt) {
+  float u2 = u * u, u3 = u2 * u;
+  return a + (-2 * u3 + 3 * u2) * (b - a) + (u3 - 2 * u2 + u) * dt * va + (u3 - u2) * dt * vb;
+}
+__device__ __forceinline__ float3 ld3(const dvs_float3 &v) { return f3(v.x, v.y, v.z); }
+__device__ __forceinline__ float3 hermite3(const dvs_float3 &a, const dvs_float3 &va, const dvs_float3 &b,
+                                           const dvs_float3 &vb, float u, float dt) {
+  return f3(hermite(a.x, va.x, b.x, vb.x, u, dt), hermite(a.y, va.y, b.y, vb.y, u, dt),
+            hermite(a.z, va.z, b.z, vb.z, u, dt));
+}
+// optical_state_at reduced to what the ray generator needs.  The quaternion
+// is renormalized with a correctly rounded 1/sqrt (the reference's rsqrtf is
+// an approximation the CPU oracle cannot reproduce).
+__device__ CellPose pose_at(const dvs_optical_interval &iv, double t) {
+  float dt = iv.t1 - iv.t0, u = dt > 0 ? fmin(1.0, fmax(0.0, (t - iv.t0) / dt)) : 0;
+  float3 pos = hermite3(iv.start.position, iv.start.velocity, iv.end.position, iv.end.velocity, u, dt);
+  float3 light = hermite3(iv.start.light, iv.start.light_rate, iv.end.light, iv.end.light_rate, u, dt);
+  float intensity = fmaxf(0, hermite(iv.start.intensity, iv.start.intensity_rate, iv.end.intensity,
+                                     iv.end.intensity_rate, u, dt));
+  float4 a = make_float4(iv.start.rotation.x, iv.start.rotation.y, iv.start.rotation.z, iv.start.rotation.w);
+  float4 b = make_float4(iv.end.rotation.x, iv.end.rotation.y, iv.end.rotation.z, iv.end.rotation.w);
+  float d = a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+  if (d < 0) { b = make_float4(-b.x, -b.y, -b.z, -b.w); d = -d; }
+  float wa = 1 - u, wb = u;
+  if (d < .9995f) {
+    float angle = acosf(fminf(1, d)), inv = 1 / sinf(angle);
+    wa = sinf((1 - u) * angle) * inv;
+    wb = sinf(u * angle) * inv;
+  }
+  float4 q = make_float4(wa * a.x + wb * b.x, wa * a.y + wb * b.y, wa * a.z + wb * b.z, wa * a.w + wb * b.w);
+  float norm = 1.0f / sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+  float3 ln = normalize(light);  // sample_pixel normalizes pose.light (device_optics.cuh:75)
+  CellPose out;
+  out.px = pos.x; out.py = pos.y; out.pz = pos.z; out.intensity = intensity;
+  out.qx = q.x * norm; out.qy = q.y * norm; out.qz = q.z * norm; out.qw = q.w * norm;
+  out.lx = ln.x; out.ly = ln.y; out.lz = ln.z; out.pad = 0;
+  return out;
+}
+__device__ __forceinline__ float3 rotate_ray(const CellPose &q, float3 v) {
+  float3 qv = f3(q.qx, q.qy, q.qz);
+  float3 c = 2 * cross(qv, v);
+  return v + q.qw * c + cross(qv, c);
+}
+
+// ---- traversal -------------------------------------------------------------------
+__device__ __forceinline__ float3 inverse_direction(float3 d) {  // device_ray.hpp:6-12
+  float3 inv;
+  inv.x = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
+  inv.y = 1.0f / (fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y));
+  inv.z = 1.0f / (fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z));
+  return inv;
+}
+
+// Moller-Trumbore with precomputed edges (device_ray.hpp:54-80).
+__device__ __forceinline__ bool intersect_tri(float3 ray, float3 o, float3 v0, float3 e1, float3 e2, float &t,
+                                              float &u, float &v) {
+  const float3 pvec = cross(ray, e2);
+  const float det = dot(e1, pvec);
+  if (fabsf(det) < kRayEps) return false;
+  const float inv_det = 1.0f / det;
+  const float3 tvec = o - v0;
+  u = dot(tvec, pvec) * inv_det;
+  if (u < 0.0f || u > 1.0f) return false;
+  const float3 qvec = cross(tvec, e1);
+  v = dot(ray, qvec) * inv_det;
+  if (v < 0.0f || (u + v) > 1.0f) return false;
+  t = dot(e2, qvec) * inv_det;
+  if (t <= kRayEps) return false;
+  return true;
+}
+
+// ---- 8-wide packet traversal ------------------------------------------------------
+// Float min/max across a warp through order-preserving unsigned keys.
+__device__ __forceinline__ unsigned ford(float f) {
+  const unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float funord(unsigned u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+__device__ __forceinline__ float wmin(float x) { return funord(__reduce_min_sync(kFull, ford(x))); }
+__device__ __forceinline__ float wmax(float x) { return funord(__reduce_max_sync(kFull, ford(x))); }
+
+struct ChildRec {
+  float3 lo, hi;
+  int child, count;
+};
+__device__ __forceinline__ ChildRec load_child(const BvhNode *nodes, int node, int slot) {
+  const float4 *p = reinterpret_cast<const float4 *>(&nodes[node].c[slot]);
+  const float4 a = __ldg(p), b = __ldg(p + 1);
+  ChildRec r;
+  r.lo = f3(a.x, a.y, a.z);
+  r.hi = f3(a.w, b.x, b.y);
+  r.child = __float_as_int(b.z);
+  r.count = __float_as_int(b.w);
+  return r;
+}
+
+// Slab test of one ray (device_ray.hpp:21-29 form).
+__device__ __forceinline__ bool slab(float3 lo, float3 hi, float3 o, float3 idir, float t_min, float t_max,
+                                     float &tnear) {
+  float tx0 = (lo.x - o.x) * idir.x, tx1 = (hi.x - o.x) * idir.x;
+  float ty0 = (lo.y - o.y) * idir.y, ty1 = (hi.y - o.y) * idir.y;
+  float tz0 = (lo.z - o.z) * idir.z, tz1 = (hi.z - o.z) * idir.z;
+  float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+  float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+  tmin = fmaxf(t_min, tmin);
+  tmax = fminf(t_max, tmax);
+  tnear = tmin;
+  return tmax >= tmin;
+}
+
+// The rays of a warp as intervals of origin and inverse direction.  A child
+// is entered when some ray of the box could hit it: every bound is an
+// extreme of the same rounded operations each ray performs, so the packet
+// never culls a node that one of its rays would enter.
+struct Packet {
+  float3 olo, ohi, ilo, ihi;
+  bool coherent;
+};
+__device__ __forceinline__ void interval_mul(float a0, float a1, float b0, float b1, float &lo, float &hi) {
+  const float p0 = a0 * b0, p1 = a0 * b1, p2 = a1 * b0, p3 = a1 * b1;
+  lo = fminf(fminf(p0, p1), fminf(p2, p3));
+  hi = fmaxf(fmaxf(p0, p1), fmaxf(p2, p3));
+}
+__device__ __forceinline__ void axis_bounds(float lo, float hi, float olo, float ohi, float ilo, float ihi, float &L,
+                                            float &U) {
+  float a0, a1, b0, b1;
+  interval_mul(lo - ohi, lo - olo, ilo, ihi, a0, a1);
+  interval_mul(hi - ohi, hi - olo, ilo, ihi, b0, b1);
+  L = fminf(a0, b0);
+  U = fmaxf(a1, b1);
+}
+__device__ __forceinline__ bool packet_slab(const ChildRec &c, const Packet &P, float t_min, float t_max,
+                                            float &tnear) {
+  float Lx, Ux, Ly, Uy, Lz, Uz;
+  axis_bounds(c.lo.x, c.hi.x, P.olo.x, P.ohi.x, P.ilo.x, P.ihi.x, Lx, Ux);
+  axis_bounds(c.lo.y, c.hi.y, P.olo.y, P.ohi.y, P.ilo.y, P.ihi.y, Ly, Uy);
+  axis_bounds(c.lo.z, c.hi.z, P.olo.z, P.ohi.z, P.ilo.z, P.ihi.z, Lz, Uz);
+  const float lb = fmaxf(fmaxf(fmaxf(Lx, Ly), Lz), t_min);
+  const float ub = fminf(fminf(fminf(Ux, Uy), Uz), t_max);
+  tnear = lb;
+  return ub >= lb;
+}
+__device__ Packet make_packet(const SceneView &S, float3 o, float3 d, float3 idir, bool active) {
+  const float inf = kInf();
+  Packet P;
+  P.olo = f3(wmin(active ? o.x : inf), wmin(active ? o.y : inf), wmin(active ? o.z : inf));
+  P.ohi = f3(wmax(active ? o.x : -inf), wmax(active ? o.y : -inf), wmax(active ? o.z : -inf));
+  P.ilo = f3(wmin(active ? idir.x : inf), wmin(active ? idir.y : inf), wmin(active ? idir.z : inf));
+  P.ihi = f3(wmax(active ? idir.x : -inf), wmax(active ? idir.y : -inf), wmax(active ? idir.z : -inf));
+  const float dx = wmax(active ? d.x : -inf) - wmin(active ? d.x : inf);
+  const float dy = wmax(active ? d.y : -inf) - wmin(active ? d.y : inf);
+  const float dz = wmax(active ? d.z : -inf) - wmin(active ? d.z : inf);
+  const float ds = fmaxf(fmaxf(dx, dy), dz);
+  const float os = fmaxf(fmaxf(P.ohi.x - P.olo.x, P.ohi.y - P.olo.y), P.ohi.z - P.olo.z);
+  // bundles whose footprint stays within a small fraction of the scene
+  P.coherent = ds <= 0.02f && os <= S.coherent_span;
+  return P;
+}
+
+// Warp-uniform traversal stack in shared memory: node codes and the packet's
+// entry distance.  Inner node: index >= 0; leaf: -(node * 8 + slot) - 1.
+struct Stack {
+  int *code;
+  float *t;
+  int sp;
+};
+__device__ __forceinline__ int leaf_code(int node, int slot) { return -(node * kBvhWidth + slot) - 1; }
+
+struct HitRecord {
+  int hit;  // 1 hit, 0 miss, -1 stack overflow (device_ray.hpp:152)
+  int tri;
+  float t, u, v;
+};
+
+// Expands an inner node: children the packet may hit are ordered near to far;
+// all but the nearest go on the stack.  Returns false when none is hit.
+// Coherent packets test one child per lane (lanes 0..7) with interval bounds;
+// others test every child per ray and take the warp minimum as the key.
+template <bool kSorted>
+__device__ __forceinline__ bool expand_node(const SceneView &S, int node, const Packet &P, float3 o, float3 idir,
+                                            bool lane_live, float t_min, float lane_tmax, float packet_tmax,
+                                            Stack &st, int &next, float &next_t, bool &overflow) {
+  const int lane = threadIdx.x & 31;
+  float key = kInf();
+  bool hit = false;
+  int code = 0;
+  if (P.coherent) {
+    if (lane < kBvhWidth) {
+      const ChildRec c = load_child(S.nodes, node, lane);
+      if (c.count >= 0) {
+        hit = packet_slab(c, P, t_min, packet_tmax, key);
+        code = c.count > 0 ? leaf_code(node, lane) : c.child;
+      }
+    }
+  } else {
+    for (int slot = 0; slot < kBvhWidth; ++slot) {
+      const ChildRec c = load_child(S.nodes, node, slot);
+      float tn = kInf();
+      const bool h = c.count >= 0 && lane_live && slab(c.lo, c.hi, o, idir, t_min, lane_tmax, tn);
+      const float k = wmin(h ? tn : kInf());
+      if (lane == slot) {
+        hit = k < kInf();
+        key = k;
+        code = c.count > 0 ? leaf_code(node, slot) : c.child;
+      }
+    }
+  }
+  const unsigned mask = __ballot_sync(kFull, hit && lane < kBvhWidth);
+  if (!mask) return false;
+  const int n = __popc(mask);
+  int rank = 0;
+  if (kSorted) {
+#pragma unroll
+    for (int j = 0; j < kBvhWidth; ++j) {
+      const float kj = __shfl_sync(kFull, key, j);
+      rank += ((mask >> j) & 1) && (kj < key || (kj == key && j < lane)) ? 1 : 0;
+    }
+  } else {
+    rank = __popc(mask & ((1u << lane) - 1u));
+  }
+  if (st.sp + n - 1 > kStackSlots) {
+    overflow = true;
+    return false;
+  }
+  if (hit && lane < kBvhWidth && rank > 0) {
+    const int slot = st.sp + (n - 1 - rank);
+    st.code[slot] = code;
+    st.t[slot] = key;
+  }
+  const int first = __ffs(__ballot_sync(kFull, hit && lane < kBvhWidth && rank == 0)) - 1;
+  next = __shfl_sync(kFull, code, first);
+  next_t = __shfl_sync(kFull, key, first);
+  st.sp += n - 1;
+  __syncwarp();
+  return true;
+}
+
+// Nearest hit for the rays of a warp (trace_nearest, device_ray.hpp:136-158).
+// All 32 lanes call converged; inactive lanes never hit.  Each lane tests a
+// leaf's triangles only when its own slab test reaches the leaf.
+__device__ HitRecord trace_nearest_packet(const SceneView &S, float3 o, float3 d, bool active, int *stack_code,
+                                          float *stack_t) {
+  const float3 idir = inverse_direction(d);
+  float closest = active ? 1e30f : -1.0f;
+  HitRecord h{0, -1, 0.f, 0.f, 0.f};
+  const Packet P = make_packet(S, o, d, idir, active);
+  float packet_tmax = wmax(active ? closest : -1.0f);
+  Stack st{stack_code, stack_t, 0};
+  int entry = 0;
+  float entry_t = 0.0f;
+  bool overflow = false;
+  while (true) {
+    if (entry_t <= packet_tmax) {
+      if (entry >= 0) {
+        int next;
+        float next_t;
+        if (expand_node<true>(S, entry, P, o, idir, active, kRayEps, closest, packet_tmax, st, next, next_t,
+                              overflow)) {
+          entry = next;
+          entry_t = next_t;
+          continue;
+        }
+        if (overflow) break;
+      } else {
+        const int lc = -entry - 1;
+        const ChildRec c = load_child(S.nodes, lc / kBvhWidth, lc % kBvhWidth);
+        float tn;
+        const bool need = active && slab(c.lo, c.hi, o, idir, kRayEps, closest, tn);
+        for (int i = 0; i < c.count; ++i) {
+          const float4 *r = reinterpret_cast<const float4 *>(S.tris + c.child + i);
+          const float4 a = __ldg(r), b = __ldg(r + 1), q = __ldg(r + 2);
+          float t, u, v;
+          if (need && intersect_tri(d, o, f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, q.x), t, u, v) &&
+              t < closest) {
+            closest = t;
+            h.hit = 1; h.tri = c.child + i; h.t = t; h.u = u; h.v = v;
+          }
+        }
+        packet_tmax = wmax(active ? closest : -1.0f);
+      }
+    }
+    if (st.sp == 0) break;
+    --st.sp;
+    entry = st.code[st.sp];
+    entry_t = st.t[st.sp];
+  }
+  __syncwarp();
+  if (overflow) h.hit = -1;
+  return h;
+}
+
+// Any hit toward the light (trace_shadow_ray_any_hit, device_ray.hpp:81-135):
+// skips the camera-hit triangle, t in (kRayEps, 1e30); overflow counts as occluded.
+__device__ bool trace_shadow_packet(const SceneView &S, float3 o, float3 d, bool active, int self, int *stack_code,
+                                    float *stack_t) {
+  const float3 idir = inverse_direction(d);
+  bool alive = active;
+  bool occluded = false;
+  const float t_max = 1e30f;
+  const Packet P = make_packet(S, o, d, idir, active);
+  Stack st{stack_code, stack_t, 0};
+  int entry = 0;
+  float entry_t = 0.0f;
+  bool overflow = false;
+  while (__any_sync(kFull, alive)) {
+    if (entry >= 0) {
+      int next;
+      float next_t;
+      if (expand_node<false>(S, entry, P, o, idir, alive, kRayEps, alive ? t_max : -1.0f, t_max, st, next, next_t,
+                             overflow)) {
+        entry = next;
+        entry_t = next_t;
+        continue;
+      }
+      if (overflow) {
+        occluded = occluded || alive;  // conservative (device_ray.hpp:119)
+        break;
+      }
+    } else {
+      const int lc = -entry - 1;
+      const ChildRec c = load_child(S.nodes, lc / kBvhWidth, lc % kBvhWidth);
+      float tn;
+      const bool need = alive && slab(c.lo, c.hi, o, idir, kRayEps, t_max, tn);
+      for (int i = 0; i < c.count; ++i) {
+        const int id = c.child + i;
+        const float4 *r = reinterpret_cast<const float4 *>(S.tris + id);
+        const float4 a = __ldg(r), b = __ldg(r + 1), q = __ldg(r + 2);
+        float t, u, v;
+        if (need && alive && id != self &&
+            intersect_tri(d, o, f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, q.x), t, u, v) && t > kRayEps &&
+            t < t_max) {
+          occluded = true;
+          alive = false;
+        }
+      }
+    }
+    if (st.sp == 0) break;
+    --st.sp;
+    entry = st.code[st.sp];
+    entry_t = st.t[st.sp];
+  }
+  (void)entry_t;
+  __syncwarp();
+  return occluded;
+}
+
+
+// shadow_origin (device_optics.cuh:37-51) from the leaf-order triangle record.
+__device__ float3 shadow_origin(float3 a, float3 e1, float3 e2, float u, float v, float3 light) {
+  float3 point = a + u * e1 + v * e2, normal = normalize(cross(e1, e2));
+  if (dot(normal, light) < 0) normal = -normal;
+  constexpr float epsilon = 5.960464477539063e-8f, gamma = 8 * epsilon / (1 - 8 * epsilon);
+  float3 error = f3(gamma * (fabsf(a.x) + fabsf(u * e1.x) + fabsf(v * e2.x)),
+                    gamma * (fabsf(a.y) + fabsf(u * e1.y) + fabsf(v * e2.y)),
+                    gamma * (fabsf(a.z) + fabsf(u * e1.z) + fabsf(v * e2.z)));
+  float distance = fabsf(normal.x) * error.x + fabsf(normal.y) * error.y + fabsf(normal.z) * error.z + 1e-6f;
+  float3 offset = normal * distance;
+  point = point + offset;
+  if (offset.x != 0) point.x = nextafterf(point.x, copysignf(kInf(), offset.x));
+  if (offset.y != 0) point.y = nextafterf(point.y, copysignf(kInf(), offset.y));
+  if (offset.z != 0) point.z = nextafterf(point.z, copysignf(kInf(), offset.z));
+  return point;
+}
+
+struct PixelSample {
+  double radiance;
+  float depth;
+  bool valid;
+  unsigned primary, shadow;
+};
+
+// What one pixel sample produces.
+enum SampleMode : int { kRadiance = 0, kRadianceDepth = 1, kDepthOnly = 2 };
+
+// cos^4 field falloff (device_optics.cuh:90) in FP64, as the reference.
+__device__ __forceinline__ double cos4_of(float px, float py) {
+  return 1.0 / ((1.0 + px * px + py * py) * (1.0 + px * px + py * py));
+}
+__device__ __forceinline__ float subray_x(const SceneView &S, int px_i, int sx) {
+  return (px_i + (sx + .5f) / S.samples - .5f - S.cx) / S.fx;
+}
+__device__ __forceinline__ float subray_y(const SceneView &S, int py_i, int sy) {
+  return (py_i + (sy + .5f) / S.samples - .5f - S.cy) / S.fy;
+}
+
+// sample_pixel (device_optics.cuh:73-94) for one lane of a converged warp.
+// cos4_table: when every lane of the warp samples the same pixel, the FP64
+// cos^4 of each sub-ray is computed once per warp (shared memory) instead of
+// once per lane; otherwise nullptr.
+template <int kMode>
+__device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool active, const CellPose &pose,
+                                           int *stack_code, float *stack_t, const double *cos4_table) {
+  PixelSample out{0.0, -1.0f, true, 0u, 0u};
+  double depth = 0;
+  int valid_depth = 0;
+  const float3 light = f3(pose.lx, pose.ly, pose.lz);
+  const float3 origin = f3(pose.px, pose.py, pose.pz);
+  const int ss = S.samples;
+  const int px_i = pixel % S.width, py_i = pixel / S.width;
+  for (int sy = 0; sy < ss; ++sy)
+    for (int sx = 0; sx < ss; ++sx) {
+      const float px = subray_x(S, px_i, sx);
+      const float py = subray_y(S, py_i, sy);
+      const float3 ray = normalize(rotate_ray(pose, f3(px, -py, -1)));
+      const HitRecord hit = trace_nearest_packet(S, origin, ray, active && out.valid, stack_code, stack_t);
+      if (active && out.valid) ++out.primary;
+      if (hit.hit < 0) out.valid = false;
+      const bool hitp = active && out.valid && hit.hit == 1;
+      bool lit = false;
+      float3 normal = f3(0, 0, 0), sorigin = f3(0, 0, 0);
+      float albedo = S.hapke.w;
+      if (hitp) {
+        if (kMode != kRadiance) {
+          depth += hit.t;
+          ++valid_depth;
+        }
+        if (kMode != kDepthOnly) {
+          const ShadeRecord *sr = S.shade + hit.tri;
+          const float4 *q = reinterpret_cast<const float4 *>(sr);
+          const float4 s0 = __ldg(q), s1 = __ldg(q + 1), s2 = __ldg(q + 2);
+          const float w = 1 - hit.u - hit.v;
+          normal = normalize(f3(s0.x, s0.y, s0.z) * w + f3(s1.x, s1.y, s1.z) * hit.u + f3(s2.x, s2.y, s2.z) * hit.v);
+          lit = !(dot(normal, light) <= 0 || dot(normal, -ray) <= 0);
+          if (lit) {
+            const float4 *r = reinterpret_cast<const float4 *>(S.tris + hit.tri);
+            const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
+            sorigin = shadow_origin(f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, c.x), hit.u, hit.v, light);
+            if (S.has_albedo) albedo = s0.w * w + s1.w * hit.u + s2.w * hit.v;
+          }
+        }
+      }
+      if (kMode != kDepthOnly) {
+        if (__any_sync(kFull, lit)) {
+          if (lit) ++out.shadow;
+          const bool occ = trace_shadow_packet(S, sorigin, light, lit, hit.tri, stack_code, stack_t);
+          if (lit && !occ) {
+            const double cos4 = cos4_table ? cos4_table[sy * ss + sx] : cos4_of(px, py);
+            // hapke_directional_reflectance (hapke.hpp:153-157)
+            const float3 n = normalize(normal), l = normalize(light), v = normalize(-ray);
+            const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo, S.hapke);
+            out.radiance += fmaxf(0, n_h * pose.intensity) * cos4;
+          }
+        }
+      }
+    }
+  out.radiance /= ss * ss;
+  out.depth = valid_depth ? float(depth / valid_depth) : -1.0f;
+  return out;
+}
+
+__device__ __forceinline__ unsigned warp_sum(unsigned v) { return __reduce_add_sync(kFull, v); }
+
+}  // namespace
+}  // namespace dvsgb

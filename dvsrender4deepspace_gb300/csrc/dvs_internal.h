@@ -11,16 +11,23 @@
 namespace dvsgb {
 
 // ---- wide BVH --------------------------------------------------------------
-// A 4-wide node, 128 bytes = 8 x 16-byte vector loads.  Child bounds are
-// stored per axis so one float4 load yields the same coordinate of all four
-// children.  child[c]: inner node index when count[c]==0, first triangle
-// (leaf order) when count[c]>0; count[c]<0 marks an empty slot.
-struct alignas(16) Bvh4Node {
-  float lo_x[4], hi_x[4], lo_y[4], hi_y[4], lo_z[4], hi_z[4];
-  int32_t child[4];
-  int32_t count[4];
+// An 8-wide node is eight 32-byte child records (256 bytes).  Lane c of a
+// warp reads child record c with two 16-byte loads, so the eight lanes that
+// test one node read it as one coalesced 256-byte access.
+// child: inner node index when count==0, first triangle (leaf order) when
+// count>0; count<0 marks an empty slot.
+constexpr int kBvhWidth = 8;
+struct alignas(32) BvhChild {
+  float lo[3];
+  float hi[3];
+  int32_t child;
+  int32_t count;
 };
-static_assert(sizeof(Bvh4Node) == 128, "Bvh4Node layout");
+struct alignas(256) BvhNode {
+  BvhChild c[kBvhWidth];
+};
+static_assert(sizeof(BvhChild) == 32, "BvhChild layout");
+static_assert(sizeof(BvhNode) == 256, "BvhNode layout");
 
 // Intersection record in leaf order, 48 bytes = 3 x 16-byte loads.  Edges are
 // precomputed with the same float subtraction the reference performs per test
@@ -46,20 +53,21 @@ struct alignas(16) ShadeRecord {
 };
 static_assert(sizeof(ShadeRecord) == 64, "ShadeRecord layout");
 
-// Maximum warp-stack depth; the builder rejects trees that could exceed it.
+// Maximum warp-stack depth; the builder rejects trees that could exceed it
+// (a depth-first walk of a W-wide tree holds at most (W-1)*depth+1 entries).
 constexpr int kStackSlots = 96;
 
-struct Bvh4Build {
-  std::vector<Bvh4Node> nodes;
+struct BvhBuild {
+  std::vector<BvhNode> nodes;
   std::vector<uint32_t> order;  // leaf order -> original triangle index
-  int depth = 0;                // levels of 4-wide nodes
+  int depth = 0;                // levels of wide nodes
   double seconds = 0;
 };
 
-// Morton-ordered radix-split binary tree collapsed to a 4-wide tree.
+// Morton-ordered radix-split binary tree collapsed to an 8-wide tree.
 // Returns false with a message on invalid input.
-bool build_bvh4(const float *vertices, size_t n_vertices, const uint32_t *indices, size_t n_triangles,
-                int leaf_size, Bvh4Build &out, std::string &error);
+bool build_bvh(const float *vertices, size_t n_vertices, const uint32_t *indices, size_t n_triangles,
+               int leaf_size, BvhBuild &out, std::string &error);
 
 // ---- FIFO readout (src/event_readout.cpp:6-34 semantics) ---------------------
 struct HostEvent {

@@ -9,12 +9,13 @@
 namespace dvsgb {
 
 struct SceneView {
-  const Bvh4Node *nodes;
+  const BvhNode *nodes;
   const TriRecord *tris;
   const ShadeRecord *shade;
   const int32_t *pixel_of_rank;  // Morton rank -> row-major pixel index
   int32_t width, height, samples, has_albedo;
   float fx, fy, cx, cy;
+  float coherent_span;  // largest origin spread a warp packet traverses as one interval bundle
   dvs_hapke hapke;
 };
 
@@ -65,6 +66,14 @@ enum : int32_t { kErrCapacity = 1, kErrOptical = 2, kErrStalled = 4 };
 // Device counters.
 enum : int { kCntPrimary = 0, kCntShadow = 1, kCntCells = 2, kCntSlots = 4 };
 
+// Radiance knot of the adaptive path (optical_sampler.hpp:278): fraction of
+// the window (negative: the segment ending here is traced exactly per cell).
+struct OpticalKnot {
+  double fraction, radiance;
+};
+// Refinement counters (OpticalRefinementStats, optical_sampler.hpp:281).
+enum : int { kRefTraced = 0, kRefFallback = 1, kRefMaxKnots = 2, kRefExactSegments = 3, kRefSlots = 4 };
+
 // ---- launchers (return cudaGetLastError()) ----------------------------------
 cudaError_t launch_pose_from_state(const dvs_optical_state *state, CellPose *out, cudaStream_t s);
 cudaError_t launch_cell_poses(const dvs_optical_interval *ivs, const Cell *cells, int n_cells, CellPose *out,
@@ -86,6 +95,40 @@ cudaError_t launch_emit_events(int n_pix, const int32_t *pixel_of_rank, int widt
 cudaError_t launch_event_depth(const SceneView &scene, const dvs_optical_interval *ivs, int n_ivs, DevEvent *events,
                                const int32_t *count, int32_t *error, unsigned long long *counters,
                                cudaStream_t s);
+// Same kernels over a list of Morton ranks (row r of the radiance chunk is rank rank_list[r]).
+cudaError_t launch_trace_list(const SceneView &scene, int n_pix, const int32_t *rank_list, const CellPose *poses,
+                              int c0, int nc, int cw_log2, double *radiance, float *depth, unsigned long long *counters,
+                              cudaStream_t s);
+cudaError_t launch_circuit_list(int n, const int32_t *rank_list, const Cell *cells, int c0, int nc,
+                                const double *radiance, PixelParams p, PhotoParams photo, int max_events,
+                                CircuitState st, int32_t *ev_count, double *slab_t, int8_t *slab_p, int32_t *error,
+                                unsigned long long *counters, cudaStream_t s);
+// Adaptive optical refinement (adaptive.cu).
+cudaError_t launch_refine(const SceneView &scene, int n, const dvs_optical_interval *ivs, int n_ivs, double start,
+                          double end, PhotoParams photo, double tolerance, CircuitState st, double charge,
+                          int capacity, OpticalKnot *knots, int32_t *counts, unsigned long long *ref_stats,
+                          int32_t *error, unsigned long long *counters, cudaStream_t s);
+cudaError_t launch_identify_exact(int n, const Cell *cells, int n_cells, double start, double end,
+                                  const OpticalKnot *knots, int32_t *knot_counts, int capacity, int32_t *exact_cells,
+                                  int32_t *exact_counts, int32_t *queue, int32_t *total,
+                                  unsigned long long *ref_stats, cudaStream_t s);
+cudaError_t launch_sample_exact(const SceneView &scene, const CellPose *poses, const int32_t *exact_cells,
+                                const int32_t *queue, const int32_t *total, int capacity, double *exact_radiance,
+                                int32_t *error, unsigned long long *counters, cudaStream_t s);
+cudaError_t launch_integrate_knots(int n, const Cell *cells, int n_cells, double start, double end,
+                                   const OpticalKnot *knots, const int32_t *knot_counts, int capacity,
+                                   const int32_t *exact_cells, const double *exact_radiance,
+                                   const int32_t *exact_counts, PixelParams p, PhotoParams photo, int max_events,
+                                   CircuitState st, int32_t *ev_count, double *slab_t, int8_t *slab_p,
+                                   int32_t *error, cudaStream_t s);
+cudaError_t launch_compact_fallback(int n, const int32_t *knot_counts, int32_t *list, int32_t *total,
+                                    cudaStream_t s);
+cudaError_t launch_capture_probes(int n_probes, const int32_t *probe_ranks, const double *receptor_log,
+                                  double *probe_state, cudaStream_t s);
+cudaError_t launch_advance_probes(int n_probes, const int32_t *probe_ranks, const Cell *cells, int c0, int nc,
+                                  const double *light, const OpticalKnot *knots, const int32_t *knot_counts,
+                                  int capacity, double start, double end, PhotoParams photo, double charge,
+                                  double *probe_state, cudaStream_t s);
 cudaError_t launch_radiance_to_float(int n_pix, const int32_t *pixel_of_rank, const double *radiance,
                                      const float *depth, float *image, float *depth_image, cudaStream_t s);
 

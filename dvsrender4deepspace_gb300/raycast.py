@@ -126,7 +126,7 @@ class EventSensor:
     """EventSensor (include/dvs/event_sensor.hpp:40-79) on the GB300 path."""
 
     def __init__(self, scene, physic, physic_effects=True, aer_delay=True, cells_per_chunk=0, cells_per_warp=0,
-                 timing=False):
+                 timing=False, row_begin=0, row_end=0):
         lib = _capi.load()
         self.scene = scene
         self.physic = dict(physic)
@@ -137,10 +137,13 @@ class EventSensor:
         opt.cells_per_chunk = int(cells_per_chunk)
         opt.cells_per_warp = int(cells_per_warp)
         opt.timing = int(timing)
+        opt.row_begin = int(row_begin)
+        opt.row_end = int(row_end)
         h = C.c_void_p()
         check(lib.dvs_sensor_create(scene.handle, C.byref(physic_struct(physic)), C.byref(opt), C.byref(h)))
         self.handle = h
         self.max_events = int(physic["max_events_per_step"])
+        self.rows = (int(row_begin), int(row_end)) if row_end > row_begin else None
 
     def initialize(self, pose, timestamp):
         st = state_array(pose)
@@ -154,6 +157,33 @@ class EventSensor:
         n = C.c_size_t()
         check(_capi.load().dvs_sensor_process(self.handle, ivs.ctypes.data, len(ivs), C.byref(n)))
         return self._read(n.value)
+
+    def process_adaptive(self, intervals, log_tolerance=1e-2, check_convergence=False):
+        """EventSensor::process_adaptive: returns the ready events, or None
+        when the convergence gate rejected the window (nothing changed)."""
+        ivs = interval_array(intervals)
+        n = C.c_size_t()
+        accepted = C.c_int32()
+        check(_capi.load().dvs_sensor_process_adaptive(self.handle, ivs.ctypes.data, len(ivs), float(log_tolerance),
+                                                       int(check_convergence), C.byref(accepted), C.byref(n)))
+        if not accepted.value:
+            return None
+        return self._read(n.value)
+
+    def refinement_statistics(self):
+        out = _capi.RefinementStats()
+        check(_capi.load().dvs_sensor_refinement_stats(self.handle, C.byref(out)))
+        return out.as_dict()
+
+    def last_convergence(self):
+        out = _capi.ReceptorProbe()
+        check(_capi.load().dvs_sensor_last_convergence(self.handle, C.byref(out)))
+        return out.as_dict()
+
+    def adaptive_cache_capacity(self):
+        out = C.c_int32()
+        check(_capi.load().dvs_sensor_adaptive_capacity(self.handle, C.byref(out)))
+        return out.value
 
     def enqueue(self, intervals):
         """Launches a batch without waiting; events stay on the device."""
@@ -201,7 +231,7 @@ class EventSensor:
         return _capi.load().dvs_sensor_stream(self.handle)
 
     def read_state(self):
-        n = self.scene.pixels
+        n = self.scene.pixels if not self.rows else (self.rows[1] - self.rows[0]) * self.scene.width
         st = np.zeros((n, 5), np.float64)
         rp = np.zeros(n, np.int32)
         check(_capi.load().dvs_sensor_read_state(self.handle, st.ctypes.data_as(C.POINTER(C.c_double)),
@@ -216,6 +246,52 @@ class EventSensor:
     def __del__(self):
         try:
             self.close()
+        except Exception:
+            pass
+
+
+class EventReadout:
+    """EventReadout (include/dvs/event_sensor.hpp:24-37): the finite FIFO bus,
+    host side, for event runs merged from several sensors."""
+
+    def __init__(self, bandwidth, latency, capacity):
+        h = C.c_void_p()
+        check(_capi.load().dvs_readout_create(float(bandwidth), float(latency), int(capacity), C.byref(h)))
+        self.handle = h
+
+    def _read(self, n):
+        out = np.zeros(max(n, 1), EVENT_DTYPE)
+        got = C.c_size_t()
+        check(_capi.load().dvs_readout_read(self.handle, out.ctypes.data, len(out), C.byref(got)))
+        return out[: got.value].copy()
+
+    def submit(self, events, now):
+        ev = np.ascontiguousarray(events, EVENT_DTYPE) if len(events) else np.zeros(0, EVENT_DTYPE)
+        n = C.c_size_t()
+        check(_capi.load().dvs_readout_submit(self.handle, ev.ctypes.data if len(ev) else None, len(ev), float(now),
+                                              C.byref(n)))
+        return self._read(n.value)
+
+    def drain(self):
+        n = C.c_size_t()
+        check(_capi.load().dvs_readout_drain(self.handle, C.byref(n)))
+        return self._read(n.value)
+
+    def dropped(self):
+        d, p = C.c_uint64(), C.c_uint64()
+        check(_capi.load().dvs_readout_counters(self.handle, C.byref(d), C.byref(p)))
+        return d.value
+
+    def peak_queue(self):
+        d, p = C.c_uint64(), C.c_uint64()
+        check(_capi.load().dvs_readout_counters(self.handle, C.byref(d), C.byref(p)))
+        return p.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                _capi.load().dvs_readout_destroy(self.handle)
+                self.handle = None
         except Exception:
             pass
 

@@ -99,7 +99,8 @@ typedef struct {
   int32_t cells_per_chunk;    /* circuit cells traced per optics launch (0 = automatic) */
   int32_t cells_per_warp;     /* 1,2,4,8,16,32: cells sharing one warp packet (0 = automatic) */
   int32_t timing;             /* record per-kernel CUDA-event timings */
-  int32_t reserved[3];
+  int32_t row_begin, row_end; /* rows [row_begin, row_end) only (one GPU's share); 0,0 = all */
+  int32_t reserved;
 } dvs_sensor_options;
 
 typedef struct {
@@ -123,6 +124,18 @@ typedef struct {
   double optics_ms, circuit_ms, events_ms, readout_ms; /* with options.timing */
   uint64_t optics_launches, circuit_launches;
 } dvs_sensor_stats;
+
+/* OpticalRefinementStats (include/dvs/optical_sampler.hpp:281). */
+typedef struct {
+  uint64_t traced_pixel_samples;
+  int32_t fallback_pixels, maximum_knots, exact_segments, native_cell_queries;
+} dvs_refinement_stats;
+
+/* ReceptorProbeResult (include/dvs/event_sensor.hpp:39). */
+typedef struct {
+  double maximum_log_voltage_error, p99_log_voltage_error, mean_log_voltage_error;
+  int32_t pixels, circuit_cells;
+} dvs_receptor_probe;
 
 typedef struct dvs_scene dvs_scene;
 typedef struct dvs_sensor dvs_sensor;
@@ -200,13 +213,42 @@ int dvs_sensor_read(dvs_sensor *sensor, dvs_event *out, size_t capacity, size_t 
 /* process + read in one call; DVS_ERR_OUTPUT_SMALL leaves the events readable. */
 int dvs_sensor_process_events(dvs_sensor *sensor, const dvs_optical_interval *intervals,
                               size_t n_intervals, dvs_event *out, size_t capacity, size_t *n_out);
+/* EventSensor::process_adaptive (event_sensor.cu:306-355) with
+ * OpticalSampler::refine / prepare_exact_cells (optical_sampler.cu:39-138,
+ * 176-264): per-pixel adaptive optical knots, exact tracing of unresolved
+ * cells, full native tracing of pixels whose knot cache overflows.  With
+ * check_convergence the receptor-convergence gate runs first
+ * (event_sensor.cu:318-326); a rejected window sets *accepted = 0 and
+ * changes no pixel, RNG or time state (the caller retries, as
+ * apps/main_dvs.cpp:308-312 does).  Events carry depth -1. */
+int dvs_sensor_process_adaptive(dvs_sensor *sensor, const dvs_optical_interval *intervals, size_t n_intervals,
+                                double log_tolerance, int32_t check_convergence, int32_t *accepted,
+                                size_t *n_ready);
+/* OpticalSampler::statistics / EventSensor::last_convergence / knot_capacity. */
+int dvs_sensor_refinement_stats(const dvs_sensor *sensor, dvs_refinement_stats *out);
+int dvs_sensor_last_convergence(const dvs_sensor *sensor, dvs_receptor_probe *out);
+int dvs_sensor_adaptive_capacity(dvs_sensor *sensor, int32_t *knot_capacity);
 /* EventSensor::drain / EventReadout::drain (event_readout.cpp:31-34). */
 int dvs_sensor_drain(dvs_sensor *sensor, dvs_event *out, size_t capacity, size_t *n_out);
 int dvs_sensor_stats_get(const dvs_sensor *sensor, dvs_sensor_stats *out);
 int dvs_sensor_stats_reset(dvs_sensor *sensor);
+/* ---- standalone readout FIFO: EventReadout (include/dvs/event_sensor.hpp:24-37,
+ *      src/event_readout.cpp:6-34).  Host only; used to read out event runs
+ *      merged from several sensors (one per GPU) through one bus. ----------- */
+typedef struct dvs_readout dvs_readout;
+int dvs_readout_create(double bandwidth, double latency, size_t capacity, dvs_readout **out);
+int dvs_readout_destroy(dvs_readout *readout);
+/* Orders `events` by (timestamp, y, x), queues them and makes the events
+ * delivered by `now` readable with dvs_readout_read (*n_ready = how many). */
+int dvs_readout_submit(dvs_readout *readout, const dvs_event *events, size_t n_events, double now,
+                       size_t *n_ready);
+int dvs_readout_drain(dvs_readout *readout, size_t *n_ready);
+int dvs_readout_read(dvs_readout *readout, dvs_event *out, size_t capacity, size_t *n_out);
+int dvs_readout_counters(const dvs_readout *readout, uint64_t *dropped, uint64_t *peak_queue);
+
 /* The CUDA stream (cudaStream_t) the handle launches on, for external timing. */
 void *dvs_sensor_stream(dvs_sensor *sensor);
-/* Per-pixel circuit state, row-major pixel order: 5 doubles per pixel
+/* Per-pixel circuit state in row-major order of the sensor's rows: 5 doubles per pixel
  * (receptor_log, reference_log, refractory_until, threshold_pos, threshold_neg)
  * and one int32 reset flag.  Either pointer may be NULL. */
 int dvs_sensor_read_state(dvs_sensor *sensor, double *state5, int32_t *reset_pending);

@@ -114,6 +114,39 @@ int main() {
     assert r.returncode == 0 and "index" in r.stdout, r.stdout + r.stderr
 
 
+def test_library_readout_matches_reference_fixtures(lib, golden):
+    """The library's FIFO (readout.cpp) against the reference EventReadout's
+    outputs on the same batches (tests/golden/readout.npz)."""
+    from dvsrender4deepspace_gb300.raycast import EventReadout
+    g = golden("readout")
+    for k in range(4):
+        bw, lat, cap = g["s%d_cfg" % k]
+        r = EventReadout(bw, lat, int(cap))
+        for b in range(3):
+            out = r.submit(g["s%d_in%d" % (k, b)], float(g["s%d_now%d" % (k, b)]))
+            exp = g["s%d_out%d" % (k, b)]
+            assert len(out) == len(exp)
+            for f in exp.dtype.names:
+                np.testing.assert_array_equal(out[f], exp[f])
+        out = r.drain()
+        np.testing.assert_array_equal(out["timestamp"], g["s%d_drain" % k]["timestamp"])
+        assert r.dropped() == int(g["s%d_dropped" % k]) and r.peak_queue() == int(g["s%d_peak" % k])
+
+
+def test_library_fifo_known_answer(lib):
+    # tests/test_sensor.cu:176-177
+    from dvsrender4deepspace_gb300.raycast import EventReadout
+    r = EventReadout(100, .001, 2)
+    ev = np.zeros(3, _capi.EVENT_DTYPE)
+    ev["x"] = [0, 1, 2]
+    ev["polarity"] = 1
+    ev["depth"] = 1
+    assert len(r.submit(ev, .005)) == 0 and r.dropped() == 1
+    out = r.submit(np.zeros(0, _capi.EVENT_DTYPE), .012)
+    assert len(out) == 1 and abs(out[0]["timestamp"] - .011) < 1e-12
+    assert len(r.drain()) == 1
+
+
 def test_sensor_calls_reject_null_handles(lib):
     h = C.c_void_p()
     assert lib.dvs_sensor_create(None, None, None, C.byref(h)) == _capi.DVS_ERR_INVALID

@@ -157,7 +157,9 @@ def test_sensor_pulse_matches_oracle_full_resolution():
     ev, oev = pixel_sorted(ev), pixel_sorted(oev)
     for f in ("x", "y", "polarity"):
         np.testing.assert_array_equal(ev[f], oev[f])
-    assert np.max(np.abs(ev["timestamp"] - oev["timestamp"])) < 1e-9
+    dt = np.abs(ev["timestamp"] - oev["timestamp"])
+    assert np.max(dt) < 1e-6          # the stated timestamp tolerance
+    assert np.median(dt) < 1e-15      # almost every crossing is the same double
     assert np.max(rel_err(ev["depth"], oev["depth"])) < RTOL
 
 
@@ -274,3 +276,27 @@ def test_sensor_matches_oracle_on_moving_terrain():
             worst = max(worst, max(abs(x - y) for (x, _), (y, _) in zip(a, b)))
     assert mismatched <= max(1, 0.002 * cam["width"] * cam["height"]), mismatched
     assert worst < 1e-6
+
+
+def test_row_band_sensors_reproduce_the_full_sensor():
+    """One GPU's share of a split sensor (dvs_sensor_options.row_begin/row_end)
+    gives exactly the full sensor's events of those rows."""
+    from dvsrender4deepspace_gb300 import shard
+    scene, phys = plane_sensor(photon_shot_noise=1, threshold_pos=0.05, threshold_neg=0.05)
+    start, end = dict(POSE, intensity_rate=8e6), dict(POSE, intensity_rate=-8e6)
+    ivs = [(POSE, POSE, 0, .0005), (start, end, .0005, .0015)]
+    full = EventSensor(scene, phys)
+    full.initialize(POSE, 0)
+    want = full.process_many(ivs)
+    got = []
+    for r0, r1 in shard.row_bands(DAVIS["height"], 3):
+        band = EventSensor(scene, phys, row_begin=r0, row_end=r1)
+        band.initialize(POSE, 0)
+        ev = band.process_many(ivs)
+        assert np.all((ev["y"] >= r0) & (ev["y"] < r1))
+        got.append(ev)
+    merged = shard.merge_runs(got)
+    assert len(merged) == len(want) > 0
+    a, b = pixel_sorted(merged), pixel_sorted(want)
+    for f in ("timestamp", "x", "y", "polarity", "depth"):
+        np.testing.assert_array_equal(a[f], b[f])
