@@ -54,7 +54,8 @@ def build(force=False, verbose=False):
     for src in _sources():
         obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
         if src.endswith(".cu"):
-            cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-Xcompiler", xhost, *inc,
+            cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
+                   "-prec-sqrt=true", *os.environ.get("DVS_NVCC_DEFINES", "").split(), "-Xcompiler", xhost, *inc,
                    "-c", src, "-o", obj]
         else:
             cmd = [os.environ.get("CXX", "g++"), *HOST_FLAGS, *inc, "-I",

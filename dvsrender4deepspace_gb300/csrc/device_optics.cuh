@@ -88,7 +88,14 @@ __device__ __forceinline__ float eta_f(float thetap, float cosy, float siny) {
 }
 __device__ __forceinline__ float f_psi(float psi) { return expf(-2.0f * tanf(psi * 0.5f)); }
 
-__device__ float hapke_reflectance(float cosi, float cose, float cosg, float albedo, const dvs_hapke &p) {
+// Inlining policy of the large shading and traversal bodies (instruction-cache pressure).
+#ifdef DVS_OUTLINE_SHADING
+#define DVS_SHADE_INLINE __noinline__
+#else
+#define DVS_SHADE_INLINE
+#endif
+DVS_SHADE_INLINE __device__ float hapke_reflectance(float cosi, float cose, float cosg, float albedo,
+                                                    const dvs_hapke &p) {
   if (cosi <= 0 || cose <= 0) return 0;
   cosi = clampf(cosi, 0, 1);
   cose = clampf(cose, 0, 1);
@@ -424,7 +431,8 @@ __device__ HitRecord trace_nearest_packet(const SceneView &S, float3 o, float3 d
 
 // Any hit toward the light (trace_shadow_ray_any_hit, device_ray.hpp:81-135):
 // skips the camera-hit triangle, t in (kRayEps, 1e30); overflow counts as occluded.
-__device__ bool trace_shadow_packet(const SceneView &S, float3 o, float3 d, bool active, int self, int *stack_code,
+DVS_SHADE_INLINE __device__ bool trace_shadow_packet(const SceneView &S, float3 o, float3 d, bool active, int self,
+                                                     int *stack_code,
                                     float *stack_t) {
   const float3 idir = inverse_direction(d);
   bool alive = active;

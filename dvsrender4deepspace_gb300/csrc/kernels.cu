@@ -50,10 +50,15 @@ __global__ void cell_poses_kernel(const dvs_optical_interval *ivs, const Cell *c
 }
 
 constexpr int kWarpsPerBlock = 4;  // all ray kernels launch 128 threads
+// Resident blocks per SM the trace kernel is compiled for (caps its registers).
+#ifndef DVS_TRACE_MIN_BLOCKS
+#define DVS_TRACE_MIN_BLOCKS 1
+#endif
 constexpr int kCos4Table = 256;    // sub-rays per pixel with a shared cos^4 table (ss <= 16)
 
 template <int kMode>
-__global__ void __launch_bounds__(128) trace_cells_kernel(SceneView S, int n_pix, const int32_t *rank_list,
+__global__ void __launch_bounds__(128, DVS_TRACE_MIN_BLOCKS) trace_cells_kernel(SceneView S, int n_pix,
+                                                                                const int32_t *rank_list,
                                                           const CellPose *poses, int c0, int nc, int cw_log2,
                                                           double *radiance, float *depth_out,
                                                           unsigned long long *counters) {
