@@ -286,7 +286,7 @@ def run_gb300(args):
                    "circuit_step": PHYSIC["circuit_step"], "shot_noise": "curand_xorwow", "sun_elevation_deg":
                    w["sun_elevation"], "intensity": w["intensity"], "l2": "inputs larger than L2 (scene %.1f GB)"
                    % (info["device_bytes"] / 1e9), "parallelism": "dp%d (independent jobs)" % world,
-                   "bvh": "4-wide Morton radix, leaf %d, depth %d" % (args.leaf, info["depth"])},
+                   "bvh": "8-wide Morton radix, leaf %d, depth %d" % (info["leaf_size"], info["depth"])},
         "rays_per_step": rays / args.steps, "events_per_s": delivered_all / e2e_s,
         "events_generated_per_step": gen2 / args.steps,
         "e2e": {"value": e2e_value, "unit": "Mrays/s",
@@ -319,7 +319,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="precision", choices=sorted(WORKLOADS))
-    ap.add_argument("--leaf", type=int, default=4)
+    ap.add_argument("--leaf", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--cw", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

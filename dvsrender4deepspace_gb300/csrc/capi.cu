@@ -2,7 +2,7 @@
 //
 // dvs_scene  replaces BVHBuilder::build + DeviceScene (src/bvh/build.cpp:27-76,
 //            src/cuda/device_scene.cu:15-37): one device arena holds the
-//            4-wide BVH, the leaf-order triangle and shading records and the
+//            8-wide BVH, the leaf-order triangle and shading records and the
 //            Morton pixel order.
 // dvs_sensor replaces EventSensor (src/cuda/event_sensor.cu:244-305): circuit
 //            state in structure-of-arrays form, cuRAND XORWOW per pixel,
@@ -133,7 +133,7 @@ struct dvs_scene {
   int32_t *pixel_of_rank = nullptr;
   std::vector<int32_t> rank_of_pixel;  // host inverse of pixel_of_rank
   size_t n_nodes = 0, n_tris = 0, n_vertices = 0;
-  int depth = 0;
+  int depth = 0, leaf_size = 0;
   double build_seconds = 0;
   float coherent_span = 1.0f;  // 0.5 % of the scene's largest extent
   // camera render buffers
@@ -287,11 +287,20 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
     if (!std::isfinite(vertices[i])) return fail(DVS_ERR_INVALID, "nonfinite mesh vertex");
   for (size_t i = 0; i < 3 * n_vertices; ++i)
     if (!std::isfinite(normals[i])) return fail(DVS_ERR_INVALID, "nonfinite mesh normal");
-  const int leaf = params && params->leaf_size > 0 ? params->leaf_size : 4;
-
+  // Default: two triangles per leaf (the fastest on terrain meshes); when the
+  // tree would be too deep for the traversal stack, wider leaves.  A leaf
+  // size given by the caller is used as given.
+  const bool leaf_given = params && params->leaf_size > 0;
   BvhBuild bvh;
   std::string err;
-  if (!build_bvh(vertices, n_vertices, indices, n_triangles, leaf, bvh, err)) return fail(DVS_ERR_INVALID, err);
+  bool built = false;
+  int leaf = leaf_given ? params->leaf_size : 2;
+  for (;; leaf *= 2) {
+    err.clear();
+    built = build_bvh(vertices, n_vertices, indices, n_triangles, leaf, bvh, err);
+    if (built || leaf_given || leaf >= 8) break;
+  }
+  if (!built) return fail(DVS_ERR_INVALID, err);
 
   // leaf-order records
   std::vector<TriRecord> tris(n_triangles);
@@ -333,6 +342,7 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   s->n_tris = n_triangles;
   s->n_vertices = n_vertices;
   s->depth = bvh.depth;
+  s->leaf_size = leaf;
   s->build_seconds = bvh.seconds;
   {
     float lo[3] = {vertices[0], vertices[1], vertices[2]}, hi[3] = {vertices[0], vertices[1], vertices[2]};
@@ -403,6 +413,8 @@ int dvs_scene_info_get(const dvs_scene *s, dvs_scene_info *out) {
   out->root = 0;
   out->device_bytes = s->arena_bytes;
   out->build_seconds = s->build_seconds;
+  out->leaf_size = s->leaf_size;
+  out->reserved = 0;
   return DVS_OK;
 }
 

@@ -55,38 +55,51 @@ __device__ __forceinline__ float b_c(float tg, float h) {
   if (T < 1e-8f) return 1.0f;
   return (1.0f + (1.0f - expf(-T)) / T) / (2.0f * (1.0f + T) * (1.0f + T));
 }
-__device__ __forceinline__ float hfunc(float x, float w) {
+__device__ __forceinline__ float hfunc(float x, float w, float r0) {
   if (x <= 1e-8f) return 1.0f;
-  const float root = sqrtf(fmaxf(0.0f, 1.0f - w));
-  const float r0 = (1.0f - root) / (1.0f + root);
   const float term = r0 + (1.0f - 2.0f * r0 * x) * 0.5f * logf(1.0f + 1.0f / x);
   return 1.0f / (1.0f - w * x * term);
+}
+__device__ __forceinline__ float hfunc_r0(float w) {
+  const float root = sqrtf(fmaxf(0.0f, 1.0f - w));
+  return (1.0f - root) / (1.0f + root);
 }
 __device__ __forceinline__ float porosity_k(float phi) {
   if (phi <= 1e-8f) return 1.0f;
   const float p = 1.209f * powf(phi, 2.0f / 3.0f);
   return -logf(1.0f - p) / p;
 }
-__device__ __forceinline__ float chi_f(float thetap) {
-  const float t = tanf(thetap);
-  return 1.0f / sqrtf(1.0f + kPi * t * t);
+__device__ __forceinline__ float f_psi(float psi) { return expf(-2.0f * tanf(psi * 0.5f)); }
+
+// The parts of hapke.hpp that depend on the material only: porosity K,
+// tan(thetap), 1/tan(thetap), chi(thetap) and the r0 of the H-function for
+// the scene's single-scattering albedo.  Each is the value hapke.hpp
+// recomputes inside every call (same operations, same rounding), evaluated
+// once per pixel sample loop instead of up to fourteen times per shaded ray.
+struct HapkeConst {
+  float K, tan_t, cot_t, chi, r0_w;
+  bool rough;
+};
+__device__ __forceinline__ HapkeConst hapke_const(const dvs_hapke &p) {
+  HapkeConst h;
+  h.K = porosity_k(p.phi);
+  h.rough = !(p.thetap <= 1e-8f);
+  h.tan_t = tanf(p.thetap);
+  h.cot_t = 1.0f / h.tan_t;
+  h.chi = 1.0f / sqrtf(1.0f + kPi * h.tan_t * h.tan_t);
+  h.r0_w = hfunc_r0(p.w);
+  return h;
 }
-__device__ __forceinline__ float e1_f(float thetap, float cosy, float siny) {
+// e1(thetap, y), e2(thetap, y) of hapke.hpp (with 1/tan(thetap) = cot_t).
+__device__ __forceinline__ float e1_c(float cot_t, float cosy, float siny) {
   const float s = fmaxf(siny, 1e-6f);
-  return expf((-2.0f / kPi) * (1.0f / tanf(thetap)) * cosy / s);
+  return expf((-2.0f / kPi) * cot_t * cosy / s);
 }
-__device__ __forceinline__ float e2_f(float thetap, float cosy, float siny) {
+__device__ __forceinline__ float e2_c(float cot_t, float cosy, float siny) {
   const float s = fmaxf(siny, 1e-6f);
-  const float v = (1.0f / tanf(thetap)) * cosy / s;
+  const float v = cot_t * cosy / s;
   return expf((-1.0f / kPi) * v * v);
 }
-__device__ __forceinline__ float eta_f(float thetap, float cosy, float siny) {
-  const float ch = chi_f(thetap);
-  const float e1 = e1_f(thetap, cosy, siny);
-  const float e2 = e2_f(thetap, cosy, siny);
-  return ch * (cosy + siny * tanf(thetap) * e2 / (2.0f - e1));
-}
-__device__ __forceinline__ float f_psi(float psi) { return expf(-2.0f * tanf(psi * 0.5f)); }
 
 // Inlining policy of the large shading and traversal bodies (instruction-cache pressure).
 #ifdef DVS_OUTLINE_SHADING
@@ -94,8 +107,9 @@ __device__ __forceinline__ float f_psi(float psi) { return expf(-2.0f * tanf(psi
 #else
 #define DVS_SHADE_INLINE
 #endif
-DVS_SHADE_INLINE __device__ float hapke_reflectance(float cosi, float cose, float cosg, float albedo,
-                                                    const dvs_hapke &p) {
+// hapke_reflectance (hapke.hpp:131-152); r0 is hfunc's r0 for this albedo.
+DVS_SHADE_INLINE __device__ float hapke_reflectance(float cosi, float cose, float cosg, float albedo, float r0,
+                                                    const dvs_hapke &p, const HapkeConst &h) {
   if (cosi <= 0 || cose <= 0) return 0;
   cosi = clampf(cosi, 0, 1);
   cose = clampf(cose, 0, 1);
@@ -105,20 +119,23 @@ DVS_SHADE_INLINE __device__ float hapke_reflectance(float cosi, float cose, floa
   const float psi = safe_acos((cosg - cosi * cose) / (sini * sine + 1e-6f));
   const float p_g = hg_double_lobe(cosg, p.b, p.c);
   const float BS = b_s(tg, p.hS);
-  const float BC = b_c(tg, p.hC);
-  const float K = porosity_k(p.phi);
+  // b_c is finite, so with B_C0 == 0 the factor (1 + BC * B_C0) is exactly 1
+  // whatever BC is: skip its evaluation.
+  const float BC = p.B_C0 != 0.0f ? b_c(tg, p.hC) : 0.0f;
+  const float K = h.K;
   float mu0, mue, S;
-  const float thetap = p.thetap;
-  if (thetap <= 1e-8f) {
+  if (!h.rough) {
     mu0 = cosi; mue = cose; S = 1.0f;
   } else {
-    const float ch = chi_f(thetap);
-    const float tan_thetap = tanf(thetap);
+    const float ch = h.chi;
+    const float tan_thetap = h.tan_t;
     const float sh = sinf(psi * 0.5f);
     const float s2 = sh * sh;
-    const float e2e = e2_f(thetap, cose, sine), e2i = e2_f(thetap, cosi, sini);
-    const float e1e = e1_f(thetap, cose, sine), e1i = e1_f(thetap, cosi, sini);
-    const float eta_e = eta_f(thetap, cose, sine), eta_i = eta_f(thetap, cosi, sini);
+    const float e2e = e2_c(h.cot_t, cose, sine), e2i = e2_c(h.cot_t, cosi, sini);
+    const float e1e = e1_c(h.cot_t, cose, sine), e1i = e1_c(h.cot_t, cosi, sini);
+    // eta(y) = chi * (cos y + sin y * tan(thetap) * e2(y) / (2 - e1(y)))
+    const float eta_e = ch * (cose + sine * tan_thetap * e2e / (2.0f - e1e));
+    const float eta_i = ch * (cosi + sini * tan_thetap * e2i / (2.0f - e1i));
     const float fp = f_psi(psi);
     if (cosi >= cose) {
       mu0 = ch * (cosi + sini * tan_thetap * (cosf(psi) * e2e + s2 * e2i) / (2.0f - e1e - (psi / kPi) * e1i));
@@ -130,7 +147,7 @@ DVS_SHADE_INLINE __device__ float hapke_reflectance(float cosi, float cose, floa
       S = mue / eta_e * cosi / eta_i * ch / (1.0f - fp + fp * ch * (cose / eta_e));
     }
   }
-  const float M = hfunc(mu0 / K, albedo) * hfunc(mue / K, albedo) - 1.0f;
+  const float M = hfunc(mu0 / K, albedo, r0) * hfunc(mue / K, albedo, r0) - 1.0f;
   const float LS = mu0 / (mu0 + mue + 1e-6f);
   return (albedo / (4.0f * kPi)) * LS * K * (p_g * (1.0f + BS * p.B_S0) + M) * (1.0f + BC * p.B_C0) * S;
 }
@@ -252,48 +269,76 @@ __device__ __forceinline__ bool slab(float3 lo, float3 hi, float3 o, float3 idir
 // is entered when some ray of the box could hit it: every bound is an
 // extreme of the same rounded operations each ray performs, so the packet
 // never culls a node that one of its rays would enter.
+//
+// Packets use interval tests only when each axis' inverse direction keeps
+// one sign across the packet.  Where a direction component changes sign
+// inside the packet (near-axial rays, e.g. the image centre of a nadir
+// camera) its inverse spans -1e20..1e20 and that axis culls nothing, so such
+// packets take the per-ray path.
 struct Packet {
   float3 olo, ohi, ilo, ihi;
+  // per axis: the origin bound that gives the earliest entry (o_near) and
+  // the latest exit (o_far), and whether the direction is negative
+  float3 o_near, o_far;
+  bool nx, ny, nz;
   bool coherent;
 };
-__device__ __forceinline__ void interval_mul(float a0, float a1, float b0, float b1, float &lo, float &hi) {
-  const float p0 = a0 * b0, p1 = a0 * b1, p2 = a1 * b0, p3 = a1 * b1;
-  lo = fminf(fminf(p0, p1), fminf(p2, p3));
-  hi = fmaxf(fmaxf(p0, p1), fmaxf(p2, p3));
-}
-__device__ __forceinline__ void axis_bounds(float lo, float hi, float olo, float ohi, float ilo, float ihi, float &L,
-                                            float &U) {
-  float a0, a1, b0, b1;
-  interval_mul(lo - ohi, lo - olo, ilo, ihi, a0, a1);
-  interval_mul(hi - ohi, hi - olo, ilo, ihi, b0, b1);
-  L = fminf(a0, b0);
-  U = fmaxf(a1, b1);
+// Interval slab bounds of one axis for a packet whose inverse direction has
+// one sign: the entry plane is the near one for every ray, and the extreme
+// of the four corner products (lo/hi plane offset x ilo/ihi) is the one
+// picked by the sign of the plane offset.  Rounded subtraction and
+// multiplication are monotone, so L and U equal the four-product interval
+// bounds (up to the sign of a zero) with a third of the arithmetic.
+__device__ __forceinline__ void axis_bounds_fixed(float lo, float hi, bool neg, float on, float of, float ilo,
+                                                  float ihi, float &L, float &U) {
+  const float aN = (neg ? hi : lo) - on;
+  const float aF = (neg ? lo : hi) - of;
+  L = aN * (aN >= 0.0f ? ilo : ihi);
+  U = aF * (aF >= 0.0f ? ihi : ilo);
 }
 __device__ __forceinline__ bool packet_slab(const ChildRec &c, const Packet &P, float t_min, float t_max,
                                             float &tnear) {
   float Lx, Ux, Ly, Uy, Lz, Uz;
-  axis_bounds(c.lo.x, c.hi.x, P.olo.x, P.ohi.x, P.ilo.x, P.ihi.x, Lx, Ux);
-  axis_bounds(c.lo.y, c.hi.y, P.olo.y, P.ohi.y, P.ilo.y, P.ihi.y, Ly, Uy);
-  axis_bounds(c.lo.z, c.hi.z, P.olo.z, P.ohi.z, P.ilo.z, P.ihi.z, Lz, Uz);
+  axis_bounds_fixed(c.lo.x, c.hi.x, P.nx, P.o_near.x, P.o_far.x, P.ilo.x, P.ihi.x, Lx, Ux);
+  axis_bounds_fixed(c.lo.y, c.hi.y, P.ny, P.o_near.y, P.o_far.y, P.ilo.y, P.ihi.y, Ly, Uy);
+  axis_bounds_fixed(c.lo.z, c.hi.z, P.nz, P.o_near.z, P.o_far.z, P.ilo.z, P.ihi.z, Lz, Uz);
   const float lb = fmaxf(fmaxf(fmaxf(Lx, Ly), Lz), t_min);
   const float ub = fminf(fminf(fminf(Ux, Uy), Uz), t_max);
   tnear = lb;
   return ub >= lb;
 }
+// Warp minimum and maximum of one value from one order-preserving key;
+// inactive lanes count as +inf for the minimum and -inf for the maximum.
+__device__ __forceinline__ void wminmax(float x, bool active, float &lo, float &hi) {
+  const unsigned k = ford(x);
+  lo = funord(__reduce_min_sync(kFull, active ? k : 0xff800000u));  // ford(+inf)
+  hi = funord(__reduce_max_sync(kFull, active ? k : 0x007fffffu));  // ford(-inf)
+}
 __device__ Packet make_packet(const SceneView &S, float3 o, float3 d, float3 idir, bool active) {
-  const float inf = kInf();
   Packet P;
-  P.olo = f3(wmin(active ? o.x : inf), wmin(active ? o.y : inf), wmin(active ? o.z : inf));
-  P.ohi = f3(wmax(active ? o.x : -inf), wmax(active ? o.y : -inf), wmax(active ? o.z : -inf));
-  P.ilo = f3(wmin(active ? idir.x : inf), wmin(active ? idir.y : inf), wmin(active ? idir.z : inf));
-  P.ihi = f3(wmax(active ? idir.x : -inf), wmax(active ? idir.y : -inf), wmax(active ? idir.z : -inf));
-  const float dx = wmax(active ? d.x : -inf) - wmin(active ? d.x : inf);
-  const float dy = wmax(active ? d.y : -inf) - wmin(active ? d.y : inf);
-  const float dz = wmax(active ? d.z : -inf) - wmin(active ? d.z : inf);
+  wminmax(o.x, active, P.olo.x, P.ohi.x);
+  wminmax(o.y, active, P.olo.y, P.ohi.y);
+  wminmax(o.z, active, P.olo.z, P.ohi.z);
+  wminmax(idir.x, active, P.ilo.x, P.ihi.x);
+  wminmax(idir.y, active, P.ilo.y, P.ihi.y);
+  wminmax(idir.z, active, P.ilo.z, P.ihi.z);
+  float dlo, dhi;
+  wminmax(d.x, active, dlo, dhi);
+  const float dx = dhi - dlo;
+  wminmax(d.y, active, dlo, dhi);
+  const float dy = dhi - dlo;
+  wminmax(d.z, active, dlo, dhi);
+  const float dz = dhi - dlo;
   const float ds = fmaxf(fmaxf(dx, dy), dz);
   const float os = fmaxf(fmaxf(P.ohi.x - P.olo.x, P.ohi.y - P.olo.y), P.ohi.z - P.olo.z);
+  P.nx = P.ihi.x < 0.0f;
+  P.ny = P.ihi.y < 0.0f;
+  P.nz = P.ihi.z < 0.0f;
+  const bool one_sign = (P.nx || P.ilo.x > 0.0f) && (P.ny || P.ilo.y > 0.0f) && (P.nz || P.ilo.z > 0.0f);
   // bundles whose footprint stays within a small fraction of the scene
-  P.coherent = ds <= 0.02f && os <= S.coherent_span;
+  P.coherent = one_sign && ds <= 0.02f && os <= S.coherent_span;
+  P.o_near = f3(P.nx ? P.olo.x : P.ohi.x, P.ny ? P.olo.y : P.ohi.y, P.nz ? P.olo.z : P.ohi.z);
+  P.o_far = f3(P.nx ? P.ohi.x : P.olo.x, P.ny ? P.ohi.y : P.olo.y, P.nz ? P.ohi.z : P.olo.z);
   return P;
 }
 
@@ -348,6 +393,12 @@ __device__ __forceinline__ bool expand_node(const SceneView &S, int node, const 
   const unsigned mask = __ballot_sync(kFull, hit && lane < kBvhWidth);
   if (!mask) return false;
   const int n = __popc(mask);
+  if (n == 1) {  // the common case of a thin packet: nothing to order or push
+    const int only = __ffs(mask) - 1;
+    next = __shfl_sync(kFull, code, only);
+    next_t = __shfl_sync(kFull, key, only);
+    return true;
+  }
   int rank = 0;
   if (kSorted) {
 #pragma unroll
@@ -538,6 +589,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
   const float3 origin = f3(pose.px, pose.py, pose.pz);
   const int ss = S.samples;
   const int px_i = pixel % S.width, py_i = pixel / S.width;
+  const HapkeConst hc = hapke_const(S.hapke);
   for (int sy = 0; sy < ss; ++sy)
     for (int sx = 0; sx < ss; ++sx) {
       const float px = subray_x(S, px_i, sx);
@@ -549,7 +601,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
       const bool hitp = active && out.valid && hit.hit == 1;
       bool lit = false;
       float3 normal = f3(0, 0, 0), sorigin = f3(0, 0, 0);
-      float albedo = S.hapke.w;
+      float albedo = S.hapke.w, r0 = hc.r0_w;
       if (hitp) {
         if (kMode != kRadiance) {
           depth += hit.t;
@@ -566,7 +618,10 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
             const float4 *r = reinterpret_cast<const float4 *>(S.tris + hit.tri);
             const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
             sorigin = shadow_origin(f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, c.x), hit.u, hit.v, light);
-            if (S.has_albedo) albedo = s0.w * w + s1.w * hit.u + s2.w * hit.v;
+            if (S.has_albedo) {
+              albedo = s0.w * w + s1.w * hit.u + s2.w * hit.v;
+              r0 = hfunc_r0(albedo);
+            }
           }
         }
       }
@@ -578,7 +633,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
             const double cos4 = cos4_table ? cos4_table[sy * ss + sx] : cos4_of(px, py);
             // hapke_directional_reflectance (hapke.hpp:153-157)
             const float3 n = normalize(normal), l = normalize(light), v = normalize(-ray);
-            const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo, S.hapke);
+            const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo, r0, S.hapke, hc);
             out.radiance += fmaxf(0, n_h * pose.intensity) * cos4;
           }
         }

@@ -9,10 +9,10 @@
 // Work decomposition
 //   * trace_cells: one warp traces a packet of 32 (pixel, cell) samples --
 //     32/CW Morton-adjacent pixels x CW consecutive circuit cells.  All lanes
-//     walk the 4-wide BVH together (warp-uniform control flow, node and
-//     triangle records fetched once per warp as 16-byte broadcast loads); each
-//     lane keeps its own closest hit.  The traversal stack is warp-uniform and
-//     lives in registers distributed across the lanes.
+//     walk the 8-wide BVH together (warp-uniform control flow); coherent
+//     packets test one child per lane against the packet's ray intervals,
+//     leaves are tested per lane, and each lane keeps its own closest hit.
+//     The traversal stack is warp-uniform and lives in shared memory.
 //   * circuit: one thread per pixel streams the per-cell radiance of a chunk
 //     and integrates the pixel circuit in FP64 (pixel_model.hpp semantics).
 //   * emit_events: warp prefix-sum compaction of the per-pixel event slabs.
@@ -50,9 +50,11 @@ __global__ void cell_poses_kernel(const dvs_optical_interval *ivs, const Cell *c
 }
 
 constexpr int kWarpsPerBlock = 4;  // all ray kernels launch 128 threads
-// Resident blocks per SM the trace kernel is compiled for (caps its registers).
+// Resident blocks per SM the trace kernel is compiled for: 5 blocks of 128
+// threads cap it at 96 registers (20 warps per SM), the fastest measured
+// balance of latency hiding against register spills.
 #ifndef DVS_TRACE_MIN_BLOCKS
-#define DVS_TRACE_MIN_BLOCKS 1
+#define DVS_TRACE_MIN_BLOCKS 5
 #endif
 constexpr int kCos4Table = 256;    // sub-rays per pixel with a shared cos^4 table (ss <= 16)
 

@@ -80,7 +80,7 @@ class DeviceScene:
     """Owner of the device-resident wide BVH, triangle and shading records
     (replaces BVHBuilder::build + DeviceScene)."""
 
-    def __init__(self, vertices, normals, indices, camera, supersample, hapke=None, albedos=None, leaf_size=4):
+    def __init__(self, vertices, normals, indices, camera, supersample, hapke=None, albedos=None, leaf_size=0):
         lib = _capi.load()
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
         n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)

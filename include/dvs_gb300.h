@@ -104,7 +104,7 @@ typedef struct {
 } dvs_sensor_options;
 
 typedef struct {
-  int32_t leaf_size;          /* triangles per BVH leaf, 1..8 (default 4) */
+  int32_t leaf_size;          /* triangles per BVH leaf, 1..8 (0: 2, wider when the tree is too deep) */
   int32_t reserved[3];
 } dvs_bvh_params;
 
@@ -113,6 +113,8 @@ typedef struct {
   int32_t depth, root;
   uint64_t device_bytes;
   double build_seconds;
+  int32_t leaf_size;          /* triangles per leaf the tree was built with */
+  int32_t reserved;
 } dvs_scene_info;
 
 typedef struct {

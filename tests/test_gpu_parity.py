@@ -105,6 +105,23 @@ def test_cam_terrain_matches_oracle():
     assert (img > 0).mean() > 0.5 and (dep > 0).mean() > 0.8
 
 
+def test_leaf_size_changes_the_tree_not_the_image():
+    """Nearest hits and occlusion do not depend on how the tree is cut: the
+    default (2 triangles per leaf) and 1/8-triangle leaves render the same image
+    up to edge ties."""
+    pose = dict(position=(13.0, -7.0, 700.0), rotation=(0.0, 0.0, 0.0, 1.0),
+                light=trajectory.sun_direction(30, 40), intensity=1000)
+    images = {}
+    for leaf in (0, 1, 8):
+        V, N, I, camera, hap, scene = terrain_scene(leaf=leaf)
+        info = scene.info()
+        assert info["leaf_size"] == (leaf or 2)
+        images[leaf] = CamRayCaster(scene).render_state(pose)
+    for leaf in (1, 8):
+        for a, b in zip(images[0], images[leaf]):
+            assert float(np.mean(rel_err(a, b) > RTOL)) < 1e-3
+
+
 # ---- sensor path (tests/test_sensor.cu:66-93,160-173) ----------------------------------
 
 def plane_sensor(**over):
