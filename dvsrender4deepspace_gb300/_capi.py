@@ -93,7 +93,21 @@ EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_d
            "dvs_sensor_stream", "dvs_sensor_read_state", "dvs_cam_render_noalloc", "dvs_sensor_process_adaptive",
            "dvs_sensor_refinement_stats", "dvs_sensor_last_convergence", "dvs_sensor_adaptive_capacity",
            "dvs_readout_create", "dvs_readout_destroy", "dvs_readout_submit", "dvs_readout_drain", "dvs_readout_read",
-           "dvs_readout_counters")
+           "dvs_readout_counters", "dvs_config_load", "dvs_frames_load", "dvs_trajectory_create",
+           "dvs_trajectory_destroy", "dvs_trajectory_range", "dvs_trajectory_evaluate")
+
+
+class SceneConfig(C.Structure):
+    _fields_ = [("frame_count", C.c_int32), ("fps", C.c_float), ("imu_fps", C.c_float), ("cam_fps", C.c_float),
+                ("time_resolution", C.c_float), ("blur_resolution", C.c_float), ("supersample_factor", C.c_int32),
+                ("translation", C.c_float * 3), ("rotation", C.c_float * 3)]
+
+
+# dvs_frame (include/dvs_gb300.h): one trajectory key of frames.bin.
+FRAME_DTYPE = np.dtype({"names": ["frame_index", "timestamp_seconds", "camera_origin", "camera_world", "light_dir",
+                                  "light_intensity"],
+                        "formats": ["<i4", "<f8", ("<f4", 3), ("<f4", 9), ("<f4", 3), "<f4"],
+                        "offsets": [0, 8, 16, 28, 64, 76], "itemsize": 80})
 
 
 class RefinementStats(C.Structure):
@@ -152,6 +166,13 @@ def _declare(lib):
     lib.dvs_readout_drain.argtypes = [vp, C.POINTER(sz)]
     lib.dvs_readout_read.argtypes = [vp, vp, sz, C.POINTER(sz)]
     lib.dvs_readout_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    lib.dvs_config_load.argtypes = [C.c_char_p, C.POINTER(Camera), C.POINTER(Physic), C.POINTER(Hapke),
+                                    C.POINTER(SceneConfig)]
+    lib.dvs_frames_load.argtypes = [C.c_char_p, vp, sz, C.POINTER(sz)]
+    lib.dvs_trajectory_create.argtypes = [vp, sz, C.POINTER(SceneConfig), C.POINTER(vp)]
+    lib.dvs_trajectory_destroy.argtypes = [vp]
+    lib.dvs_trajectory_range.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    lib.dvs_trajectory_evaluate.argtypes = [vp, C.c_float, vp, f_p]
     return lib
 
 

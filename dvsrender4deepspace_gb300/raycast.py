@@ -23,7 +23,9 @@ HAPKE_DEFAULT = dict(b=0.24, c=0.305, hS=0.08, hC=1.0, thetap=26.0 * float(np.fl
 
 
 def state_array(states):
-    """Packs one or more optical-state dicts into the OpticalState layout."""
+    """Packs one or more optical-state dicts (or OpticalState records) into the OpticalState layout."""
+    if isinstance(states, (np.void, np.ndarray)) and states.dtype == STATE_DTYPE:
+        return np.atleast_1d(np.array(states, STATE_DTYPE))
     if isinstance(states, dict):
         states = [states]
     out = np.zeros(len(states), STATE_DTYPE)

@@ -255,6 +255,49 @@ void *dvs_sensor_stream(dvs_sensor *sensor);
  * and one int32 reset flag.  Either pointer may be NULL. */
 int dvs_sensor_read_state(dvs_sensor *sensor, double *state5, int32_t *reset_pending);
 
+/* ---- host inputs of bin/dvs and bin/cam ------------------------------------------
+ * The YAML config (src/scene_types.cpp:170-345), the frames.bin trajectory of a
+ * scene bundle (src/scene_data.cpp:163-193) and the continuous camera/light
+ * trajectory (src/trajectory.cpp), restated in C++ without Eigen.  Host only:
+ * these calls need no GPU. */
+typedef struct {
+  int32_t frame_count;
+  float fps, imu_fps, cam_fps, time_resolution, blur_resolution;
+  int32_t supersample_factor;
+  float translation[3], rotation[3]; /* camera mount in the trajectory frame; Euler X, Y, Z (radians) */
+} dvs_scene_config;
+
+typedef struct {
+  int32_t frame_index;
+  double timestamp_seconds;   /* NaN: the frame's time is frame_index / fps */
+  float camera_origin[3];
+  float camera_world[9];      /* row-major camera-to-world rotation */
+  float light_dir[3];
+  float light_intensity;
+} dvs_frame;
+
+typedef struct dvs_trajectory dvs_trajectory;
+
+/* Parses a config file; DVS_ERR_INVALID with the reference's message when it
+ * is missing, malformed or out of range.  Any output pointer may be NULL. */
+int dvs_config_load(const char *path, dvs_camera *camera, dvs_physic *physic, dvs_hapke *hapke,
+                    dvs_scene_config *scene);
+/* Reads <bundle_dir>/frames.bin.  *n_frames = frames in the file; copies
+ * min(capacity, n) of them; frames == NULL queries the count.
+ * DVS_ERR_OUTPUT_SMALL when capacity < n (the first capacity are copied). */
+int dvs_frames_load(const char *bundle_dir, dvs_frame *frames, size_t capacity, size_t *n_frames);
+/* CameraTrajectory(frames, scene config) (include/dvs/trajectory.hpp:88-92);
+ * DVS_ERR_INVALID for non-increasing or non-finite times, non-rigid poses,
+ * invalid lighting or mount transforms. */
+int dvs_trajectory_create(const dvs_frame *frames, size_t n_frames, const dvs_scene_config *scene,
+                          dvs_trajectory **out);
+int dvs_trajectory_destroy(dvs_trajectory *trajectory);
+int dvs_trajectory_range(const dvs_trajectory *trajectory, float *start_time, float *end_time);
+/* CameraTrajectory::evaluate(t) as an OpticalState (include/dvs/raycast.hpp:17-22);
+ * orientation9 (row-major camera-to-world) may be NULL. */
+int dvs_trajectory_evaluate(const dvs_trajectory *trajectory, float time, dvs_optical_state *state,
+                            float *orientation9);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,6 +15,7 @@
 // Failures throw what the reference throws: std::invalid_argument for bad
 // inputs, std::runtime_error for device status and CUDA errors.
 #pragma once
+#include <cmath>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -35,7 +36,7 @@ class DeviceScene {
  public:
   DeviceScene(const std::vector<float> &vertices, const std::vector<float> &normals,
               const std::vector<uint32_t> &indices, const dvs_camera &camera, int supersample,
-              const dvs_hapke &hapke, const std::vector<float> *albedos = nullptr, int leaf_size = 4) {
+              const dvs_hapke &hapke, const std::vector<float> *albedos = nullptr, int leaf_size = 0) {
     if (vertices.size() % 3 || normals.size() != vertices.size() || indices.size() % 3 ||
         (albedos && albedos->size() * 3 != vertices.size()))
       throw std::invalid_argument("invalid indexed mesh/BVH/material dimensions");
@@ -84,6 +85,36 @@ class DvsRayCaster {
     check(dvs_sensor_process(sensor_.get(), intervals.data(), intervals.size(), &n));
     read(n, events);
   }
+  // EventSensor::process_adaptive (include/dvs/raycast.hpp:40-43): false when
+  // the convergence gate rejected the window (nothing changed; retry smaller).
+  bool advance_adaptive(const std::vector<dvs_optical_interval> &intervals, double tolerance,
+                        std::vector<dvs_event> &events, bool check_convergence = false) {
+    size_t n = 0;
+    int32_t accepted = 0;
+    check(dvs_sensor_process_adaptive(sensor_.get(), intervals.data(), intervals.size(), tolerance,
+                                      check_convergence ? 1 : 0, &accepted, &n));
+    if (!accepted) {
+      events.clear();
+      return false;
+    }
+    read(n, events);
+    return true;
+  }
+  int adaptive_cache_capacity() {
+    int32_t k = 0;
+    check(dvs_sensor_adaptive_capacity(sensor_.get(), &k));
+    return k;
+  }
+  dvs_refinement_stats refinement_statistics() const {
+    dvs_refinement_stats r{};
+    check(dvs_sensor_refinement_stats(sensor_.get(), &r));
+    return r;
+  }
+  dvs_receptor_probe last_convergence() const {
+    dvs_receptor_probe r{};
+    check(dvs_sensor_last_convergence(sensor_.get(), &r));
+    return r;
+  }
   void drain(std::vector<dvs_event> &events) {
     events.clear();
     std::vector<dvs_event> chunk(1 << 16);
@@ -124,6 +155,55 @@ class CamRayCaster {
     light_frame.resize(n);
     depth_map.resize(n);
     check(dvs_cam_render(scene_->get(), &pose, light_frame.data(), depth_map.data()));
+  }
+  // The reference's call (src/cuda/cam_render.cu:16-28): camera_world is a
+  // column-major 3x3 camera-to-world rotation, turned into a unit quaternion.
+  void render_main(const dvs_float3 &origin, const float *camera_world, const dvs_float3 &light, float intensity,
+                   std::vector<float> &light_frame, std::vector<float> &depth_map) {
+    dvs_optical_state pose{};
+    pose.position = origin;
+    pose.light = light;
+    pose.intensity = intensity;
+    pose.rotation = quaternion_of(camera_world);
+    render_main(pose, light_frame, depth_map);
+  }
+
+  // Unit quaternion (x, y, z, w) of a column-major rotation matrix
+  // (Shepperd's method: branch on the largest of trace and diagonal).
+  static dvs_float4 quaternion_of(const float *m) {
+    auto R = [m](int r, int c) { return m[c * 3 + r]; };
+    float q[4];  // x, y, z, w
+    const float trace = R(0, 0) + R(1, 1) + R(2, 2);
+    if (trace > 0) {
+      float t = std::sqrt(trace + 1.0f);
+      q[3] = 0.5f * t;
+      t = 0.5f / t;
+      q[0] = (R(2, 1) - R(1, 2)) * t;
+      q[1] = (R(0, 2) - R(2, 0)) * t;
+      q[2] = (R(1, 0) - R(0, 1)) * t;
+    } else {
+      int i = 0;
+      if (R(1, 1) > R(0, 0)) i = 1;
+      if (R(2, 2) > R(i, i)) i = 2;
+      const int j = (i + 1) % 3, k = (j + 1) % 3;
+      float t = std::sqrt(R(i, i) - R(j, j) - R(k, k) + 1.0f);
+      q[i] = 0.5f * t;
+      t = 0.5f / t;
+      q[3] = (R(k, j) - R(j, k)) * t;
+      q[j] = (R(j, i) + R(i, j)) * t;
+      q[k] = (R(k, i) + R(i, k)) * t;
+    }
+    const float n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    if (n2 > 0) {
+      const float n = std::sqrt(n2);
+      for (float &v : q) v /= n;
+    }
+    dvs_float4 out{};
+    out.x = q[0];
+    out.y = q[1];
+    out.z = q[2];
+    out.w = q[3];
+    return out;
   }
 
  private:
