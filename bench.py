@@ -287,7 +287,11 @@ def run_gb300(args):
                    w["sun_elevation"], "intensity": w["intensity"], "l2": "inputs larger than L2 (scene %.1f GB)"
                    % (info["device_bytes"] / 1e9), "parallelism": "dp%d (independent jobs)" % world,
                    "bvh": "8-wide Morton radix, leaf %d, depth %d" % (info["leaf_size"], info["depth"])},
-        "rays_per_step": rays / args.steps, "events_per_s": delivered_all / e2e_s,
+        "rays_per_step": rays / args.steps,
+        "rays": {"primary_per_step": st["primary_rays"] / args.steps, "shadow_per_step": st["shadow_rays"] / args.steps,
+                 "primary_mrays_s": st["primary_rays"] / (dev_ms / 1e3) / 1e6 if world == 1 else None,
+                 "shadow_mrays_s": st["shadow_rays"] / (dev_ms / 1e3) / 1e6 if world == 1 else None},
+        "events_per_s": delivered_all / e2e_s,
         "events_generated_per_step": gen2 / args.steps,
         "e2e": {"value": e2e_value, "unit": "Mrays/s",
                 "h2d_bytes_per_step": B * 176, "d2h_bytes_per_step": int(events_total * 24 / args.steps)},
@@ -312,20 +316,97 @@ def run_gb300(args):
     return 0
 
 
+SERVING_GRIDS = (512, 768, 1024, 1536, 2048, 2560, 3072, 4096)
+
+
+def run_serving(args):
+    """Serving workload: a seeded Poisson stream (200 req/s) of render+DVS
+    jobs -- resolutions uniform over 64x48 / 346x260 / 640x480 / 1280x720,
+    durations log-uniform, terrains uniform over a pool of 8 heightfields of
+    512^2 ... 4096^2 vertices -- admitted under a 150 GB HBM budget by the
+    continuous-batching server, against the plain path (the same jobs one at
+    a time, first come first served).  Durations are the stream's 0.05-2 s
+    scaled by --serving-scale (default 0.01: 0.5-20 ms of simulated time per
+    job, 1 us circuit cells) so that the stream completes in about a minute."""
+    import torch
+    from dvsrender4deepspace_gb300 import DeviceScene, serve, terrain
+    from dvsrender4deepspace_gb300.build import build
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    build()
+    t_setup = time.time()
+    scenes = []
+    for k, g in enumerate(SERVING_GRIDS):
+        V, N, I = terrain.terrain_mesh(g, 20260100 + k)
+        scenes.append(DeviceScene(V, N, I, dict(width=8, height=8, fx=8.0, fy=8.0, cx=4.0, cy=4.0), 1, HAPKE))
+    setup_s = time.time() - t_setup
+    phys = dict(PHYSIC)
+
+    def stream():
+        return serve.synthetic_stream(args.serving_jobs, 20260104, len(scenes), rate_hz=200.0,
+                                      duration_scale=args.serving_scale, physic=phys, intensity=1000.0)
+
+    # warm-up: one small job per terrain through the server (first-use allocations, module load)
+    warm = [j for j in stream() if j.camera["width"] == 64][:2]
+    serve.Server(scenes, 150 << 30).run(warm, realtime=False)
+    results = {}
+    for mode, max_active in (("served", 64), ("plain", 1)):
+        jobs = stream()
+        srv = serve.Server(scenes, 150 << 30, horizons_per_step=64, max_active=max_active)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with ClockSampler(local) as clocks:
+            done = srv.run(jobs, realtime=True)
+            torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        events = sum(len(j.events) for j in done)
+        rays = sum(j.rays for j in done)
+        res = serve.latency_summary(done)
+        res.update({"jobs": len(done), "makespan_s": wall, "events": events, "events_per_s": events / wall,
+                    "mrays_per_s": rays / wall / 1e6, "peak_active": srv.peak_active,
+                    "peak_device_gb": srv.peak_used / 1e9, "scheduler_steps": srv.steps,
+                    "clocks": clocks.summary()})
+        results[mode] = res
+    line = {"metric": METRIC, "value": results["served"]["p99_ms"], "unit": "ms (p99 request latency)",
+            "n_gpus": 1, "steps": args.serving_jobs, "warmup": len(warm), "ms_per_step": None,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": "serving", "jobs": args.serving_jobs, "rate_hz": 200.0,
+                       "resolutions": ["64x48", "346x260", "640x480", "1280x720"],
+                       "durations_s": [0.05 * args.serving_scale, 2.0 * args.serving_scale],
+                       "terrain_grids": list(SERVING_GRIDS), "hbm_budget_gb": 150, "supersample": 1,
+                       "time_resolution": 1e-5, "circuit_step": PHYSIC["circuit_step"]},
+            "served": results["served"], "plain": results["plain"],
+            "p99_speedup_vs_plain": results["plain"]["p99_ms"] / results["served"]["p99_ms"],
+            "throughput_vs_plain": results["served"]["events_per_s"] / max(1e-9, results["plain"]["events_per_s"]),
+            "setup_s": setup_s}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="precision", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="precision", choices=sorted(WORKLOADS) + ["serving"])
+    ap.add_argument("--serving-jobs", type=int, default=48)
+    ap.add_argument("--serving-scale", type=float, default=0.01)
     ap.add_argument("--leaf", type=int, default=0)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--cw", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
+        if args.workload == "serving":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving layer"}))
+            return 0
         return run_reference(args)
+    if args.workload == "serving":
+        return run_serving(args)
     return run_gb300(args)
 
 

@@ -94,7 +94,8 @@ EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_d
            "dvs_sensor_refinement_stats", "dvs_sensor_last_convergence", "dvs_sensor_adaptive_capacity",
            "dvs_readout_create", "dvs_readout_destroy", "dvs_readout_submit", "dvs_readout_drain", "dvs_readout_read",
            "dvs_readout_counters", "dvs_config_load", "dvs_frames_load", "dvs_trajectory_create",
-           "dvs_trajectory_destroy", "dvs_trajectory_range", "dvs_trajectory_evaluate")
+           "dvs_trajectory_destroy", "dvs_trajectory_range", "dvs_trajectory_evaluate", "dvs_cam_render_blur",
+           "dvs_scene_view_create", "dvs_sensor_device_bytes")
 
 
 class SceneConfig(C.Structure):
@@ -155,6 +156,9 @@ def _declare(lib):
     lib.dvs_sensor_stream.restype = vp
     lib.dvs_sensor_read_state.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
     lib.dvs_cam_render_noalloc.argtypes = [vp, vp, vp, vp, vp]
+    lib.dvs_cam_render_blur.argtypes = [vp, vp, f_p, sz, f_p]
+    lib.dvs_scene_view_create.argtypes = [vp, C.POINTER(Camera), C.c_int32, C.POINTER(Hapke), C.POINTER(vp)]
+    lib.dvs_sensor_device_bytes.argtypes = [vp, C.POINTER(C.c_uint64)]
     lib.dvs_sensor_process_adaptive.argtypes = [vp, vp, sz, C.c_double, C.c_int32, C.POINTER(C.c_int32),
                                                 C.POINTER(sz)]
     lib.dvs_sensor_refinement_stats.argtypes = [vp, C.POINTER(RefinementStats)]

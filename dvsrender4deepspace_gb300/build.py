@@ -18,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 APPS = os.path.join(PKG, "apps")
 BIN = os.path.join(ROOT, "bin")
-APP_MAINS = {"dvs": "main_dvs.cpp", "cam": "main_cam.cpp"}
+APP_MAINS = {"dvs": "main_dvs.cpp", "cam": "main_cam.cpp", "cam_blur": "main_cam_blur.cpp"}
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libdvs_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

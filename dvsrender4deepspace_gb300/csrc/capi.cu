@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -125,7 +126,9 @@ struct dvs_scene {
   int samples = 1;
   dvs_hapke hapke{};
   bool has_albedo = false;
-  void *arena = nullptr;
+  // geometry arena (nodes, triangle and shading records), shared by the
+  // scene views created from this scene; freed with the last of them
+  std::shared_ptr<void> geometry;
   size_t arena_bytes = 0;
   BvhNode *nodes = nullptr;
   TriRecord *tris = nullptr;
@@ -143,6 +146,12 @@ struct dvs_scene {
   CellPose *cam_pose = nullptr;
   dvs_optical_state *cam_state = nullptr;
   dvs_optical_state *h_state = nullptr;
+  // motion-blur exposures: poses, weights and per-pose radiance, grown on demand
+  size_t blur_cap = 0;
+  dvs_optical_state *blur_states = nullptr, *h_blur_states = nullptr;
+  float *blur_weights = nullptr, *h_blur_weights = nullptr;
+  CellPose *blur_poses = nullptr;
+  double *blur_radiance = nullptr;
 
   SceneView view() const {
     SceneView v;
@@ -357,19 +366,22 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   const size_t off_nodes = 0;
   const size_t off_tris = align_up(off_nodes + sizeof(BvhNode) * s->n_nodes, 256);
   const size_t off_shade = align_up(off_tris + sizeof(TriRecord) * n_triangles, 256);
-  const size_t off_pix = align_up(off_shade + sizeof(ShadeRecord) * n_triangles, 256);
-  const size_t total = align_up(off_pix + sizeof(int32_t) * order.size(), 256);
-  cudaError_t e = cudaMalloc(&s->arena, total);
+  const size_t total = align_up(off_shade + sizeof(ShadeRecord) * n_triangles, 256);
+  void *arena = nullptr;
+  cudaError_t e = cudaMalloc(&arena, total);
+  if (e == cudaSuccess) {
+    s->geometry = std::shared_ptr<void>(arena, [](void *p) { cudaFree(p); });
+    e = cudaMalloc(&s->pixel_of_rank, sizeof(int32_t) * order.size());
+  }
   if (e != cudaSuccess) {
-    delete s;
+    dvs_scene_destroy(s);
     return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in allocate scene arena : ") + cudaGetErrorString(e));
   }
-  s->arena_bytes = total;
-  char *base = static_cast<char *>(s->arena);
+  s->arena_bytes = total + sizeof(int32_t) * order.size();
+  char *base = static_cast<char *>(arena);
   s->nodes = reinterpret_cast<BvhNode *>(base + off_nodes);
   s->tris = reinterpret_cast<TriRecord *>(base + off_tris);
   s->shade = reinterpret_cast<ShadeRecord *>(base + off_shade);
-  s->pixel_of_rank = reinterpret_cast<int32_t *>(base + off_pix);
   s->rank_of_pixel.assign(order.size(), 0);
   for (size_t r = 0; r < order.size(); ++r) s->rank_of_pixel[order[r]] = (int32_t)r;
   e = cudaMemcpy(s->nodes, bvh.nodes.data(), sizeof(BvhNode) * s->n_nodes, cudaMemcpyHostToDevice);
@@ -398,9 +410,62 @@ int dvs_scene_destroy(dvs_scene *s) {
   cudaFree(s->cam_pose);
   cudaFree(s->cam_state);
   if (s->h_state) cudaFreeHost(s->h_state);
+  cudaFree(s->blur_states);
+  cudaFree(s->blur_weights);
+  cudaFree(s->blur_poses);
+  cudaFree(s->blur_radiance);
+  if (s->h_blur_states) cudaFreeHost(s->h_blur_states);
+  if (s->h_blur_weights) cudaFreeHost(s->h_blur_weights);
   if (s->stream) cudaStreamDestroy(s->stream);
-  cudaFree(s->arena);
+  cudaFree(s->pixel_of_rank);
+  s->geometry.reset();
   delete s;
+  return DVS_OK;
+}
+
+int dvs_scene_view_create(const dvs_scene *base, const dvs_camera *camera, int32_t supersample,
+                          const dvs_hapke *hapke, dvs_scene **out) {
+  // a camera over an existing scene's geometry: one device copy of a
+  // terrain's BVH serves every job that renders it
+  if (!out) return fail(DVS_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (!base || !camera || !hapke) return fail(DVS_ERR_INVALID, "invalid indexed mesh/BVH/material dimensions");
+  if (camera->width <= 0 || camera->height <= 0 || camera->width > 32767 || camera->height > 32767 ||
+      !(camera->fx > 0) || !(camera->fy > 0) || !std::isfinite(camera->cx) || !std::isfinite(camera->cy))
+    return fail(DVS_ERR_INVALID, "invalid scene or camera range");
+  if (supersample < 1 || supersample > 64 ||
+      double(camera->width) * camera->height * supersample * supersample > std::numeric_limits<int>::max())
+    return fail(DVS_ERR_INVALID, "too many aperture samples");
+  CUDA_TRY(cudaSetDevice(base->device), "select device");
+  const std::vector<int32_t> order = morton_pixel_order(camera->width, camera->height);
+  dvs_scene *s = new dvs_scene;
+  s->device = base->device;
+  s->camera = *camera;
+  s->samples = supersample;
+  s->hapke = *hapke;
+  s->has_albedo = base->has_albedo;
+  s->geometry = base->geometry;
+  s->nodes = base->nodes;
+  s->tris = base->tris;
+  s->shade = base->shade;
+  s->n_nodes = base->n_nodes;
+  s->n_tris = base->n_tris;
+  s->n_vertices = base->n_vertices;
+  s->depth = base->depth;
+  s->leaf_size = base->leaf_size;
+  s->coherent_span = base->coherent_span;
+  s->rank_of_pixel.assign(order.size(), 0);
+  for (size_t r = 0; r < order.size(); ++r) s->rank_of_pixel[order[r]] = (int32_t)r;
+  cudaError_t e = cudaMalloc(&s->pixel_of_rank, sizeof(int32_t) * order.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(s->pixel_of_rank, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    dvs_scene_destroy(s);
+    return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in upload scene array : ") + cudaGetErrorString(e));
+  }
+  s->arena_bytes = sizeof(int32_t) * order.size();  // its own allocations; the geometry is the base's
+  *out = s;
   return DVS_OK;
 }
 
@@ -448,6 +513,63 @@ int dvs_cam_render(dvs_scene *s, const dvs_optical_state *pose, float *radiance,
   CUDA_TRY(cudaStreamSynchronize(s->stream), "parallel optical status");
   for (int i = 0; i < n; ++i)
     if (!std::isfinite(radiance[i])) return fail(DVS_ERR_OPTICAL, "invalid optical sample/BVH stack overflow");
+  return DVS_OK;
+}
+
+int dvs_cam_render_blur(dvs_scene *s, const dvs_optical_state *poses, const float *weights, size_t n_poses,
+                        float *image) {
+  // main_cam_blur.cpp:64-77 with all sub-exposure poses in one multi-pose
+  // launch (the pose_count form of optical_sampler.cu:154-168)
+  if (!s || !poses || !weights || !image || n_poses == 0 || n_poses > (1u << 20))
+    return fail(DVS_ERR_INVALID, "invalid parallel optical request");
+  for (size_t j = 0; j < n_poses; ++j)
+    if (!std::isfinite(weights[j])) return fail(DVS_ERR_INVALID, "invalid exposure weight");
+  CUDA_TRY(cudaSetDevice(s->device), "select device");
+  const int n = s->pixels();
+  if (n_poses > s->blur_cap) {
+    cudaStreamSynchronize(s->stream);
+    cudaFree(s->blur_states);
+    cudaFree(s->blur_weights);
+    cudaFree(s->blur_poses);
+    cudaFree(s->blur_radiance);
+    if (s->h_blur_states) cudaFreeHost(s->h_blur_states);
+    if (s->h_blur_weights) cudaFreeHost(s->h_blur_weights);
+    s->blur_states = s->h_blur_states = nullptr;
+    s->blur_weights = s->h_blur_weights = nullptr;
+    s->blur_poses = nullptr;
+    s->blur_radiance = nullptr;
+    s->blur_cap = 0;
+    CUDA_TRY(cudaMalloc(&s->blur_states, sizeof(dvs_optical_state) * n_poses), "allocate exposure poses");
+    CUDA_TRY(cudaMalloc(&s->blur_weights, sizeof(float) * n_poses), "allocate exposure weights");
+    CUDA_TRY(cudaMalloc(&s->blur_poses, sizeof(CellPose) * n_poses), "allocate exposure poses");
+    CUDA_TRY(cudaMalloc(&s->blur_radiance, sizeof(double) * n_poses * (size_t)n), "allocate exposure radiance");
+    CUDA_TRY(cudaMallocHost(&s->h_blur_states, sizeof(dvs_optical_state) * n_poses), "allocate pose staging");
+    CUDA_TRY(cudaMallocHost(&s->h_blur_weights, sizeof(float) * n_poses), "allocate weight staging");
+    s->blur_cap = n_poses;
+  }
+  if (!s->cam_image) CUDA_TRY(cudaMalloc(&s->cam_image, sizeof(float) * n), "allocate image");
+  std::memcpy(s->h_blur_states, poses, sizeof(dvs_optical_state) * n_poses);
+  std::memcpy(s->h_blur_weights, weights, sizeof(float) * n_poses);
+  CUDA_TRY(cudaMemcpyAsync(s->blur_states, s->h_blur_states, sizeof(dvs_optical_state) * n_poses,
+                           cudaMemcpyHostToDevice, s->stream),
+           "upload optical poses");
+  CUDA_TRY(cudaMemcpyAsync(s->blur_weights, s->h_blur_weights, sizeof(float) * n_poses, cudaMemcpyHostToDevice,
+                           s->stream),
+           "upload exposure weights");
+  CUDA_TRY(launch_poses_from_states(s->blur_states, (int)n_poses, s->blur_poses, s->stream), "pose");
+  int cw_log2 = 0;
+  while (cw_log2 < 5 && (size_t(2) << cw_log2) <= n_poses) ++cw_log2;  // poses sharing a warp packet
+  CUDA_TRY(launch_trace_cells(s->view(), n, s->blur_poses, 0, (int)n_poses, cw_log2, s->blur_radiance, nullptr,
+                              nullptr, s->stream),
+           "parallel optical launch");
+  CUDA_TRY(launch_blur_accumulate(n, (int)n_poses, s->pixel_of_rank, s->blur_radiance, s->blur_weights,
+                                  s->cam_image, s->stream),
+           "exposure accumulation");
+  CUDA_TRY(cudaMemcpyAsync(image, s->cam_image, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream),
+           "download optical values");
+  CUDA_TRY(cudaStreamSynchronize(s->stream), "parallel optical status");
+  for (int i = 0; i < n; ++i)
+    if (!std::isfinite(image[i])) return fail(DVS_ERR_OPTICAL, "invalid optical sample/BVH stack overflow");
   return DVS_OK;
 }
 
@@ -1082,6 +1204,21 @@ int dvs_sensor_drain(dvs_sensor *s, dvs_event *out, size_t capacity, size_t *n_o
   if (!s || !n_out) return fail(DVS_ERR_INVALID, "null argument");
   s->readout->drain(s->ready);
   return dvs_sensor_read(s, out, capacity, n_out);
+}
+
+int dvs_sensor_device_bytes(const dvs_sensor *s, uint64_t *bytes) {
+  if (!s || !bytes) return fail(DVS_ERR_INVALID, "null argument");
+  const uint64_t n = (uint64_t)s->pixels(), ev = (uint64_t)s->max_events;
+  uint64_t b = n * (5 * sizeof(double) + sizeof(int8_t) + sizeof(curandStateXORWOW_t) + sizeof(int32_t));
+  b += n * ev * (sizeof(double) + sizeof(int8_t) + sizeof(DevEvent));
+  b += s->radiance_cap * sizeof(double) + s->ivs_cap * sizeof(dvs_optical_interval) + s->cells_cap * sizeof(Cell) +
+       s->poses_cap * sizeof(CellPose);
+  if (s->own_order) b += n * sizeof(int32_t);
+  if (s->knots) b += n * (uint64_t)s->knot_capacity * sizeof(OpticalKnot) + 3 * n * sizeof(int32_t);
+  if (s->exact_cells) b += n * (uint64_t)s->knot_capacity * (2 * sizeof(int32_t) + sizeof(double));
+  if (s->probe_state) b += (uint64_t)s->n_probes * (sizeof(int32_t) + 2 * sizeof(double));
+  *bytes = b;
+  return DVS_OK;
 }
 
 int dvs_sensor_stats_get(const dvs_sensor *s, dvs_sensor_stats *out) {

@@ -42,6 +42,19 @@ __global__ void pose_from_state_kernel(const dvs_optical_state *state, CellPose 
   *out = o;
 }
 
+__global__ void poses_from_states_kernel(const dvs_optical_state *states, int n, CellPose *out) {
+  // pose_from_state_kernel for n states: pose as given, light normalized
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const dvs_optical_state s = states[i];
+  const float3 ln = normalize(ld3(s.light));
+  CellPose o;
+  o.px = s.position.x; o.py = s.position.y; o.pz = s.position.z; o.intensity = s.intensity;
+  o.qx = s.rotation.x; o.qy = s.rotation.y; o.qz = s.rotation.z; o.qw = s.rotation.w;
+  o.lx = ln.x; o.ly = ln.y; o.lz = ln.z; o.pad = 0;
+  out[i] = o;
+}
+
 __global__ void cell_poses_kernel(const dvs_optical_interval *ivs, const Cell *cells, int n, CellPose *out) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
@@ -252,6 +265,17 @@ __global__ void radiance_to_float_kernel(int n, const int32_t *pixel_of_rank, co
   if (depth_image) depth_image[pixel] = depth[k];
 }
 
+// Time-weighted exposure of a motion-blur frame (apps/main_cam_blur.cpp:66-73):
+// per pixel, in pose order, acc += float(radiance of pose j) * weight[j].
+__global__ void blur_accumulate_kernel(int n, int n_poses, const int32_t *pixel_of_rank, const double *radiance,
+                                       const float *weights, float *image) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  float acc = 0.0f;
+  for (int j = 0; j < n_poses; ++j) acc = acc + (float)radiance[(size_t)j * n + k] * __ldg(weights + j);
+  image[pixel_of_rank[k]] = acc;
+}
+
 inline int blocks(long long threads, int per_block) { return (int)((threads + per_block - 1) / per_block); }
 
 }  // namespace
@@ -259,6 +283,18 @@ inline int blocks(long long threads, int per_block) { return (int)((threads + pe
 // ---- launchers ----------------------------------------------------------------------
 cudaError_t launch_pose_from_state(const dvs_optical_state *state, CellPose *out, cudaStream_t s) {
   pose_from_state_kernel<<<1, 32, 0, s>>>(state, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_poses_from_states(const dvs_optical_state *states, int n, CellPose *out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  poses_from_states_kernel<<<blocks(n, 128), 128, 0, s>>>(states, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_blur_accumulate(int n, int n_poses, const int32_t *pixel_of_rank, const double *radiance,
+                                   const float *weights, float *image, cudaStream_t s) {
+  blur_accumulate_kernel<<<blocks(n, 128), 128, 0, s>>>(n, n_poses, pixel_of_rank, radiance, weights, image);
   return cudaGetLastError();
 }
 

@@ -76,6 +76,10 @@ enum : int { kRefTraced = 0, kRefFallback = 1, kRefMaxKnots = 2, kRefExactSegmen
 
 // ---- launchers (return cudaGetLastError()) ----------------------------------
 cudaError_t launch_pose_from_state(const dvs_optical_state *state, CellPose *out, cudaStream_t s);
+cudaError_t launch_poses_from_states(const dvs_optical_state *states, int n, CellPose *out, cudaStream_t s);
+// Motion-blur exposure: image[pixel] = sum_j float(radiance[j][rank]) * weights[j], in pose order.
+cudaError_t launch_blur_accumulate(int n_pix, int n_poses, const int32_t *pixel_of_rank, const double *radiance,
+                                   const float *weights, float *image, cudaStream_t s);
 cudaError_t launch_cell_poses(const dvs_optical_interval *ivs, const Cell *cells, int n_cells, CellPose *out,
                               cudaStream_t s);
 // Radiance (and optionally depth) of every pixel at every cell in [c0, c0+nc).

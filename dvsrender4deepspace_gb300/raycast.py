@@ -24,8 +24,9 @@ HAPKE_DEFAULT = dict(b=0.24, c=0.305, hS=0.08, hC=1.0, thetap=26.0 * float(np.fl
 
 def state_array(states):
     """Packs one or more optical-state dicts (or OpticalState records) into the OpticalState layout."""
-    if isinstance(states, (np.void, np.ndarray)) and states.dtype == STATE_DTYPE:
-        return np.atleast_1d(np.array(states, STATE_DTYPE))
+    if isinstance(states, (np.void, np.ndarray)) and states.dtype.names == STATE_DTYPE.names:
+        # same fields, possibly without the padding (np.concatenate drops it)
+        return np.atleast_1d(np.asarray(states).astype(STATE_DTYPE))
     if isinstance(states, dict):
         states = [states]
     out = np.zeros(len(states), STATE_DTYPE)
@@ -40,8 +41,9 @@ def state_array(states):
 
 def interval_array(intervals):
     """[(start_state, end_state, t0, t1), ...] -> OpticalInterval layout."""
-    if isinstance(intervals, np.ndarray) and intervals.dtype == INTERVAL_DTYPE:
-        return np.ascontiguousarray(intervals)
+    if isinstance(intervals, np.ndarray) and intervals.dtype.names == INTERVAL_DTYPE.names:
+        # same fields, possibly without the padding (np.concatenate drops it)
+        return np.ascontiguousarray(intervals.astype(INTERVAL_DTYPE))
     out = np.zeros(len(intervals), INTERVAL_DTYPE)
     for i, (a, b, t0, t1) in enumerate(intervals):
         out[i]["start"] = state_array(a)[0]
@@ -102,6 +104,21 @@ class DeviceScene:
         self.handle = h
         self.width = int(camera["width"])
         self.height = int(camera["height"])
+
+    def view(self, camera, supersample, hapke=None):
+        """A scene with its own camera over this scene's device geometry
+        (dvs_scene_view_create): no BVH rebuild, no second copy."""
+        v = DeviceScene.__new__(DeviceScene)
+        v.camera = dict(camera)
+        v.samples = int(supersample)
+        v.hapke = dict(hapke or self.hapke)
+        h = C.c_void_p()
+        check(_capi.load().dvs_scene_view_create(self.handle, C.byref(camera_struct(camera)), v.samples,
+                                                 C.byref(hapke_struct(v.hapke)), C.byref(h)))
+        v.handle = h
+        v.width = int(camera["width"])
+        v.height = int(camera["height"])
+        return v
 
     @property
     def pixels(self):
@@ -222,6 +239,11 @@ class EventSensor:
 
     def reset_stats(self):
         check(_capi.load().dvs_sensor_stats_reset(self.handle))
+
+    def device_bytes(self):
+        out = C.c_uint64()
+        check(_capi.load().dvs_sensor_device_bytes(self.handle, C.byref(out)))
+        return out.value
 
     def dropped(self):
         return self.stats()["dropped"]
@@ -359,6 +381,21 @@ class CamRayCaster:
         check(_capi.load().dvs_cam_render(self.scene.handle, st.ctypes.data, img.ctypes.data_as(fp),
                                           dep.ctypes.data_as(fp)))
         return img, dep
+
+    def render_blur(self, states, weights):
+        """Motion-blur exposure: sum_j weights[j] * image(states[j]) in float, pose order."""
+        # an explicit 80-byte record array: np.concatenate would drop the
+        # trailing padding of STATE_DTYPE and the C side would misread records
+        st = np.zeros(len(states), STATE_DTYPE)
+        for i, s in enumerate(states):
+            st[i] = state_array(s)[0]
+        w = np.ascontiguousarray(weights, np.float32)
+        assert len(w) == len(st)
+        img = np.zeros(self.scene.pixels, np.float32)
+        fp = C.POINTER(C.c_float)
+        check(_capi.load().dvs_cam_render_blur(self.scene.handle, st.ctypes.data, w.ctypes.data_as(fp), len(st),
+                                               img.ctypes.data_as(fp)))
+        return img
 
     def render_main(self, camera_origin, camera_world, light_dir, light_intensity):
         """camera_world: 3x3 rotation (row-major here); light_dir: world light direction."""

@@ -162,6 +162,14 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
                      const dvs_camera *camera, int32_t supersample, const dvs_hapke *hapke,
                      const dvs_bvh_params *params, dvs_scene **out);
 int dvs_scene_destroy(dvs_scene *scene);
+/* A scene with its own camera, supersampling, Hapke parameters and stream over
+ * the geometry (BVH, triangle and shading records) of an existing scene: no
+ * rebuild and no second device copy.  The geometry lives until the last scene
+ * using it is destroyed, so base and views may be destroyed in any order.
+ * Vertex albedos keep the base scene's fallback (its hapke.w).  No
+ * counterpart in the reference (one DeviceScene per camera there). */
+int dvs_scene_view_create(const dvs_scene *base, const dvs_camera *camera, int32_t supersample,
+                          const dvs_hapke *hapke, dvs_scene **out);
 int dvs_scene_info_get(const dvs_scene *scene, dvs_scene_info *out);
 
 /* ---- camera image: replaces CamRayCaster::render_main / OpticalSampler::evaluate
@@ -184,6 +192,12 @@ int dvs_cam_render(dvs_scene *scene, const dvs_optical_state *pose, float *radia
  * The first call on a device looks up that array's device address (once per
  * device), so make that first call before any stream capture.  All calls
  * share the array: calls that overlap on the GPU race on it. */
+/* Motion-blur exposure (apps/main_cam_blur.cpp:64-77): the image
+ * sum_j weights[j] * radiance(poses[j]), accumulated in float in pose order,
+ * row-major, n_poses sub-exposure poses traced in one launch (the pose_count
+ * form of OpticalSampler::evaluate, src/cuda/optical_sampler.cu:154-168). */
+int dvs_cam_render_blur(dvs_scene *scene, const dvs_optical_state *poses, const float *weights, size_t n_poses,
+                        float *image);
 int dvs_cam_render_noalloc(dvs_scene *scene, const dvs_optical_state *pose, float *radiance, float *depth,
                            void *stream);
 
@@ -248,6 +262,9 @@ int dvs_readout_drain(dvs_readout *readout, size_t *n_ready);
 int dvs_readout_read(dvs_readout *readout, dvs_event *out, size_t capacity, size_t *n_out);
 int dvs_readout_counters(const dvs_readout *readout, uint64_t *dropped, uint64_t *peak_queue);
 
+/* Device memory the sensor holds now (state, RNG, event slabs, radiance
+ * chunk, batch buffers, adaptive caches), for admission by a memory budget. */
+int dvs_sensor_device_bytes(const dvs_sensor *sensor, uint64_t *bytes);
 /* The CUDA stream (cudaStream_t) the handle launches on, for external timing. */
 void *dvs_sensor_stream(dvs_sensor *sensor);
 /* Per-pixel circuit state in row-major order of the sensor's rows: 5 doubles per pixel

@@ -156,6 +156,14 @@ class CamRayCaster {
     depth_map.resize(n);
     check(dvs_cam_render(scene_->get(), &pose, light_frame.data(), depth_map.data()));
   }
+  // Motion-blur exposure: all sub-exposure poses in one launch, accumulated
+  // with the given weights in pose order (apps/main_cam_blur.cpp:64-77).
+  void render_blur(const std::vector<dvs_optical_state> &poses, const std::vector<float> &weights,
+                   std::vector<float> &image) {
+    if (poses.size() != weights.size()) throw std::invalid_argument("one exposure weight per pose");
+    image.resize(size_t(scene_->camera().width) * scene_->camera().height);
+    check(dvs_cam_render_blur(scene_->get(), poses.data(), weights.data(), poses.size(), image.data()));
+  }
   // The reference's call (src/cuda/cam_render.cu:16-28): camera_world is a
   // column-major 3x3 camera-to-world rotation, turned into a unit quaternion.
   void render_main(const dvs_float3 &origin, const float *camera_world, const dvs_float3 &light, float intensity,

@@ -105,6 +105,15 @@ def test_dvs_app_adaptive_hdf5(bundle, tmp_path):
     assert (h5["x"] >= 0).all() and (h5["x"] < CAMERA["width"]).all() and set(np.unique(h5["p"])) <= {0, 1}
 
 
+def test_cam_blur_app(bundle, tmp_path):
+    out = run_app("cam_blur", bundle, tmp_path)
+    assert "Wrote 2 images" in out
+    names = sorted(os.listdir(tmp_path / "blur_images"))
+    assert names == ["0.000000.png", "0.010000.png"]
+    img = read_png(tmp_path / "blur_images" / names[1])
+    assert img.shape == (CAMERA["height"], CAMERA["width"]) and img.max() > 0
+
+
 def test_cam_app_matches_direct_render(bundle, tmp_path):
     out = run_app("cam", bundle, tmp_path)
     n = math.ceil(0.02 * SCENE["cam_fps"])

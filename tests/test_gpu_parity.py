@@ -122,6 +122,28 @@ def test_leaf_size_changes_the_tree_not_the_image():
             assert float(np.mean(rel_err(a, b) > RTOL)) < 1e-3
 
 
+def test_motion_blur_exposure_is_the_weighted_sum_of_renders():
+    """dvs_cam_render_blur (all poses in one launch) equals the float
+    accumulation, in pose order, of one render per pose
+    (apps/main_cam_blur.cpp:66-73)."""
+    V, N, I, camera, hap, scene = terrain_scene()
+    cam = CamRayCaster(scene)
+    light = trajectory.sun_direction(30, 40)
+    for n_poses in (1, 5, 40):
+        poses = [dict(position=(13.0 + 0.5 * j, -7.0 + 0.1 * j, 700.0 - j), rotation=(0.0, 0.0, 0.0, 1.0),
+                      light=light, intensity=1000) for j in range(n_poses)]
+        w = np.full(n_poses, 1.0 / n_poses, np.float32)
+        w[-1] = np.float32(1.0) - np.float32(w[:-1].sum()) if n_poses > 1 else 1.0
+        acc = np.zeros(scene.pixels, np.float32)
+        for p, wj in zip(poses, w):
+            acc = acc + cam.render_state(p)[0] * np.float32(wj)
+        got = cam.render_blur(poses, w)
+        assert got.dtype == np.float32 and float(np.mean(got != acc)) < 1e-3, n_poses
+        assert float(np.mean(rel_err(got, acc) > RTOL)) < 1e-3
+    with pytest.raises(ValueError):
+        cam.render_blur([poses[0]], np.array([np.nan], np.float32))
+
+
 # ---- sensor path (tests/test_sensor.cu:66-93,160-173) ----------------------------------
 
 def plane_sensor(**over):
