@@ -196,7 +196,8 @@ def run_gb300(args):
     t_setup = time.time()
     scene = DeviceScene(V, N, I, w["camera"], w["ss"], HAPKE, leaf_size=args.leaf)
     info = scene.info()
-    sensor = EventSensor(scene, PHYSIC, timing=True, cells_per_chunk=args.chunk, cells_per_warp=args.cw)
+    sensor = EventSensor(scene, PHYSIC, timing=True, cells_per_chunk=args.chunk, cells_per_warp=args.cw,
+                         circuit_precision=args.circuit)
     sensor.initialize(traj.state(0.0), 0.0)
     setup_s = time.time() - t_setup
     dt, B = w["time_resolution"], w["batch"]
@@ -286,7 +287,8 @@ def run_gb300(args):
                    "circuit_step": PHYSIC["circuit_step"], "shot_noise": "curand_xorwow", "sun_elevation_deg":
                    w["sun_elevation"], "intensity": w["intensity"], "l2": "inputs larger than L2 (scene %.1f GB)"
                    % (info["device_bytes"] / 1e9), "parallelism": "dp%d (independent jobs)" % world,
-                   "bvh": "8-wide Morton radix, leaf %d, depth %d" % (info["leaf_size"], info["depth"])},
+                   "bvh": "8-wide Morton radix, leaf %d, depth %d" % (info["leaf_size"], info["depth"]),
+                   "circuit_precision": args.circuit},
         "rays_per_step": rays / args.steps,
         "rays": {"primary_per_step": st["primary_rays"] / args.steps, "shadow_per_step": st["shadow_rays"] / args.steps,
                  "primary_mrays_s": st["primary_rays"] / (dev_ms / 1e3) / 1e6 if world == 1 else None,
@@ -352,9 +354,9 @@ def run_serving(args):
     warm = [j for j in stream() if j.camera["width"] == 64][:2]
     serve.Server(scenes, 150 << 30).run(warm, realtime=False)
     results = {}
-    for mode, max_active in (("served", 64), ("plain", 1)):
+    for mode, max_active, policy in (("served", 64, "srpt"), ("served_fair", 64, "fair"), ("plain", 1, "fair")):
         jobs = stream()
-        srv = serve.Server(scenes, 150 << 30, horizons_per_step=64, max_active=max_active)
+        srv = serve.Server(scenes, 150 << 30, horizons_per_step=64, max_active=max_active, policy=policy)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with ClockSampler(local) as clocks:
@@ -378,7 +380,7 @@ def run_serving(args):
                        "durations_s": [0.05 * args.serving_scale, 2.0 * args.serving_scale],
                        "terrain_grids": list(SERVING_GRIDS), "hbm_budget_gb": 150, "supersample": 1,
                        "time_resolution": 1e-5, "circuit_step": PHYSIC["circuit_step"]},
-            "served": results["served"], "plain": results["plain"],
+            "served": results["served"], "served_fair": results["served_fair"], "plain": results["plain"],
             "p99_speedup_vs_plain": results["plain"]["p99_ms"] / results["served"]["p99_ms"],
             "throughput_vs_plain": results["served"]["events_per_s"] / max(1e-9, results["plain"]["events_per_s"]),
             "setup_s": setup_s}
@@ -399,6 +401,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--cw", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--circuit", default="fp64", choices=["fp64", "fp32"],
+                    help="pixel-circuit arithmetic: fp64 (reference) or fp32 (precision mode)")
     args = ap.parse_args()
     if args.impl == "reference":
         if args.workload == "serving":

@@ -61,7 +61,7 @@ class Physic(C.Structure):
 class SensorOptions(C.Structure):
     _fields_ = [("physic_effects", C.c_int32), ("aer_delay", C.c_int32), ("cells_per_chunk", C.c_int32),
                 ("cells_per_warp", C.c_int32), ("timing", C.c_int32), ("row_begin", C.c_int32),
-                ("row_end", C.c_int32), ("reserved", C.c_int32)]
+                ("row_end", C.c_int32), ("circuit_precision", C.c_int32)]
 
 
 class BvhParams(C.Structure):

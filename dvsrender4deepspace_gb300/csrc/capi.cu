@@ -592,6 +592,8 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
       (long long)n * physic->max_events_per_step > std::numeric_limits<int>::max())
     return fail(DVS_ERR_INVALID, "invalid sensor capacity");
   if (!(physic->circuit_step > 0)) return fail(DVS_ERR_INVALID, "invalid optical/circuit model parameter range");
+  if (opt.circuit_precision != 0 && opt.circuit_precision != 1)
+    return fail(DVS_ERR_INVALID, "circuit precision must be 0 (FP64) or 1 (FP32)");
   dvs_sensor *s = new dvs_sensor;
   s->scene = scene;
   s->physic = *physic;
@@ -599,6 +601,7 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
   s->n_pix = n;
   s->order = scene->pixel_of_rank;
   derive(*physic, s->opt.physic_effects != 0, s->p, s->photo);
+  s->photo.fp32_circuit = s->opt.circuit_precision;
   s->threshold_std = s->opt.physic_effects ? physic->threshold_std : 0;
   s->threshold_min = physic->threshold_min;
   s->max_events = physic->max_events_per_step;

@@ -152,30 +152,52 @@ __global__ void __launch_bounds__(128) circuit_kernel(int n, const int32_t *rank
   const int k = rank_list ? rank_list[r] : r;
   int cnt = ev_count[k];
   if (cnt < 0) return;  // failed earlier in this batch
-  PixelRegs s{st.receptor_log[k], st.reference_log[k], st.refractory_until[k], st.threshold_pos[k],
-              st.threshold_neg[k], st.reset_pending[k] != 0};
   const bool need_rng = photo.shot_noise || p.reset_noise_std > 0;
   curandStateXORWOW_t rng;
   if (need_rng) rng = st.rng[k];
   double *my_t = slab_t + (size_t)k * max_events;
   int8_t *my_p = slab_p + (size_t)k * max_events;
   int failed = 0;
-  for (int c = 0; c < nc; ++c) {
-    const Cell cell = cells[c0 + c];
-    const double rad = radiance[(size_t)c * n + r];
-    if (!isfinite(rad)) { failed = kErrOptical; break; }
-    double rate = rad * photo.electrons_per_radiance + photo.dark_electrons;
-    const double t0 = cell.t0, t1 = cell.t1;
-    if (photo.shot_noise) rate = poisson_electrons(rng, rate * (t1 - t0)) / (t1 - t0);
-    const int emitted = advance_pixel(s, p, rate, t0, t1, my_t + cnt, my_p + cnt, max_events - cnt, rng);
-    if (emitted == -1) { failed = kErrCapacity; break; }
-    if (emitted == -2) { failed = kErrStalled; break; }
-    cnt += emitted;
+  if (!photo.fp32_circuit) {
+    PixelRegs s{st.receptor_log[k], st.reference_log[k], st.refractory_until[k], st.threshold_pos[k],
+                st.threshold_neg[k], st.reset_pending[k] != 0};
+    for (int c = 0; c < nc; ++c) {
+      const Cell cell = cells[c0 + c];
+      const double rad = radiance[(size_t)c * n + r];
+      if (!isfinite(rad)) { failed = kErrOptical; break; }
+      double rate = rad * photo.electrons_per_radiance + photo.dark_electrons;
+      const double t0 = cell.t0, t1 = cell.t1;
+      if (photo.shot_noise) rate = poisson_electrons(rng, rate * (t1 - t0)) / (t1 - t0);
+      const int emitted = advance_pixel(s, p, rate, t0, t1, my_t + cnt, my_p + cnt, max_events - cnt, rng);
+      if (emitted == -1) { failed = kErrCapacity; break; }
+      if (emitted == -2) { failed = kErrStalled; break; }
+      cnt += emitted;
+    }
+    st.receptor_log[k] = s.receptor_log;
+    st.reference_log[k] = s.reference_log;
+    st.refractory_until[k] = s.refractory_until;
+    st.reset_pending[k] = s.reset_pending ? 1 : 0;
+  } else {
+    // precision mode: the state is held in FP32 registers for the chunk
+    PixelRegsF s{(float)st.receptor_log[k], (float)st.reference_log[k], st.refractory_until[k],
+                 (float)st.threshold_pos[k], (float)st.threshold_neg[k], st.reset_pending[k] != 0};
+    for (int c = 0; c < nc; ++c) {
+      const Cell cell = cells[c0 + c];
+      const double rad = radiance[(size_t)c * n + r];
+      if (!isfinite(rad)) { failed = kErrOptical; break; }
+      double rate = rad * photo.electrons_per_radiance + photo.dark_electrons;
+      const double t0 = cell.t0, t1 = cell.t1;
+      if (photo.shot_noise) rate = poisson_electrons(rng, rate * (t1 - t0)) / (t1 - t0);
+      const int emitted = advance_pixel_f32(s, p, rate, t0, t1, my_t + cnt, my_p + cnt, max_events - cnt, rng);
+      if (emitted == -1) { failed = kErrCapacity; break; }
+      if (emitted == -2) { failed = kErrStalled; break; }
+      cnt += emitted;
+    }
+    st.receptor_log[k] = s.receptor_log;
+    st.reference_log[k] = s.reference_log;
+    st.refractory_until[k] = s.refractory_until;
+    st.reset_pending[k] = s.reset_pending ? 1 : 0;
   }
-  st.receptor_log[k] = s.receptor_log;
-  st.reference_log[k] = s.reference_log;
-  st.refractory_until[k] = s.refractory_until;
-  st.reset_pending[k] = s.reset_pending ? 1 : 0;
   if (need_rng) st.rng[k] = rng;
   if (failed) {
     atomicOr(error, failed);

@@ -40,6 +40,7 @@ struct PixelParams {
 struct PhotoParams {
   double electrons_per_radiance, dark_electrons, integration_step;
   int32_t shot_noise;
+  int32_t fp32_circuit;  // receptor/contrast arithmetic in FP32 (times and crossing solves stay FP64)
 };
 
 // Pixel-circuit state, structure of arrays indexed by Morton rank.

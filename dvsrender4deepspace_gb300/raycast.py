@@ -145,7 +145,7 @@ class EventSensor:
     """EventSensor (include/dvs/event_sensor.hpp:40-79) on the GB300 path."""
 
     def __init__(self, scene, physic, physic_effects=True, aer_delay=True, cells_per_chunk=0, cells_per_warp=0,
-                 timing=False, row_begin=0, row_end=0):
+                 timing=False, row_begin=0, row_end=0, circuit_precision="fp64"):
         lib = _capi.load()
         self.scene = scene
         self.physic = dict(physic)
@@ -158,6 +158,9 @@ class EventSensor:
         opt.timing = int(timing)
         opt.row_begin = int(row_begin)
         opt.row_end = int(row_end)
+        if circuit_precision not in ("fp64", "fp32"):
+            raise ValueError("circuit_precision must be fp64 or fp32")
+        opt.circuit_precision = 1 if circuit_precision == "fp32" else 0
         h = C.c_void_p()
         check(lib.dvs_sensor_create(scene.handle, C.byref(physic_struct(physic)), C.byref(opt), C.byref(h)))
         self.handle = h

@@ -4,15 +4,21 @@ Jobs (a camera, a trajectory over one terrain of a pool, a physic block and
 a simulated duration) arrive over time.  The server keeps every admitted
 job's state on the device -- a scene view over its terrain's shared BVH
 (dvs_scene_view_create: one device copy per terrain), its sensor's circuit
-state, RNG and event buffers -- and advances all admitted jobs together: one
-scheduler step enqueues the next horizon batch of every active job on that
+state, RNG and event buffers -- and advances admitted jobs in scheduler
+steps: a step enqueues the next horizon batch of each chosen job on that
 job's own CUDA stream (dvs_sensor_enqueue, asynchronous, so the jobs' kernels
-overlap on the GPU), then collects each job's ready events.  A job that
-reaches its duration is drained and released; arrivals are admitted in
-arrival order whenever their device memory fits under the HBM budget
-(continuous batching: admission happens between steps, while other jobs are
-in flight).  Each job's events depend only on its own inputs, so a job
-yields the same events alone and in any mix.
+overlap on the GPU), then collects those jobs' ready events.  A job that
+reaches its duration is drained and released; arrivals are admitted whenever
+their device memory fits under the HBM budget (continuous batching:
+admission happens between steps, while other jobs are in flight).
+
+Which admitted jobs a step advances is the policy: "srpt" takes jobs in
+order of least remaining work (pixel-cell samples) until the step holds
+fill_samples of work, so short jobs that arrive while a long one runs finish
+first (preemption at batch granularity; the long job's state stays
+resident); "fair" advances every admitted job each step.  Each job's events
+depend only on its own inputs, so a job yields the same events alone, in any
+mix and under either policy.
 
 The reference has no serving layer (one process per sequence,
 tools/run_sequences.py:247-256); this is the GB300 addition.
@@ -69,11 +75,16 @@ class Server:
     """scenes: base DeviceScene per terrain of the pool (their BVHs stay
     resident); hbm_budget: device bytes the admitted jobs may hold."""
 
-    def __init__(self, scenes, hbm_budget, horizons_per_step=64, max_active=64):
+    def __init__(self, scenes, hbm_budget, horizons_per_step=64, max_active=64, policy="srpt",
+                 fill_samples=1 << 26):
+        if policy not in ("srpt", "fair"):
+            raise ValueError("policy must be srpt or fair")
         self.scenes = list(scenes)
         self.budget = int(hbm_budget)
         self.horizons = int(horizons_per_step)
         self.max_active = int(max_active)
+        self.policy = policy
+        self.fill = int(fill_samples)
         self.used = 0
         self.peak_used = 0
         self.peak_active = 0
@@ -87,6 +98,31 @@ class Server:
         chunk = min(RADIANCE_CHUNK_CAP, 8 * n * min(2048, cells))
         return (n * (STATE_BYTES + EVENT_SLAB_BYTES * int(job.physic.get("max_events_per_step", 16)) + 4) + chunk
                 + cells * 256 + (1 << 20))
+
+    @staticmethod
+    def _cells_per_horizon(job):
+        return max(1, math.ceil(job.time_resolution / job.physic.get("circuit_step", 1e-6) - 1e-9))
+
+    def _remaining_samples(self, a):
+        j = a.job
+        horizons = max(0, math.ceil((j.duration - a.cursor) / j.time_resolution - 1e-9))
+        return j.pixels * j.supersample ** 2 * horizons * self._cells_per_horizon(j)
+
+    def _step_samples(self, a):
+        j = a.job
+        horizons = min(self.horizons, max(1, math.ceil((j.duration - a.cursor) / j.time_resolution - 1e-9)))
+        return j.pixels * j.supersample ** 2 * horizons * self._cells_per_horizon(j)
+
+    def _choose(self, active):
+        if self.policy == "fair":
+            return list(active)
+        chosen, work = [], 0
+        for a in sorted(active, key=lambda a: (self._remaining_samples(a), a.job.arrival, a.job.job_id)):
+            if chosen and work + self._step_samples(a) > self.fill:
+                continue
+            chosen.append(a)
+            work += self._step_samples(a)
+        return chosen
 
     def _admit(self, job, now):
         scene = self.scenes[job.terrain].view(job.camera, job.supersample)
@@ -131,21 +167,21 @@ class Server:
                     time.sleep(max(0.0, pending[0].arrival - now()))
                 continue
             self.peak_active = max(self.peak_active, len(active))
-            for a in active:  # launch every job's next batch; nothing waits here
+            chosen = self._choose(active)
+            for a in chosen:  # launch each chosen job's next batch; nothing waits here
                 j = a.job
                 count = min(self.horizons, max(1, math.ceil((j.duration - a.cursor) / j.time_resolution - 1e-9)))
                 ivs = T.horizons(j.path, a.cursor, j.time_resolution, count)
                 a.sensor.enqueue(interval_array(ivs))
                 a.cursor = ivs[-1][3]
             self.steps += 1
-            still = []
-            for a in active:
+            done = set()
+            for a in chosen:
                 a.chunks.append(a.sensor.collect())
                 if a.cursor >= a.job.duration - 1e-12:
                     self._release(a, now())
-                else:
-                    still.append(a)
-            active = still
+                    done.add(id(a))
+            active = [a for a in active if id(a) not in done]
         return jobs
 
 

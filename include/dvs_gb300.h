@@ -100,7 +100,9 @@ typedef struct {
   int32_t cells_per_warp;     /* 1,2,4,8,16,32: cells sharing one warp packet (0 = automatic) */
   int32_t timing;             /* record per-kernel CUDA-event timings */
   int32_t row_begin, row_end; /* rows [row_begin, row_end) only (one GPU's share); 0,0 = all */
-  int32_t reserved;
+  int32_t circuit_precision;  /* 0: FP64 pixel circuit (reference arithmetic); 1: FP32 receptor and
+                                 contrast arithmetic, FP64 times, refractory deadlines and crossing-time
+                                 solves (precision mode; no counterpart in the reference) */
 } dvs_sensor_options;
 
 typedef struct {

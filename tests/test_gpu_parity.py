@@ -202,6 +202,32 @@ def test_sensor_pulse_matches_oracle_full_resolution():
     assert np.max(rel_err(ev["depth"], oev["depth"])) < RTOL
 
 
+def test_fp32_circuit_precision_mode_against_the_fp64_oracle():
+    """Precision mode (FP32 receptor/contrast arithmetic, FP64 times and
+    crossing solves) on the pulse case: the same per-pixel polarity sequences
+    as the FP64 oracle except pixels within 1e-4 of a threshold, timestamps
+    within the stated 1 us."""
+    scene, phys = plane_sensor()
+    start = dict(POSE, intensity_rate=8e6)
+    end = dict(POSE, intensity_rate=-8e6)
+    ivs = [(POSE, POSE, 0, 0.001), (start, end, 0.001, 0.003)]
+    s = EventSensor(scene, phys, circuit_precision="fp32")
+    s.initialize(POSE, 0)
+    ev = pixel_sorted(s.process_many(ivs))
+    V, N, I = plane_mesh()
+    ors = O.OracleSensor(O.OracleScene(V, N, I, DAVIS, 1, DAVIS_HAPKE), phys)
+    ors.initialize(POSE, 0)
+    oev = pixel_sorted(ors.process(ivs))
+    assert abs(len(ev) - len(oev)) <= max(2, len(oev) // 1000) and len(oev) > 0
+    if len(ev) == len(oev):
+        for f in ("x", "y", "polarity"):
+            assert float(np.mean(ev[f] != oev[f])) < 1e-3
+        same = (ev["x"] == oev["x"]) & (ev["y"] == oev["y"]) & (ev["polarity"] == oev["polarity"])
+        assert np.max(np.abs(ev["timestamp"][same] - oev["timestamp"][same])) < 1e-6
+    with pytest.raises(ValueError):
+        EventSensor(scene, phys, circuit_precision="fp16")
+
+
 def pixel_sorted(ev):
     return ev[np.lexsort((ev["timestamp"], ev["x"], ev["y"]))]
 

@@ -73,8 +73,10 @@ def test_jobs_give_the_same_events_alone_and_in_the_mix(pool):
     tight_server = serve.Server(pool, hbm_budget=budget, horizons_per_step=16, max_active=8)
     tight = events_by_job(tight_server.run(jobs(), realtime=False))
     assert 1 <= tight_server.peak_active < 6 and tight_server.peak_used <= budget
+    fair = events_by_job(serve.Server(pool, hbm_budget=8 << 30, horizons_per_step=16, policy="fair",
+                                      fill_samples=1).run(jobs(), realtime=False))
     for k, ev in alone.items():
-        for other in (mixed[k], tight[k]):
+        for other in (mixed[k], tight[k], fair[k]):
             assert len(other) == len(ev)
             for f in ev.dtype.names:
                 assert np.array_equal(other[f], ev[f]), (k, f)
