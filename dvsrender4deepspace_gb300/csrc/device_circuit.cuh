@@ -51,12 +51,14 @@ __device__ int advance_pixel(PixelRegs &s, const PixelParams &p, double rate, do
     double remaining = t1 - cursor;
     double c0 = u - s.reference_log;
     double boundary = remaining;
-    double x = exp(u), target = rate + p.charge_scale * p.reference_leak;
-    if (p.reference_leak > 0 && x > target && target > rate) {
-      double extremum;
-      if (rate > 0) extremum = -p.charge_scale / rate * log((1.0 / target - 1.0 / rate) / (1.0 / x - 1.0 / rate));
-      else extremum = p.charge_scale * (1.0 / target - 1.0 / x);
-      if (extremum > 1e-15 && extremum < boundary) boundary = extremum;
+    if (p.reference_leak > 0) {  // the leak extremum exists only with a leak: no exp(u) otherwise
+      const double x = exp(u), target = rate + p.charge_scale * p.reference_leak;
+      if (x > target && target > rate) {
+        double extremum;
+        if (rate > 0) extremum = -p.charge_scale / rate * log((1.0 / target - 1.0 / rate) / (1.0 / x - 1.0 / rate));
+        else extremum = p.charge_scale * (1.0 / target - 1.0 / x);
+        if (extremum > 1e-15 && extremum < boundary) boundary = extremum;
+      }
     }
     double ub = receptor_log_at(u, rate, boundary, p.charge_scale);
     double cb = ub - s.reference_log + p.reference_leak * boundary;

@@ -140,6 +140,7 @@ __global__ void init_pixels_kernel(int n, const int32_t *pixel_of_rank, const do
   st.rng[k] = rng;
 }
 
+template <bool kF32>
 __global__ void __launch_bounds__(128) circuit_kernel(int n, const int32_t *rank_list, const Cell *cells, int c0,
                                                       int nc, const double *radiance, PixelParams p,
                                                       PhotoParams photo, int max_events, CircuitState st,
@@ -158,7 +159,7 @@ __global__ void __launch_bounds__(128) circuit_kernel(int n, const int32_t *rank
   double *my_t = slab_t + (size_t)k * max_events;
   int8_t *my_p = slab_p + (size_t)k * max_events;
   int failed = 0;
-  if (!photo.fp32_circuit) {
+  if (!kF32) {
     PixelRegs s{st.receptor_log[k], st.reference_log[k], st.refractory_until[k], st.threshold_pos[k],
                 st.threshold_neg[k], st.reset_pending[k] != 0};
     for (int c = 0; c < nc; ++c) {
@@ -360,8 +361,12 @@ cudaError_t launch_circuit_list(int n, const int32_t *rank_list, const Cell *cel
                                 CircuitState st, int32_t *ev_count, double *slab_t, int8_t *slab_p, int32_t *error,
                                 unsigned long long *counters, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  circuit_kernel<<<blocks(n, 128), 128, 0, s>>>(n, rank_list, cells, c0, nc, radiance, p, photo, max_events, st,
-                                                ev_count, slab_t, slab_p, error, counters);
+  if (photo.fp32_circuit)
+    circuit_kernel<true><<<blocks(n, 128), 128, 0, s>>>(n, rank_list, cells, c0, nc, radiance, p, photo, max_events,
+                                                        st, ev_count, slab_t, slab_p, error, counters);
+  else
+    circuit_kernel<false><<<blocks(n, 128), 128, 0, s>>>(n, rank_list, cells, c0, nc, radiance, p, photo, max_events,
+                                                         st, ev_count, slab_t, slab_p, error, counters);
   return cudaGetLastError();
 }
 
