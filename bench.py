@@ -208,8 +208,12 @@ def run_gb300(args):
         t_cursor[0] = ivs[-1][3]
         return interval_array(ivs)
 
-    for _ in range(args.warmup):
-        sensor.process_many(next_batch())
+    tuning = None
+    for k in range(args.warmup):
+        b = next_batch()
+        if k == 0 and args.autotune:
+            tuning = sensor.autotune(b)
+        sensor.process_many(b)
     # ---- device-resident timed region (value)
     batches = [next_batch() for _ in range(args.steps)]
     stream = torch.cuda.ExternalStream(sensor.stream())
@@ -307,7 +311,7 @@ def run_gb300(args):
         "roofline_circuit": {"bound": "hbm", "kernel": "circuit_kernel",
                              "achieved": circuit_bytes / (circuit_ms / 1e3) / 1e9 if circuit_ms > 0 else None,
                              "peak": peak, "unit": "GB/s"},
-        "clocks": clocks.summary(), "setup_s": setup_s, "bvh_build_s": info["build_seconds"],
+        "clocks": clocks.summary(), "setup_s": setup_s, "bvh_build_s": info["build_seconds"], "tuning": tuning,
         "cpu_baseline": cb,
     }
     if line["roofline_circuit"]["achieved"]:
@@ -401,6 +405,7 @@ def main():
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--cw", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--autotune", action="store_true", help="time the packet shapes on the first warm-up batch")
     ap.add_argument("--circuit", default="fp64", choices=["fp64", "fp32"],
                     help="pixel-circuit arithmetic: fp64 (reference) or fp32 (precision mode)")
     args = ap.parse_args()

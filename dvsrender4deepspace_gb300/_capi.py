@@ -95,7 +95,12 @@ EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_d
            "dvs_readout_create", "dvs_readout_destroy", "dvs_readout_submit", "dvs_readout_drain", "dvs_readout_read",
            "dvs_readout_counters", "dvs_config_load", "dvs_frames_load", "dvs_trajectory_create",
            "dvs_trajectory_destroy", "dvs_trajectory_range", "dvs_trajectory_evaluate", "dvs_cam_render_blur",
-           "dvs_scene_view_create", "dvs_sensor_device_bytes")
+           "dvs_scene_view_create", "dvs_sensor_device_bytes", "dvs_sensor_set_tuning", "dvs_sensor_autotune")
+
+
+class Tuning(C.Structure):
+    _fields_ = [("cells_per_warp", C.c_int32), ("rays_per_lane", C.c_int32), ("candidates", C.c_int32),
+                ("cells_timed", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double)]
 
 
 class SceneConfig(C.Structure):
@@ -159,6 +164,8 @@ def _declare(lib):
     lib.dvs_cam_render_blur.argtypes = [vp, vp, f_p, sz, f_p]
     lib.dvs_scene_view_create.argtypes = [vp, C.POINTER(Camera), C.c_int32, C.POINTER(Hapke), C.POINTER(vp)]
     lib.dvs_sensor_device_bytes.argtypes = [vp, C.POINTER(C.c_uint64)]
+    lib.dvs_sensor_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
+    lib.dvs_sensor_autotune.argtypes = [vp, vp, sz, C.POINTER(Tuning)]
     lib.dvs_sensor_process_adaptive.argtypes = [vp, vp, sz, C.c_double, C.c_int32, C.POINTER(C.c_int32),
                                                 C.POINTER(sz)]
     lib.dvs_sensor_refinement_stats.argtypes = [vp, C.POINTER(RefinementStats)]

@@ -169,6 +169,7 @@ struct dvs_scene {
     v.cy = camera.cy;
     v.coherent_span = coherent_span;
     v.hapke = hapke;
+    v.pairs = 1;
     return v;
   }
   int pixels() const { return camera.width * camera.height; }
@@ -243,9 +244,11 @@ struct dvs_sensor {
   int32_t *own_order = nullptr;      // allocated when the sensor covers a row band
   std::vector<int32_t> band_rank_of_pixel;  // band-local row-major pixel -> rank
   int pixels() const { return n_pix; }
+  int rays_per_lane = 2;  // traversal tuning: 1 or 2 sub-rays per lane (dvs_sensor_set_tuning / autotune)
   SceneView view() const {
     SceneView v = scene->view();
     v.pixel_of_rank = order;
+    v.pairs = rays_per_lane == 2 ? 1 : 0;
     return v;
   }
 };
@@ -1234,6 +1237,77 @@ int dvs_sensor_stats_get(const dvs_sensor *s, dvs_sensor_stats *out) {
   out->primary_rays = c[kCntPrimary];
   out->shadow_rays = c[kCntShadow];
   out->circuit_cells = c[kCntCells];
+  return DVS_OK;
+}
+
+int dvs_sensor_set_tuning(dvs_sensor *s, int32_t cells_per_warp, int32_t rays_per_lane) {
+  if (!s) return fail(DVS_ERR_INVALID, "null argument");
+  if (cells_per_warp < 0 || cells_per_warp > 32 || (cells_per_warp & (cells_per_warp - 1)) ||
+      (rays_per_lane != 1 && rays_per_lane != 2))
+    return fail(DVS_ERR_INVALID, "invalid traversal tuning");
+  s->opt.cells_per_warp = cells_per_warp;
+  s->rays_per_lane = rays_per_lane;
+  return DVS_OK;
+}
+
+int dvs_sensor_autotune(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, dvs_tuning *out) {
+  // Times the optics of (a prefix of) the next batch for every packet shape
+  // -- cells per warp 4..32, one or two sub-rays per lane -- and keeps the
+  // fastest.  Only the trace kernel runs: no circuit state, RNG or time
+  // changes, so the same batch is then processed as usual.
+  if (!out) return fail(DVS_ERR_INVALID, "null argument");
+  size_t n_cells = 0;
+  int r = upload_batch(s, ivs, count, n_cells);
+  if (r) return r;
+  const int n = s->pixels();
+  size_t chunk;
+  int default_log2;
+  chunk_shape(s, n_cells, (size_t)n, chunk, default_log2);
+  const int nc = (int)std::min<size_t>(std::min<size_t>(chunk, n_cells), 256);
+  CUDA_TRY(ensure_radiance(s, (size_t)nc), "radiance chunk allocation");
+  const int ss2 = s->scene->samples * s->scene->samples;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0), "autotune timer");
+  CUDA_TRY(cudaEventCreate(&e1), "autotune timer");
+  SceneView view = s->view();
+  float best = -1, def_ms = -1;
+  int best_log2 = default_log2, best_rays = s->rays_per_lane, tried = 0;
+  cudaError_t err = cudaSuccess;
+  for (int rays = 1; rays <= 2 && err == cudaSuccess; ++rays) {
+    if (rays == 2 && ss2 % 2) break;
+    view.pairs = rays == 2;
+    for (int lg = 2; lg <= 5 && err == cudaSuccess; ++lg) {
+      if ((1 << lg) > nc && lg > 2) break;
+      float ms = 0;
+      for (int rep = 0; rep < 2 && err == cudaSuccess; ++rep) {  // first launch warms caches
+        err = cudaEventRecord(e0, s->stream);
+        if (err == cudaSuccess)
+          err = launch_trace_cells(view, n, s->poses, 0, nc, lg, s->radiance, nullptr, nullptr, s->stream);
+        if (err == cudaSuccess) err = cudaEventRecord(e1, s->stream);
+        if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+      }
+      if (err != cudaSuccess) break;
+      ++tried;
+      if (lg == default_log2 && rays == s->rays_per_lane) def_ms = ms;
+      if (best < 0 || ms < best) {
+        best = ms;
+        best_log2 = lg;
+        best_rays = rays;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in autotune : ") + cudaGetErrorString(err));
+  s->opt.cells_per_warp = 1 << best_log2;
+  s->rays_per_lane = best_rays;
+  out->cells_per_warp = 1 << best_log2;
+  out->rays_per_lane = best_rays;
+  out->candidates = tried;
+  out->cells_timed = nc;
+  out->best_ms = best;
+  out->default_ms = def_ms;
   return DVS_OK;
 }
 

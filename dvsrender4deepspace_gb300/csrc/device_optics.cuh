@@ -644,6 +644,368 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
   return out;
 }
 
+// ---- two sub-rays per lane ------------------------------------------------------
+// The same traversal with each lane carrying R rays (two neighbouring sub-rays
+// of its pixel-cell): the packet is 32 x R rays, so the interval node tests,
+// the stack traffic and the packet set-up are paid once per 32 x R rays, and
+// a leaf's triangle records are loaded once for the lane's R rays.  Per-ray
+// results are those of the one-ray traversal (every interval bound covers
+// all R rays; leaves are tested per ray).
+
+// Warp extremes of per-lane [lo, hi] ranges; inactive lanes count as empty.
+__device__ __forceinline__ void wrange(float lo, float hi, bool active, float &wlo, float &whi) {
+  wlo = funord(__reduce_min_sync(kFull, active ? ford(lo) : 0xff800000u));
+  whi = funord(__reduce_max_sync(kFull, active ? ford(hi) : 0x007fffffu));
+}
+
+template <int R>
+__device__ Packet make_packet_r(const SceneView &S, const float3 (&o)[R], const float3 (&d)[R],
+                                const float3 (&idir)[R], const bool (&active)[R]) {
+  float3 olo = f3(kInf(), kInf(), kInf()), ohi = -olo, ilo = olo, ihi = -olo, dlo = olo, dhi = -olo;
+  bool any = false;
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (active[r]) {
+      any = true;
+      olo = f3(fminf(olo.x, o[r].x), fminf(olo.y, o[r].y), fminf(olo.z, o[r].z));
+      ohi = f3(fmaxf(ohi.x, o[r].x), fmaxf(ohi.y, o[r].y), fmaxf(ohi.z, o[r].z));
+      ilo = f3(fminf(ilo.x, idir[r].x), fminf(ilo.y, idir[r].y), fminf(ilo.z, idir[r].z));
+      ihi = f3(fmaxf(ihi.x, idir[r].x), fmaxf(ihi.y, idir[r].y), fmaxf(ihi.z, idir[r].z));
+      dlo = f3(fminf(dlo.x, d[r].x), fminf(dlo.y, d[r].y), fminf(dlo.z, d[r].z));
+      dhi = f3(fmaxf(dhi.x, d[r].x), fmaxf(dhi.y, d[r].y), fmaxf(dhi.z, d[r].z));
+    }
+  Packet P;
+  wrange(olo.x, ohi.x, any, P.olo.x, P.ohi.x);
+  wrange(olo.y, ohi.y, any, P.olo.y, P.ohi.y);
+  wrange(olo.z, ohi.z, any, P.olo.z, P.ohi.z);
+  wrange(ilo.x, ihi.x, any, P.ilo.x, P.ihi.x);
+  wrange(ilo.y, ihi.y, any, P.ilo.y, P.ihi.y);
+  wrange(ilo.z, ihi.z, any, P.ilo.z, P.ihi.z);
+  float wl, wh;
+  wrange(dlo.x, dhi.x, any, wl, wh);
+  const float dx = wh - wl;
+  wrange(dlo.y, dhi.y, any, wl, wh);
+  const float dy = wh - wl;
+  wrange(dlo.z, dhi.z, any, wl, wh);
+  const float dz = wh - wl;
+  const float ds = fmaxf(fmaxf(dx, dy), dz);
+  const float os = fmaxf(fmaxf(P.ohi.x - P.olo.x, P.ohi.y - P.olo.y), P.ohi.z - P.olo.z);
+  P.nx = P.ihi.x < 0.0f;
+  P.ny = P.ihi.y < 0.0f;
+  P.nz = P.ihi.z < 0.0f;
+  const bool one_sign = (P.nx || P.ilo.x > 0.0f) && (P.ny || P.ilo.y > 0.0f) && (P.nz || P.ilo.z > 0.0f);
+  P.coherent = one_sign && ds <= 0.02f && os <= S.coherent_span;
+  P.o_near = f3(P.nx ? P.olo.x : P.ohi.x, P.ny ? P.olo.y : P.ohi.y, P.nz ? P.olo.z : P.ohi.z);
+  P.o_far = f3(P.nx ? P.ohi.x : P.olo.x, P.ny ? P.ohi.y : P.olo.y, P.nz ? P.ohi.z : P.olo.z);
+  return P;
+}
+
+template <bool kSorted, int R>
+__device__ __forceinline__ bool expand_node_r(const SceneView &S, int node, const Packet &P, const float3 (&o)[R],
+                                              const float3 (&idir)[R], const bool (&live)[R], float t_min,
+                                              const float (&lane_tmax)[R], float packet_tmax, Stack &st, int &next,
+                                              float &next_t, bool &overflow) {
+  const int lane = threadIdx.x & 31;
+  float key = kInf();
+  bool hit = false;
+  int code = 0;
+  if (P.coherent) {
+    if (lane < kBvhWidth) {
+      const ChildRec c = load_child(S.nodes, node, lane);
+      if (c.count >= 0) {
+        hit = packet_slab(c, P, t_min, packet_tmax, key);
+        code = c.count > 0 ? leaf_code(node, lane) : c.child;
+      }
+    }
+  } else {
+    for (int slot = 0; slot < kBvhWidth; ++slot) {
+      const ChildRec c = load_child(S.nodes, node, slot);
+      float near = kInf();
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        float tn = kInf();
+        if (c.count >= 0 && live[r] && slab(c.lo, c.hi, o[r], idir[r], t_min, lane_tmax[r], tn)) near = fminf(near, tn);
+      }
+      const float k = wmin(near);
+      if (lane == slot) {
+        hit = k < kInf();
+        key = k;
+        code = c.count > 0 ? leaf_code(node, slot) : c.child;
+      }
+    }
+  }
+  const unsigned mask = __ballot_sync(kFull, hit && lane < kBvhWidth);
+  if (!mask) return false;
+  const int n = __popc(mask);
+  if (n == 1) {
+    const int only = __ffs(mask) - 1;
+    next = __shfl_sync(kFull, code, only);
+    next_t = __shfl_sync(kFull, key, only);
+    return true;
+  }
+  int rank = 0;
+  if (kSorted) {
+#pragma unroll
+    for (int j = 0; j < kBvhWidth; ++j) {
+      const float kj = __shfl_sync(kFull, key, j);
+      rank += ((mask >> j) & 1) && (kj < key || (kj == key && j < lane)) ? 1 : 0;
+    }
+  } else {
+    rank = __popc(mask & ((1u << lane) - 1u));
+  }
+  if (st.sp + n - 1 > kStackSlots) {
+    overflow = true;
+    return false;
+  }
+  if (hit && lane < kBvhWidth && rank > 0) {
+    const int slot = st.sp + (n - 1 - rank);
+    st.code[slot] = code;
+    st.t[slot] = key;
+  }
+  const int first = __ffs(__ballot_sync(kFull, hit && lane < kBvhWidth && rank == 0)) - 1;
+  next = __shfl_sync(kFull, code, first);
+  next_t = __shfl_sync(kFull, key, first);
+  st.sp += n - 1;
+  __syncwarp();
+  return true;
+}
+
+template <int R>
+__device__ __forceinline__ float lane_reach(const bool (&active)[R], const float (&closest)[R]) {
+  float m = -1.0f;
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (active[r]) m = fmaxf(m, closest[r]);
+  return m;
+}
+
+template <int R>
+__device__ void trace_nearest_packet_r(const SceneView &S, const float3 (&o)[R], const float3 (&d)[R],
+                                       const bool (&active)[R], int *stack_code, float *stack_t, HitRecord (&h)[R]) {
+  float3 idir[R];
+  float closest[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    idir[r] = inverse_direction(d[r]);
+    closest[r] = active[r] ? 1e30f : -1.0f;
+    h[r] = HitRecord{0, -1, 0.f, 0.f, 0.f};
+  }
+  const Packet P = make_packet_r<R>(S, o, d, idir, active);
+  float packet_tmax = wmax(lane_reach<R>(active, closest));
+  Stack st{stack_code, stack_t, 0};
+  int entry = 0;
+  float entry_t = 0.0f;
+  bool overflow = false;
+  while (true) {
+    if (entry_t <= packet_tmax) {
+      if (entry >= 0) {
+        int next;
+        float next_t;
+        if (expand_node_r<true, R>(S, entry, P, o, idir, active, kRayEps, closest, packet_tmax, st, next, next_t,
+                                   overflow)) {
+          entry = next;
+          entry_t = next_t;
+          continue;
+        }
+        if (overflow) break;
+      } else {
+        const int lc = -entry - 1;
+        const ChildRec c = load_child(S.nodes, lc / kBvhWidth, lc % kBvhWidth);
+        bool need[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          float tn;
+          need[r] = active[r] && slab(c.lo, c.hi, o[r], idir[r], kRayEps, closest[r], tn);
+        }
+        for (int i = 0; i < c.count; ++i) {
+          const float4 *q4 = reinterpret_cast<const float4 *>(S.tris + c.child + i);
+          const float4 a = __ldg(q4), b = __ldg(q4 + 1), q = __ldg(q4 + 2);
+          const float3 v0 = f3(a.x, a.y, a.z), e1 = f3(a.w, b.x, b.y), e2 = f3(b.z, b.w, q.x);
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            float t, u, v;
+            if (need[r] && intersect_tri(d[r], o[r], v0, e1, e2, t, u, v) && t < closest[r]) {
+              closest[r] = t;
+              h[r].hit = 1; h[r].tri = c.child + i; h[r].t = t; h[r].u = u; h[r].v = v;
+            }
+          }
+        }
+        packet_tmax = wmax(lane_reach<R>(active, closest));
+      }
+    }
+    if (st.sp == 0) break;
+    --st.sp;
+    entry = st.code[st.sp];
+    entry_t = st.t[st.sp];
+  }
+  __syncwarp();
+  if (overflow)
+#pragma unroll
+    for (int r = 0; r < R; ++r) h[r].hit = -1;
+}
+
+template <int R>
+__device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], float3 light, const bool (&active)[R],
+                                      const int (&self)[R], int *stack_code, float *stack_t, bool (&occluded)[R]) {
+  const float3 idir1 = inverse_direction(light);
+  float3 d[R], idir[R];
+  bool alive[R];
+  float reach[R];
+  const float t_max = 1e30f;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    d[r] = light;
+    idir[r] = idir1;
+    alive[r] = active[r];
+    occluded[r] = false;
+  }
+  const Packet P = make_packet_r<R>(S, o, d, idir, active);
+  Stack st{stack_code, stack_t, 0};
+  int entry = 0;
+  bool overflow = false;
+  while (true) {
+    bool any = false;
+#pragma unroll
+    for (int r = 0; r < R; ++r) any = any || alive[r];
+    if (!__any_sync(kFull, any)) break;
+    if (entry >= 0) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) reach[r] = alive[r] ? t_max : -1.0f;
+      int next;
+      float next_t;
+      if (expand_node_r<false, R>(S, entry, P, o, idir, alive, kRayEps, reach, t_max, st, next, next_t, overflow)) {
+        entry = next;
+        continue;
+      }
+      if (overflow) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) occluded[r] = occluded[r] || alive[r];  // conservative (device_ray.hpp:119)
+        break;
+      }
+    } else {
+      const int lc = -entry - 1;
+      const ChildRec c = load_child(S.nodes, lc / kBvhWidth, lc % kBvhWidth);
+      bool need[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        float tn;
+        need[r] = alive[r] && slab(c.lo, c.hi, o[r], idir[r], kRayEps, t_max, tn);
+      }
+      for (int i = 0; i < c.count; ++i) {
+        const int id = c.child + i;
+        const float4 *q4 = reinterpret_cast<const float4 *>(S.tris + id);
+        const float4 a = __ldg(q4), b = __ldg(q4 + 1), q = __ldg(q4 + 2);
+        const float3 v0 = f3(a.x, a.y, a.z), e1 = f3(a.w, b.x, b.y), e2 = f3(b.z, b.w, q.x);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          float t, u, v;
+          if (need[r] && alive[r] && id != self[r] && intersect_tri(light, o[r], v0, e1, e2, t, u, v) &&
+              t > kRayEps && t < t_max) {
+            occluded[r] = true;
+            alive[r] = false;
+          }
+        }
+      }
+    }
+    if (st.sp == 0) break;
+    --st.sp;
+    entry = st.code[st.sp];
+  }
+  __syncwarp();
+}
+
+// sample_pixel_packet with two neighbouring sub-rays per lane (ss^2 even).
+// The per-ray work, the order of the FP64 radiance and depth sums and the
+// ray counts are those of the one-ray loop.
+template <int kMode>
+__device__ PixelSample sample_pixel_pairs(const SceneView &S, int pixel, bool active, const CellPose &pose,
+                                          int *stack_code, float *stack_t, const double *cos4_table) {
+  constexpr int R = 2;
+  PixelSample out{0.0, -1.0f, true, 0u, 0u};
+  double depth = 0;
+  int valid_depth = 0;
+  const float3 light = f3(pose.lx, pose.ly, pose.lz);
+  const float3 origin = f3(pose.px, pose.py, pose.pz);
+  const int ss = S.samples, n_sub = ss * ss;
+  const int px_i = pixel % S.width, py_i = pixel / S.width;
+  const HapkeConst hc = hapke_const(S.hapke);
+  for (int j = 0; j < n_sub; j += R) {
+    float px[R], py[R];
+    float3 ray[R], org[R];
+    bool live[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int sx = (j + r) % ss, sy = (j + r) / ss;
+      px[r] = subray_x(S, px_i, sx);
+      py[r] = subray_y(S, py_i, sy);
+      ray[r] = normalize(rotate_ray(pose, f3(px[r], -py[r], -1)));
+      org[r] = origin;
+      live[r] = active && out.valid;
+    }
+    HitRecord hit[R];
+    trace_nearest_packet_r<R>(S, org, ray, live, stack_code, stack_t, hit);
+    bool lit[R];
+    float3 normal[R], sorigin[R];
+    float albedo[R], r0[R];
+    int self[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (active && out.valid) ++out.primary;
+      if (hit[r].hit < 0) out.valid = false;
+      const bool hitp = active && out.valid && hit[r].hit == 1;
+      lit[r] = false;
+      normal[r] = f3(0, 0, 0);
+      sorigin[r] = f3(0, 0, 0);
+      albedo[r] = S.hapke.w;
+      r0[r] = hc.r0_w;
+      self[r] = hit[r].tri;
+      if (hitp) {
+        if (kMode != kRadiance) {
+          depth += hit[r].t;
+          ++valid_depth;
+        }
+        if (kMode != kDepthOnly) {
+          const float4 *q = reinterpret_cast<const float4 *>(S.shade + hit[r].tri);
+          const float4 s0 = __ldg(q), s1 = __ldg(q + 1), s2 = __ldg(q + 2);
+          const float w = 1 - hit[r].u - hit[r].v;
+          normal[r] = normalize(f3(s0.x, s0.y, s0.z) * w + f3(s1.x, s1.y, s1.z) * hit[r].u +
+                                f3(s2.x, s2.y, s2.z) * hit[r].v);
+          lit[r] = !(dot(normal[r], light) <= 0 || dot(normal[r], -ray[r]) <= 0);
+          if (lit[r]) {
+            const float4 *t4 = reinterpret_cast<const float4 *>(S.tris + hit[r].tri);
+            const float4 a = __ldg(t4), b = __ldg(t4 + 1), c = __ldg(t4 + 2);
+            sorigin[r] = shadow_origin(f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, c.x), hit[r].u, hit[r].v,
+                                       light);
+            if (S.has_albedo) {
+              albedo[r] = s0.w * w + s1.w * hit[r].u + s2.w * hit[r].v;
+              r0[r] = hfunc_r0(albedo[r]);
+            }
+          }
+        }
+      }
+    }
+    if (kMode != kDepthOnly) {
+      if (__any_sync(kFull, lit[0] || lit[1])) {
+        bool occ[R];
+        trace_shadow_packet_r<R>(S, sorigin, light, lit, self, stack_code, stack_t, occ);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (lit[r]) ++out.shadow;
+          if (lit[r] && !occ[r]) {
+            const double cos4 = cos4_table ? cos4_table[j + r] : cos4_of(px[r], py[r]);
+            const float3 n = normalize(normal[r]), l = normalize(light), v = normalize(-ray[r]);
+            const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo[r], r0[r], S.hapke, hc);
+            out.radiance += fmaxf(0, n_h * pose.intensity) * cos4;
+          }
+        }
+      }
+    }
+  }
+  out.radiance /= ss * ss;
+  out.depth = valid_depth ? float(depth / valid_depth) : -1.0f;
+  return out;
+}
+
 __device__ __forceinline__ unsigned warp_sum(unsigned v) { return __reduce_add_sync(kFull, v); }
 
 }  // namespace

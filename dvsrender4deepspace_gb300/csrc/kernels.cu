@@ -70,9 +70,19 @@ constexpr int kWarpsPerBlock = 4;  // all ray kernels launch 128 threads
 #define DVS_TRACE_MIN_BLOCKS 5
 #endif
 constexpr int kCos4Table = 256;    // sub-rays per pixel with a shared cos^4 table (ss <= 16)
+// Two sub-rays per lane when a pixel has an even number of them; that
+// kernel carries twice the ray state and is compiled for 4 blocks per SM
+// (128 registers).
+#ifndef DVS_TRACE_PAIRS
+#define DVS_TRACE_PAIRS 1
+#endif
+#ifndef DVS_TRACE_PAIR_MIN_BLOCKS
+#define DVS_TRACE_PAIR_MIN_BLOCKS 4
+#endif
 
-template <int kMode>
-__global__ void __launch_bounds__(128, DVS_TRACE_MIN_BLOCKS) trace_cells_kernel(SceneView S, int n_pix,
+template <int kMode, bool kPairs>
+__global__ void __launch_bounds__(128, kPairs ? DVS_TRACE_PAIR_MIN_BLOCKS : DVS_TRACE_MIN_BLOCKS)
+    trace_cells_kernel(SceneView S, int n_pix,
                                                                                 const int32_t *rank_list,
                                                           const CellPose *poses, int c0, int nc, int cw_log2,
                                                           double *radiance, float *depth_out,
@@ -101,8 +111,11 @@ __global__ void __launch_bounds__(128, DVS_TRACE_MIN_BLOCKS) trace_cells_kernel(
       s_cos4[wib][j] = cos4_of(subray_x(S, pixel % S.width, j % S.samples), subray_y(S, pixel / S.width, j / S.samples));
     __syncwarp();
   }
-  const PixelSample s = sample_pixel_packet<kMode>(S, pixel, active, pose, s_code[wib], s_t[wib],
-                                                   shared_cos4 ? s_cos4[wib] : nullptr);
+  const PixelSample s =
+      kPairs ? sample_pixel_pairs<kMode>(S, pixel, active, pose, s_code[wib], s_t[wib],
+                                         shared_cos4 ? s_cos4[wib] : nullptr)
+             : sample_pixel_packet<kMode>(S, pixel, active, pose, s_code[wib], s_t[wib],
+                                          shared_cos4 ? s_cos4[wib] : nullptr);
   if (active) {
     const size_t o = (size_t)cell * n_pix + rank;
     radiance[o] = s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll);
@@ -334,12 +347,23 @@ cudaError_t launch_trace_list(const SceneView &scene, int n_pix, const int32_t *
   if (n_pix <= 0 || nc <= 0) return cudaSuccess;
   const int cw = 1 << cw_log2, ppw = 32 >> cw_log2;
   const long long warps = (long long)((n_pix + ppw - 1) / ppw) * ((nc + cw - 1) / cw);
-  if (depth)
-    trace_cells_kernel<kRadianceDepth><<<blocks(warps * 32, 128), 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc,
-                                                                               cw_log2, radiance, depth, counters);
-  else
-    trace_cells_kernel<kRadiance><<<blocks(warps * 32, 128), 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc,
-                                                                          cw_log2, radiance, nullptr, counters);
+  const bool pairs = DVS_TRACE_PAIRS && scene.pairs && (scene.samples * scene.samples) % 2 == 0;
+  const int grid = blocks(warps * 32, 128);
+  if (depth) {
+    if (pairs)
+      trace_cells_kernel<kRadianceDepth, true><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2,
+                                                                    radiance, depth, counters);
+    else
+      trace_cells_kernel<kRadianceDepth, false><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2,
+                                                                     radiance, depth, counters);
+  } else {
+    if (pairs)
+      trace_cells_kernel<kRadiance, true><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2,
+                                                               radiance, nullptr, counters);
+    else
+      trace_cells_kernel<kRadiance, false><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2,
+                                                                radiance, nullptr, counters);
+  }
   return cudaGetLastError();
 }
 

@@ -243,6 +243,17 @@ class EventSensor:
     def reset_stats(self):
         check(_capi.load().dvs_sensor_stats_reset(self.handle))
 
+    def set_tuning(self, cells_per_warp=0, rays_per_lane=2):
+        check(_capi.load().dvs_sensor_set_tuning(self.handle, int(cells_per_warp), int(rays_per_lane)))
+
+    def autotune(self, intervals):
+        """Times the trace of the next batch for each packet shape and keeps
+        the fastest (dvs_sensor_autotune); the batch is then processed as usual."""
+        ivs = interval_array(intervals)
+        out = _capi.Tuning()
+        check(_capi.load().dvs_sensor_autotune(self.handle, ivs.ctypes.data, len(ivs), C.byref(out)))
+        return {k: getattr(out, k) for k, _ in out._fields_}
+
     def device_bytes(self):
         out = C.c_uint64()
         check(_capi.load().dvs_sensor_device_bytes(self.handle, C.byref(out)))

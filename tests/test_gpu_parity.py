@@ -343,6 +343,51 @@ def test_sensor_matches_oracle_on_moving_terrain():
     assert worst < 1e-6
 
 
+def test_packet_shape_and_autotuner_do_not_change_events():
+    """Cells per warp, one or two sub-rays per lane and the autotuner's
+    choice change how rays share warps, not what each ray computes: the
+    events of a moving, pulsed terrain pass (4 sub-rays per pixel) are the
+    same for every shape."""
+    cam = dict(width=64, height=48, fx=60.0, fy=60.0, cx=32.0, cy=24.0)
+    V, N, I, camera, hap, scene = terrain_scene(n=80, seed=9, camera=cam, ss=2)
+    traj = trajectory.StraightPass((0.0, 0.0, 400.0), (50.0, 0.0, 0.0), trajectory.sun_direction(30), 1000.0)
+    phys = davis_physic(threshold_std=0, max_events_per_step=64, readout_bandwidth=0, readout_latency=0,
+                        threshold_pos=0.05, threshold_neg=0.05, refractory_time=5e-5, random_seed=5)
+
+    def run(shape):
+        s = EventSensor(scene, phys)
+        s.initialize(traj.state(0.0), 0.0)
+        out, t, tuned = [], 0.0, None
+        for batch in range(2):
+            ivs = trajectory.horizons(traj, t, 1e-4, 20)
+            a, b = traj.state(ivs[-1][3]), traj.state(ivs[-1][3] + 2e-3)
+            ivs.append((dict(a, intensity_rate=8e6), dict(b, intensity_rate=-8e6), ivs[-1][3], ivs[-1][3] + 2e-3))
+            t = ivs[-1][3]
+            if shape == "auto" and batch == 0:
+                tuned = s.autotune(ivs)
+            elif shape != "auto" and batch == 0:
+                s.set_tuning(*shape)
+            out.append(s.process_many(ivs))
+        out.append(s.drain())
+        return np.concatenate(out), tuned
+
+    ref, _ = run((32, 2))
+    assert len(ref) > 100
+    for shape in ((32, 1), (4, 2), (8, 1), "auto"):
+        ev, tuned = run(shape)
+        assert len(ev) == len(ref), shape
+        for f in ref.dtype.names:
+            assert np.array_equal(ev[f], ref[f]), (shape, f)
+        if tuned:
+            assert tuned["rays_per_lane"] in (1, 2) and tuned["cells_per_warp"] in (4, 8, 16, 32)
+            assert tuned["candidates"] >= 4 and tuned["best_ms"] > 0
+    s = EventSensor(scene, phys)
+    with pytest.raises(ValueError):
+        s.set_tuning(3, 2)
+    with pytest.raises(ValueError):
+        s.set_tuning(8, 4)
+
+
 def test_row_band_sensors_reproduce_the_full_sensor():
     """One GPU's share of a split sensor (dvs_sensor_options.row_begin/row_end)
     gives exactly the full sensor's events of those rows."""
