@@ -56,6 +56,11 @@ PHYSIC = dict(threshold_pos=0.2, threshold_neg=0.2, refractory_time=200e-6, read
               photon_shot_noise=1, reset_thermal_noise=0, random_seed=114514, max_events_per_step=16,
               readout_queue_capacity=1000000)
 METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency vs plain path"
+# DRAM bytes (read + write) per pixel-cell of one trace_cells_kernel launch,
+# from the ncu captures summarised in profiles/trace_cells_kernel_orbit_346x260_ss4.md
+# (precision: a 4-cell launch of the same workload, scaled by the cells traced).
+TRACE_DRAM_BYTES_PER_PIXEL_CELL = {"precision": (32344832 + 1251328) / (4 * 921600),
+                                   "orbit": (22470144 + 407428864) / (640 * 89960)}
 
 
 def dist_env():
@@ -209,6 +214,8 @@ def run_gb300(args):
         return interval_array(ivs)
 
     tuning = None
+    if args.rays:
+        sensor.set_tuning(args.cw, args.rays)
     for k in range(args.warmup):
         b = next_batch()
         if k == 0 and args.autotune:
@@ -305,7 +312,10 @@ def run_gb300(args):
         "kernel_ms": {"optics_per_launch": optics_ms, "circuit_per_launch": circuit_ms,
                       "events_total": st["events_ms"]},
         "roofline": {"bound": "hbm", "kernel": "trace_cells_kernel", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": (TRACE_DRAM_BYTES_PER_PIXEL_CELL[args.workload] * n_pix * cells_per_launch
+                                 if args.workload in TRACE_DRAM_BYTES_PER_PIXEL_CELL else None),
+                     "algorithmic_bytes": alg_bytes,
                      "peak_source": "measured" if peaks else "fallback",
                      "note": "traversal is L1-broadcast/ALU bound; bytes = radiance written per launch"},
         "roofline_circuit": {"bound": "hbm", "kernel": "circuit_kernel",
@@ -406,6 +416,7 @@ def main():
     ap.add_argument("--cw", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action="store_true", help="time the packet shapes on the first warm-up batch")
+    ap.add_argument("--rays", type=int, default=0, help="sub-rays per lane: 1, 2 or 4 (0 = default)")
     ap.add_argument("--circuit", default="fp64", choices=["fp64", "fp32"],
                     help="pixel-circuit arithmetic: fp64 (reference) or fp32 (precision mode)")
     args = ap.parse_args()

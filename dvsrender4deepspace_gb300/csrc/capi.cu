@@ -169,7 +169,7 @@ struct dvs_scene {
     v.cy = camera.cy;
     v.coherent_span = coherent_span;
     v.hapke = hapke;
-    v.pairs = 1;
+    v.rays = 2;
     return v;
   }
   int pixels() const { return camera.width * camera.height; }
@@ -244,11 +244,11 @@ struct dvs_sensor {
   int32_t *own_order = nullptr;      // allocated when the sensor covers a row band
   std::vector<int32_t> band_rank_of_pixel;  // band-local row-major pixel -> rank
   int pixels() const { return n_pix; }
-  int rays_per_lane = 2;  // traversal tuning: 1 or 2 sub-rays per lane (dvs_sensor_set_tuning / autotune)
+  int rays_per_lane = 2;  // traversal tuning: 1, 2 or 4 sub-rays per lane (dvs_sensor_set_tuning / autotune)
   SceneView view() const {
     SceneView v = scene->view();
     v.pixel_of_rank = order;
-    v.pairs = rays_per_lane == 2 ? 1 : 0;
+    v.rays = rays_per_lane;
     return v;
   }
 };
@@ -1243,7 +1243,7 @@ int dvs_sensor_stats_get(const dvs_sensor *s, dvs_sensor_stats *out) {
 int dvs_sensor_set_tuning(dvs_sensor *s, int32_t cells_per_warp, int32_t rays_per_lane) {
   if (!s) return fail(DVS_ERR_INVALID, "null argument");
   if (cells_per_warp < 0 || cells_per_warp > 32 || (cells_per_warp & (cells_per_warp - 1)) ||
-      (rays_per_lane != 1 && rays_per_lane != 2))
+      (rays_per_lane != 1 && rays_per_lane != 2 && rays_per_lane != 4))
     return fail(DVS_ERR_INVALID, "invalid traversal tuning");
   s->opt.cells_per_warp = cells_per_warp;
   s->rays_per_lane = rays_per_lane;
@@ -1263,29 +1263,49 @@ int dvs_sensor_autotune(dvs_sensor *s, const dvs_optical_interval *ivs, size_t c
   size_t chunk;
   int default_log2;
   chunk_shape(s, n_cells, (size_t)n, chunk, default_log2);
-  const int nc = (int)std::min<size_t>(std::min<size_t>(chunk, n_cells), 256);
-  CUDA_TRY(ensure_radiance(s, (size_t)nc), "radiance chunk allocation");
+  const int nc = (int)std::min<size_t>(std::min<size_t>(chunk, n_cells), 64);
+  // four patches of Morton-consecutive pixels spread over the image (at most
+  // 32768 pixels in all) keep each timed launch short at any resolution
+  const int n_sub = std::min(n, 32768), patch = n_sub / 4;
+  std::vector<int32_t> ranks(n_sub);
+  for (int i = 0; i < n_sub; ++i) {
+    const int p = std::min(3, i / std::max(1, patch)), off = i - p * patch;
+    ranks[i] = n_sub == n ? i : std::min(n - 1, (int)((2 * p + 1) * (long long)n / 8) + off);
+  }
+  int32_t *d_ranks = nullptr;
+  CUDA_TRY(cudaMalloc(&d_ranks, sizeof(int32_t) * n_sub), "autotune pixels");
+  cudaError_t cerr = cudaMemcpy(d_ranks, ranks.data(), sizeof(int32_t) * n_sub, cudaMemcpyHostToDevice);
+  if (cerr == cudaSuccess) cerr = ensure_radiance(s, (size_t)nc);
+  if (cerr != cudaSuccess) {
+    cudaFree(d_ranks);
+    return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in autotune : ") + cudaGetErrorString(cerr));
+  }
   const int ss2 = s->scene->samples * s->scene->samples;
   cudaEvent_t e0, e1;
-  CUDA_TRY(cudaEventCreate(&e0), "autotune timer");
-  CUDA_TRY(cudaEventCreate(&e1), "autotune timer");
+  if ((cerr = cudaEventCreate(&e0)) != cudaSuccess || (cerr = cudaEventCreate(&e1)) != cudaSuccess) {
+    cudaFree(d_ranks);
+    return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in autotune timer : ") + cudaGetErrorString(cerr));
+  }
   SceneView view = s->view();
   float best = -1, def_ms = -1;
   int best_log2 = default_log2, best_rays = s->rays_per_lane, tried = 0;
   cudaError_t err = cudaSuccess;
-  for (int rays = 1; rays <= 2 && err == cudaSuccess; ++rays) {
-    if (rays == 2 && ss2 % 2) break;
-    view.pairs = rays == 2;
+  for (int rays = 1; rays <= 4 && err == cudaSuccess; rays *= 2) {
+    if (ss2 % rays) break;
+    view.rays = rays;
     for (int lg = 2; lg <= 5 && err == cudaSuccess; ++lg) {
       if ((1 << lg) > nc && lg > 2) break;
-      float ms = 0;
-      for (int rep = 0; rep < 2 && err == cudaSuccess; ++rep) {  // first launch warms caches
+      float ms = -1;
+      for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {  // the first launch warms caches
+        float t = 0;
         err = cudaEventRecord(e0, s->stream);
         if (err == cudaSuccess)
-          err = launch_trace_cells(view, n, s->poses, 0, nc, lg, s->radiance, nullptr, nullptr, s->stream);
+          err = launch_trace_list(view, n_sub, d_ranks, s->poses, 0, nc, lg, s->radiance, nullptr, nullptr,
+                                  s->stream);
         if (err == cudaSuccess) err = cudaEventRecord(e1, s->stream);
         if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+        if (rep > 0 && (ms < 0 || t < ms)) ms = t;
       }
       if (err != cudaSuccess) break;
       ++tried;
@@ -1299,7 +1319,13 @@ int dvs_sensor_autotune(dvs_sensor *s, const dvs_optical_interval *ivs, size_t c
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaFree(d_ranks);
   if (err != cudaSuccess) return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in autotune : ") + cudaGetErrorString(err));
+  if (def_ms > 0 && best > 0.97f * def_ms) {  // keep the current shape unless another is clearly faster
+    best = def_ms;
+    best_log2 = default_log2;
+    best_rays = s->rays_per_lane;
+  }
   s->opt.cells_per_warp = 1 << best_log2;
   s->rays_per_lane = best_rays;
   out->cells_per_warp = 1 << best_log2;

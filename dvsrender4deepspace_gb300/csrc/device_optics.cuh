@@ -914,13 +914,12 @@ __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], 
   __syncwarp();
 }
 
-// sample_pixel_packet with two neighbouring sub-rays per lane (ss^2 even).
-// The per-ray work, the order of the FP64 radiance and depth sums and the
-// ray counts are those of the one-ray loop.
-template <int kMode>
-__device__ PixelSample sample_pixel_pairs(const SceneView &S, int pixel, bool active, const CellPose &pose,
+// sample_pixel_packet with R neighbouring sub-rays per lane (ss^2 a multiple
+// of R).  The per-ray work, the order of the FP64 radiance and depth sums and
+// the ray counts are those of the one-ray loop.
+template <int kMode, int R>
+__device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool active, const CellPose &pose,
                                           int *stack_code, float *stack_t, const double *cos4_table) {
-  constexpr int R = 2;
   PixelSample out{0.0, -1.0f, true, 0u, 0u};
   double depth = 0;
   int valid_depth = 0;
@@ -985,7 +984,10 @@ __device__ PixelSample sample_pixel_pairs(const SceneView &S, int pixel, bool ac
       }
     }
     if (kMode != kDepthOnly) {
-      if (__any_sync(kFull, lit[0] || lit[1])) {
+      bool any_lit = false;
+#pragma unroll
+      for (int r = 0; r < R; ++r) any_lit = any_lit || lit[r];
+      if (__any_sync(kFull, any_lit)) {
         bool occ[R];
         trace_shadow_packet_r<R>(S, sorigin, light, lit, self, stack_code, stack_t, occ);
 #pragma unroll

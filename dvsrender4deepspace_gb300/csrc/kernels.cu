@@ -70,18 +70,20 @@ constexpr int kWarpsPerBlock = 4;  // all ray kernels launch 128 threads
 #define DVS_TRACE_MIN_BLOCKS 5
 #endif
 constexpr int kCos4Table = 256;    // sub-rays per pixel with a shared cos^4 table (ss <= 16)
-// Two sub-rays per lane when a pixel has an even number of them; that
-// kernel carries twice the ray state and is compiled for 4 blocks per SM
-// (128 registers).
-#ifndef DVS_TRACE_PAIRS
-#define DVS_TRACE_PAIRS 1
-#endif
+// Several sub-rays per lane (SceneView::rays: 1, 2 or 4, when the pixel's
+// sub-ray count is a multiple): the kernels with more ray state per lane are
+// compiled for fewer resident blocks (more registers).
 #ifndef DVS_TRACE_PAIR_MIN_BLOCKS
 #define DVS_TRACE_PAIR_MIN_BLOCKS 4
 #endif
+#ifndef DVS_TRACE_QUAD_MIN_BLOCKS
+#define DVS_TRACE_QUAD_MIN_BLOCKS 3
+#endif
 
-template <int kMode, bool kPairs>
-__global__ void __launch_bounds__(128, kPairs ? DVS_TRACE_PAIR_MIN_BLOCKS : DVS_TRACE_MIN_BLOCKS)
+template <int kMode, int kRays>
+__global__ void __launch_bounds__(128, kRays == 4   ? DVS_TRACE_QUAD_MIN_BLOCKS
+                                       : kRays == 2 ? DVS_TRACE_PAIR_MIN_BLOCKS
+                                                    : DVS_TRACE_MIN_BLOCKS)
     trace_cells_kernel(SceneView S, int n_pix,
                                                                                 const int32_t *rank_list,
                                                           const CellPose *poses, int c0, int nc, int cw_log2,
@@ -112,10 +114,10 @@ __global__ void __launch_bounds__(128, kPairs ? DVS_TRACE_PAIR_MIN_BLOCKS : DVS_
     __syncwarp();
   }
   const PixelSample s =
-      kPairs ? sample_pixel_pairs<kMode>(S, pixel, active, pose, s_code[wib], s_t[wib],
-                                         shared_cos4 ? s_cos4[wib] : nullptr)
-             : sample_pixel_packet<kMode>(S, pixel, active, pose, s_code[wib], s_t[wib],
-                                          shared_cos4 ? s_cos4[wib] : nullptr);
+      kRays > 1 ? sample_pixel_group<kMode, kRays>(S, pixel, active, pose, s_code[wib], s_t[wib],
+                                                   shared_cos4 ? s_cos4[wib] : nullptr)
+                : sample_pixel_packet<kMode>(S, pixel, active, pose, s_code[wib], s_t[wib],
+                                             shared_cos4 ? s_cos4[wib] : nullptr);
   if (active) {
     const size_t o = (size_t)cell * n_pix + rank;
     radiance[o] = s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll);
@@ -347,23 +349,22 @@ cudaError_t launch_trace_list(const SceneView &scene, int n_pix, const int32_t *
   if (n_pix <= 0 || nc <= 0) return cudaSuccess;
   const int cw = 1 << cw_log2, ppw = 32 >> cw_log2;
   const long long warps = (long long)((n_pix + ppw - 1) / ppw) * ((nc + cw - 1) / cw);
-  const bool pairs = DVS_TRACE_PAIRS && scene.pairs && (scene.samples * scene.samples) % 2 == 0;
+  const int ss2 = scene.samples * scene.samples;
+  const int rays = (scene.rays >= 4 && ss2 % 4 == 0) ? 4 : (scene.rays >= 2 && ss2 % 2 == 0) ? 2 : 1;
   const int grid = blocks(warps * 32, 128);
+#define DVS_TRACE_LAUNCH(MODE, RAYS, DEPTH)                                                                  \
+  trace_cells_kernel<MODE, RAYS><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2, radiance, \
+                                                      DEPTH, counters)
   if (depth) {
-    if (pairs)
-      trace_cells_kernel<kRadianceDepth, true><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2,
-                                                                    radiance, depth, counters);
-    else
-      trace_cells_kernel<kRadianceDepth, false><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2,
-                                                                     radiance, depth, counters);
+    if (rays == 4) DVS_TRACE_LAUNCH(kRadianceDepth, 4, depth);
+    else if (rays == 2) DVS_TRACE_LAUNCH(kRadianceDepth, 2, depth);
+    else DVS_TRACE_LAUNCH(kRadianceDepth, 1, depth);
   } else {
-    if (pairs)
-      trace_cells_kernel<kRadiance, true><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2,
-                                                               radiance, nullptr, counters);
-    else
-      trace_cells_kernel<kRadiance, false><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2,
-                                                                radiance, nullptr, counters);
+    if (rays == 4) DVS_TRACE_LAUNCH(kRadiance, 4, nullptr);
+    else if (rays == 2) DVS_TRACE_LAUNCH(kRadiance, 2, nullptr);
+    else DVS_TRACE_LAUNCH(kRadiance, 1, nullptr);
   }
+#undef DVS_TRACE_LAUNCH
   return cudaGetLastError();
 }
 

@@ -17,7 +17,7 @@ struct SceneView {
   float fx, fy, cx, cy;
   float coherent_span;  // largest origin spread a warp packet traverses as one interval bundle
   dvs_hapke hapke;
-  int32_t pairs;        // a lane may carry two sub-rays (used when samples^2 is even)
+  int32_t rays;         // sub-rays a lane may carry: 1, 2 or 4 (used when samples^2 is a multiple)
 };
 
 // Camera state at one circuit-cell midpoint, already interpolated

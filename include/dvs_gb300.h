@@ -265,17 +265,19 @@ int dvs_readout_read(dvs_readout *readout, dvs_event *out, size_t capacity, size
 int dvs_readout_counters(const dvs_readout *readout, uint64_t *dropped, uint64_t *peak_queue);
 
 /* Traversal packet shape: cells_per_warp 1..32 (power of two; 0 = automatic)
- * and rays_per_lane 1 or 2 (two neighbouring sub-rays per lane when the pixel
- * has an even number of them; the default). */
+ * and rays_per_lane 1, 2 (the default) or 4 neighbouring sub-rays per lane,
+ * used when the pixel's sub-ray count is a multiple of it. */
 int dvs_sensor_set_tuning(dvs_sensor *sensor, int32_t cells_per_warp, int32_t rays_per_lane);
 typedef struct {
   int32_t cells_per_warp, rays_per_lane;  /* the shape chosen and now set */
   int32_t candidates, cells_timed;        /* shapes timed, circuit cells in the timed launch */
   double best_ms, default_ms;             /* trace time of the chosen shape and of the previous one */
 } dvs_tuning;
-/* Autotuner: times the trace of a prefix of the next batch (the intervals
- * dvs_sensor_process/enqueue will be given next) for each packet shape and
- * sets the fastest.  Runs optics only: no circuit state, RNG or time changes. */
+/* Autotuner: times the trace of a prefix (up to 64 circuit cells) of the next
+ * batch (the intervals dvs_sensor_process/enqueue will be given next) over a
+ * patch of up to 32768 pixels from the middle of the image, for each packet
+ * shape, and sets the fastest.  Runs optics only: no circuit state, RNG or
+ * time changes. */
 int dvs_sensor_autotune(dvs_sensor *sensor, const dvs_optical_interval *intervals, size_t n_intervals,
                         dvs_tuning *out);
 /* Device memory the sensor holds now (state, RNG, event slabs, radiance

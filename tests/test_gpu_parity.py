@@ -373,19 +373,19 @@ def test_packet_shape_and_autotuner_do_not_change_events():
 
     ref, _ = run((32, 2))
     assert len(ref) > 100
-    for shape in ((32, 1), (4, 2), (8, 1), "auto"):
+    for shape in ((32, 1), (4, 2), (8, 1), (16, 4), "auto"):
         ev, tuned = run(shape)
         assert len(ev) == len(ref), shape
         for f in ref.dtype.names:
             assert np.array_equal(ev[f], ref[f]), (shape, f)
         if tuned:
-            assert tuned["rays_per_lane"] in (1, 2) and tuned["cells_per_warp"] in (4, 8, 16, 32)
+            assert tuned["rays_per_lane"] in (1, 2, 4) and tuned["cells_per_warp"] in (4, 8, 16, 32)
             assert tuned["candidates"] >= 4 and tuned["best_ms"] > 0
     s = EventSensor(scene, phys)
     with pytest.raises(ValueError):
         s.set_tuning(3, 2)
     with pytest.raises(ValueError):
-        s.set_tuning(8, 4)
+        s.set_tuning(8, 3)
 
 
 def test_row_band_sensors_reproduce_the_full_sensor():
