@@ -20,6 +20,7 @@ collective on the data path.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -253,6 +254,32 @@ def run_gb300(args):
     st2 = sensor.stats()
     rays2 = st2["primary_rays"] + st2["shadow_rays"]
     gen2 = st2["events_generated"]
+    # ---- adaptive optical solver over a longer window (the app's solver for
+    # long sequences, apps/main_dvs.cpp:54,106-113): simulated seconds per wall
+    # second and events per wall second, 200 horizons per call
+    adaptive = None
+    if args.adaptive_ms > 0:
+        ab = 200
+        n_calls = int(math.ceil(args.adaptive_ms * 1e-3 / (float(np.float32(dt)) * ab) - 1e-9))
+        sim0, ev_a, rejected = t_cursor[0], 0, 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(n_calls):
+            ivs = trajectory.horizons(traj, t_cursor[0], dt, ab)
+            arr = interval_array(ivs)
+            r = sensor.process_adaptive(arr, 1e-2, check_convergence=(k == 0))
+            if r is None:  # rejected window: the native solver takes it
+                rejected += 1
+                r = sensor.process_many(arr)
+            t_cursor[0] = ivs[-1][3]
+            ev_a += len(r)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        adaptive = {"simulated_s": t_cursor[0] - sim0, "wall_s": wall,
+                    "simulated_s_per_wall_s": (t_cursor[0] - sim0) / wall, "events": ev_a,
+                    "events_per_s": ev_a / wall, "calls": n_calls, "horizons_per_call": ab,
+                    "rejected_windows": rejected, "refinement": sensor.refinement_statistics(),
+                    "knot_capacity": sensor.adaptive_cache_capacity()}
     # max over ranks
     vals = torch.tensor([dev_ms, e2e_s, rays, rays2, st2["events_delivered"]], dtype=torch.float64, device="cuda")
     if world > 1:
@@ -295,7 +322,8 @@ def run_gb300(args):
         "config": {"workload": args.workload, "pixels": n_pix, "width": w["camera"]["width"],
                    "height": w["camera"]["height"], "supersample": w["ss"], "terrain_grid": w["grid"],
                    "triangles": int(info["triangles"]), "horizons_per_step": B, "time_resolution": dt,
-                   "circuit_step": PHYSIC["circuit_step"], "shot_noise": "curand_xorwow", "sun_elevation_deg":
+                   "circuit_step": PHYSIC["circuit_step"],
+                   "shot_noise": "philox" if args.circuit == "fp32-philox" else "curand_xorwow", "sun_elevation_deg":
                    w["sun_elevation"], "intensity": w["intensity"], "l2": "inputs larger than L2 (scene %.1f GB)"
                    % (info["device_bytes"] / 1e9), "parallelism": "dp%d (independent jobs)" % world,
                    "bvh": "8-wide Morton radix, leaf %d, depth %d" % (info["leaf_size"], info["depth"]),
@@ -322,6 +350,7 @@ def run_gb300(args):
                              "achieved": circuit_bytes / (circuit_ms / 1e3) / 1e9 if circuit_ms > 0 else None,
                              "peak": peak, "unit": "GB/s"},
         "clocks": clocks.summary(), "setup_s": setup_s, "bvh_build_s": info["build_seconds"], "tuning": tuning,
+        "adaptive": adaptive,
         "cpu_baseline": cb,
     }
     if line["roofline_circuit"]["achieved"]:
@@ -417,7 +446,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--autotune", action="store_true", help="time the packet shapes on the first warm-up batch")
     ap.add_argument("--rays", type=int, default=0, help="sub-rays per lane: 1, 2 or 4 (0 = default)")
-    ap.add_argument("--circuit", default="fp64", choices=["fp64", "fp32"],
+    ap.add_argument("--adaptive-ms", type=float, default=2.0,
+                    help="also run the adaptive optical solver over this many simulated milliseconds")
+    ap.add_argument("--circuit", default="fp64", choices=["fp64", "fp32", "fp32-philox"],
                     help="pixel-circuit arithmetic: fp64 (reference) or fp32 (precision mode)")
     args = ap.parse_args()
     if args.impl == "reference":

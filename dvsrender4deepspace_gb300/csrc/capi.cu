@@ -595,8 +595,8 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
       (long long)n * physic->max_events_per_step > std::numeric_limits<int>::max())
     return fail(DVS_ERR_INVALID, "invalid sensor capacity");
   if (!(physic->circuit_step > 0)) return fail(DVS_ERR_INVALID, "invalid optical/circuit model parameter range");
-  if (opt.circuit_precision != 0 && opt.circuit_precision != 1)
-    return fail(DVS_ERR_INVALID, "circuit precision must be 0 (FP64) or 1 (FP32)");
+  if (opt.circuit_precision < 0 || opt.circuit_precision > 2)
+    return fail(DVS_ERR_INVALID, "circuit precision must be 0 (FP64), 1 (FP32) or 2 (FP32 with Philox noise)");
   dvs_sensor *s = new dvs_sensor;
   s->scene = scene;
   s->physic = *physic;
@@ -604,7 +604,9 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
   s->n_pix = n;
   s->order = scene->pixel_of_rank;
   derive(*physic, s->opt.physic_effects != 0, s->p, s->photo);
-  s->photo.fp32_circuit = s->opt.circuit_precision;
+  s->photo.fp32_circuit = s->opt.circuit_precision >= 1;
+  s->photo.philox = s->opt.circuit_precision == 2;
+  s->photo.seed = (uint32_t)physic->random_seed;
   s->threshold_std = s->opt.physic_effects ? physic->threshold_std : 0;
   s->threshold_min = physic->threshold_min;
   s->max_events = physic->max_events_per_step;
@@ -644,6 +646,7 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
   ALLOC(s->st.threshold_neg, sizeof(double) * n, "pixel states");
   ALLOC(s->st.reset_pending, sizeof(int8_t) * n, "pixel states");
   ALLOC(s->st.rng, sizeof(curandStateXORWOW_t) * n, "pixel RNG");
+  s->st.pixel = s->order;
   ALLOC(s->ev_count, sizeof(int32_t) * n, "event counts");
   ALLOC(s->slab_t, sizeof(double) * (size_t)n * s->max_events, "event slabs");
   ALLOC(s->slab_p, sizeof(int8_t) * (size_t)n * s->max_events, "event slabs");
@@ -1039,6 +1042,8 @@ int dvs_sensor_process_adaptive(dvs_sensor *s, const dvs_optical_interval *ivs, 
   if (accepted) *accepted = 0;
   if (n_ready) *n_ready = 0;
   if (!s || !ivs || count == 0) return fail(DVS_ERR_INVALID, "empty adaptive optical horizon");
+  if (s->photo.philox)
+    return fail(DVS_ERR_INVALID, "adaptive optics draws the reference's XORWOW stream; use circuit precision 0 or 1");
   const double start = ivs[0].t0, end = ivs[count - 1].t1;
   if (!std::isfinite(tolerance) || tolerance <= 0 || s->p.refractory_time <= 0 ||
       (end - start) / s->p.refractory_time + 2 > s->max_events)

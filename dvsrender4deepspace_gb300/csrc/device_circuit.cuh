@@ -126,46 +126,51 @@ struct PixelRegsF {
   bool reset_pending;
 };
 
-__device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, double rate_d, double t0, double t1,
-                                 double *out_t, int8_t *out_p, int capacity, curandStateXORWOW_t &rng) {
-  if (t1 <= t0) return 0;
-  const float rate = (float)rate_d, charge = (float)p.charge_scale, leak = (float)p.reference_leak;
+// Time inside the cell is an FP32 offset from the cell start (t0) and the
+// refractory deadline an FP32 offset too, so the no-event path has no FP64
+// arithmetic; absolute event times and deadlines are formed in FP64 only
+// when an event happens.
+template <class Rng>
+__device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, float rate, double t0, float dt,
+                                 double *out_t, int8_t *out_p, int capacity, Rng &rng) {
+  if (!(dt > 0)) return 0;
+  const float charge = (float)p.charge_scale, leak = (float)p.reference_leak;
   int count = 0;
-  double cursor = t0;
+  float off = 0.0f, ref_off = (float)(s.refractory_until - t0);
   float u = s.receptor_log;
   int passes = 0;
-  while (cursor < t1) {
+  while (off < dt) {
     if (++passes > 4096) return -2;  // bounded: see kErrStalled
-    if (cursor < s.refractory_until) {
-      const double end = fmin(t1, s.refractory_until);
-      u = receptor_log_at_f(u, rate, (float)(end - cursor), charge);
-      cursor = end;
+    if (off < ref_off) {
+      const float end = fminf(dt, ref_off);
+      u = receptor_log_at_f(u, rate, end - off, charge);
+      off = end;
       s.reference_log = u;
-      if (cursor < t1 || cursor == s.refractory_until) {
-        if (cursor >= s.refractory_until && s.reset_pending) {
+      if (off < dt || off == ref_off) {
+        if (off >= ref_off && s.reset_pending) {
           if (p.reset_noise_std > 0) s.reference_log += (float)(p.reset_noise_std * curand_normal_double(&rng));
           s.reset_pending = false;
         }
       }
-      if (cursor >= t1) break;
+      if (off >= dt) break;
     } else if (s.reset_pending) {
       if (p.reset_noise_std > 0) s.reference_log += (float)(p.reset_noise_std * curand_normal_double(&rng));
       s.reset_pending = false;
     }
-    const double remaining = t1 - cursor;
-    double boundary = remaining;
+    const float remaining = dt - off;
+    float boundary = remaining;
     if (leak > 0) {  // leak extremum in FP64 (it places the segment end)
-      const double x = exp((double)u), target = rate_d + p.charge_scale * p.reference_leak;
+      const double rate_d = rate, x = exp((double)u), target = rate_d + p.charge_scale * p.reference_leak;
       if (x > target && target > rate_d) {
         double extremum;
         if (rate_d > 0) extremum = -p.charge_scale / rate_d * log((1.0 / target - 1.0 / rate_d) / (1.0 / x - 1.0 / rate_d));
         else extremum = p.charge_scale * (1.0 / target - 1.0 / x);
-        if (extremum > 1e-15 && extremum < boundary) boundary = extremum;
+        if (extremum > 1e-15 && extremum < (double)boundary) boundary = (float)extremum;
       }
     }
     const float c0 = u - s.reference_log;
-    const float ub = receptor_log_at_f(u, rate, (float)boundary, charge);
-    const float cb = ub - s.reference_log + leak * (float)boundary;
+    const float ub = receptor_log_at_f(u, rate, boundary, charge);
+    const float cb = ub - s.reference_log + leak * boundary;
     int polarity = -1;
     float level = 0;
     if (c0 >= s.threshold_pos) { polarity = 1; level = s.threshold_pos; }
@@ -174,14 +179,14 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, double rat
     else if (cb <= -s.threshold_neg) { polarity = 0; level = -s.threshold_neg; }
     if (polarity < 0) {
       u = ub;
-      s.reference_log -= leak * (float)boundary;
-      cursor += boundary;
+      s.reference_log -= leak * boundary;
+      off = boundary == remaining ? dt : off + boundary;
       continue;
     }
     if (count == capacity) return -1;
     // crossing time in FP64 from the FP32 state
-    const double ud = u, refd = s.reference_log, leveld = level;
-    double lo = 0, hi = boundary;
+    const double rate_d = rate, ud = u, refd = s.reference_log, leveld = level, bnd = boundary;
+    double lo = 0, hi = bnd;
     if (c0 >= s.threshold_pos || c0 <= -s.threshold_neg) hi = 0;
     else if (p.reference_leak == 0) {
       const double target_inverse = exp(-(refd + leveld)), initial_inverse = exp(-ud);
@@ -189,7 +194,7 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, double rat
         const double stationary_inverse = 1.0 / rate_d;
         hi = -p.charge_scale / rate_d * log1p((target_inverse - initial_inverse) / (initial_inverse - stationary_inverse));
       } else hi = p.charge_scale * (target_inverse - initial_inverse);
-      hi = fmin(boundary, fmax(0.0, hi));
+      hi = fmin(bnd, fmax(0.0, hi));
     } else
       for (int j = 0; j < 48; ++j) {
         const double mid = (lo + hi) * .5;
@@ -197,16 +202,51 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, double rat
         if (polarity ? cm >= leveld : cm <= leveld) hi = mid; else lo = mid;
       }
     u = (float)receptor_log_at(ud, rate_d, hi, p.charge_scale);
-    cursor += hi;
-    out_t[count] = cursor;
+    const double t_event = t0 + (double)off + hi;
+    off = fminf(dt, off + (float)hi);
+    out_t[count] = t_event;
     out_p[count] = (int8_t)polarity;
     ++count;
     s.reference_log = u;
-    s.refractory_until = cursor + p.refractory_time;
+    s.refractory_until = t_event + p.refractory_time;
+    ref_off = (float)(s.refractory_until - t0);
     s.reset_pending = true;
   }
   s.receptor_log = u;
   return count;
+}
+
+// Photon count of one cell from a counter-based Philox stream (precision
+// mode): inversion of the Poisson CDF by sequential search for small means
+// (the photon-starved regime of the sensor), a rounded normal approximation
+// above 64 electrons.  The stream is keyed by (seed, pixel) and placed at the
+// cell's absolute index, so the draws do not depend on how cells are batched.
+__device__ __forceinline__ float poisson_electrons_philox(curandStatePhilox4_32_10_t &st, float lambda) {
+  if (!(lambda > 0)) return 0;
+  if (lambda > 64) return fmaxf(0.0f, floorf(lambda + sqrtf(lambda) * curand_normal(&st) + 0.5f));
+  const float u = curand_uniform(&st);  // (0, 1]
+  float p = expf(-lambda), F = p;
+  int k = 0;
+  while (u > F && k < 512) {
+    ++k;
+    p *= lambda / (float)k;
+    if (!(p > 0.0f)) break;  // the CDF stopped growing in float
+    F += p;
+  }
+  return (float)k;
+}
+// The pixel's Philox stream at a place fixed by the cell's start time: a
+// 64-bit mix (the SplitMix64 finalizer) of the bits of t0, aligned to 16
+// draws, so distinct cells get disjoint draws whatever their length and
+// however they are batched.  Offsets 0..15 belong to the initialization.
+__device__ __forceinline__ curandStatePhilox4_32_10_t philox_at(unsigned seed, int pixel, double cell_t0) {
+  unsigned long long z = (unsigned long long)__double_as_longlong(cell_t0) + 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  curandStatePhilox4_32_10_t st;
+  curand_init(seed, (unsigned long long)pixel, (z | 16ull) & ~15ull, &st);
+  return st;
 }
 
 // poisson_electrons (include/dvs/photon_noise.cuh:4-9): cuRAND draws in the

@@ -18,6 +18,7 @@
 //   * emit_events: warp prefix-sum compaction of the per-pixel event slabs.
 //   * event_depth: depth re-trace at each event time (event_sensor.cu:51-59).
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <curand_kernel.h>
 
@@ -130,19 +131,21 @@ __global__ void __launch_bounds__(128, kRays == 4   ? DVS_TRACE_QUAD_MIN_BLOCKS
   }
 }
 
+template <class Rng>
 __global__ void init_pixels_kernel(int n, const int32_t *pixel_of_rank, const double *radiance, PixelParams p,
                                    PhotoParams photo, double stddev, double minimum, unsigned seed, CircuitState st,
                                    int32_t *error) {
-  // initialize_pixels (event_sensor.cu:18-28)
+  // initialize_pixels (event_sensor.cu:18-28); Rng = XORWOW (the reference's
+  // generator) or, in precision mode, the head of the pixel's Philox stream
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int pixel = pixel_of_rank[k];
-  curandStateXORWOW_t rng;
+  Rng rng;
   curand_init(seed, pixel, 0, &rng);
   const double rad = radiance[k];
   if (!isfinite(rad)) {
     atomicOr(error, kErrOptical);
-    st.rng[k] = rng;
+    if constexpr (std::is_same<Rng, curandStateXORWOW_t>::value) st.rng[k] = rng;
     return;
   }
   const double u = log(fmax(1e-30, rad * photo.electrons_per_radiance + photo.dark_electrons));
@@ -152,10 +155,10 @@ __global__ void init_pixels_kernel(int n, const int32_t *pixel_of_rank, const do
   st.threshold_pos[k] = fmax(minimum, p.threshold_pos + stddev * curand_normal_double(&rng));
   st.threshold_neg[k] = fmax(minimum, p.threshold_neg + stddev * curand_normal_double(&rng));
   st.reset_pending[k] = 0;
-  st.rng[k] = rng;
+  if constexpr (std::is_same<Rng, curandStateXORWOW_t>::value) st.rng[k] = rng;
 }
 
-template <bool kF32>
+template <bool kF32, bool kPhilox>
 __global__ void __launch_bounds__(128) circuit_kernel(int n, const int32_t *rank_list, const Cell *cells, int c0,
                                                       int nc, const double *radiance, PixelParams p,
                                                       PhotoParams photo, int max_events, CircuitState st,
@@ -168,7 +171,7 @@ __global__ void __launch_bounds__(128) circuit_kernel(int n, const int32_t *rank
   const int k = rank_list ? rank_list[r] : r;
   int cnt = ev_count[k];
   if (cnt < 0) return;  // failed earlier in this batch
-  const bool need_rng = photo.shot_noise || p.reset_noise_std > 0;
+  const bool need_rng = !kPhilox && (photo.shot_noise || p.reset_noise_std > 0);
   curandStateXORWOW_t rng;
   if (need_rng) rng = st.rng[k];
   double *my_t = slab_t + (size_t)k * max_events;
@@ -197,14 +200,23 @@ __global__ void __launch_bounds__(128) circuit_kernel(int n, const int32_t *rank
     // precision mode: the state is held in FP32 registers for the chunk
     PixelRegsF s{(float)st.receptor_log[k], (float)st.reference_log[k], st.refractory_until[k],
                  (float)st.threshold_pos[k], (float)st.threshold_neg[k], st.reset_pending[k] != 0};
+    const int pixel = kPhilox ? st.pixel[k] : 0;
+    const float e_rad = (float)photo.electrons_per_radiance, dark = (float)photo.dark_electrons;
     for (int c = 0; c < nc; ++c) {
       const Cell cell = cells[c0 + c];
       const double rad = radiance[(size_t)c * n + r];
       if (!isfinite(rad)) { failed = kErrOptical; break; }
-      double rate = rad * photo.electrons_per_radiance + photo.dark_electrons;
-      const double t0 = cell.t0, t1 = cell.t1;
-      if (photo.shot_noise) rate = poisson_electrons(rng, rate * (t1 - t0)) / (t1 - t0);
-      const int emitted = advance_pixel_f32(s, p, rate, t0, t1, my_t + cnt, my_p + cnt, max_events - cnt, rng);
+      float rate = (float)rad * e_rad + dark;
+      const float dt = (float)(cell.t1 - cell.t0);
+      int emitted;
+      if (kPhilox) {
+        curandStatePhilox4_32_10_t ph = philox_at(photo.seed, pixel, cell.t0);
+        if (photo.shot_noise) rate = poisson_electrons_philox(ph, rate * dt) / dt;
+        emitted = advance_pixel_f32(s, p, rate, cell.t0, dt, my_t + cnt, my_p + cnt, max_events - cnt, ph);
+      } else {
+        if (photo.shot_noise) rate = (float)poisson_electrons(rng, (double)(rate * dt)) / dt;
+        emitted = advance_pixel_f32(s, p, rate, cell.t0, dt, my_t + cnt, my_p + cnt, max_events - cnt, rng);
+      }
       if (emitted == -1) { failed = kErrCapacity; break; }
       if (emitted == -2) { failed = kErrStalled; break; }
       cnt += emitted;
@@ -376,8 +388,12 @@ cudaError_t launch_trace_cells(const SceneView &scene, int n_pix, const CellPose
 cudaError_t launch_init_pixels(int n, const int32_t *pixel_of_rank, const double *radiance, PixelParams p,
                                PhotoParams photo, double stddev, double minimum, unsigned seed, CircuitState st,
                                int32_t *error, cudaStream_t s) {
-  init_pixels_kernel<<<blocks(n, 128), 128, 0, s>>>(n, pixel_of_rank, radiance, p, photo, stddev, minimum, seed, st,
-                                                    error);
+  if (photo.philox)
+    init_pixels_kernel<curandStatePhilox4_32_10_t><<<blocks(n, 128), 128, 0, s>>>(n, pixel_of_rank, radiance, p, photo,
+                                                                                stddev, minimum, seed, st, error);
+  else
+    init_pixels_kernel<curandStateXORWOW_t><<<blocks(n, 128), 128, 0, s>>>(n, pixel_of_rank, radiance, p, photo, stddev,
+                                                                         minimum, seed, st, error);
   return cudaGetLastError();
 }
 
@@ -386,12 +402,16 @@ cudaError_t launch_circuit_list(int n, const int32_t *rank_list, const Cell *cel
                                 CircuitState st, int32_t *ev_count, double *slab_t, int8_t *slab_p, int32_t *error,
                                 unsigned long long *counters, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  if (photo.fp32_circuit)
-    circuit_kernel<true><<<blocks(n, 128), 128, 0, s>>>(n, rank_list, cells, c0, nc, radiance, p, photo, max_events,
-                                                        st, ev_count, slab_t, slab_p, error, counters);
+  if (photo.fp32_circuit && photo.philox)
+    circuit_kernel<true, true><<<blocks(n, 128), 128, 0, s>>>(n, rank_list, cells, c0, nc, radiance, p, photo,
+                                                              max_events, st, ev_count, slab_t, slab_p, error, counters);
+  else if (photo.fp32_circuit)
+    circuit_kernel<true, false><<<blocks(n, 128), 128, 0, s>>>(n, rank_list, cells, c0, nc, radiance, p, photo,
+                                                               max_events, st, ev_count, slab_t, slab_p, error, counters);
   else
-    circuit_kernel<false><<<blocks(n, 128), 128, 0, s>>>(n, rank_list, cells, c0, nc, radiance, p, photo, max_events,
-                                                         st, ev_count, slab_t, slab_p, error, counters);
+    circuit_kernel<false, false><<<blocks(n, 128), 128, 0, s>>>(n, rank_list, cells, c0, nc, radiance, p, photo,
+                                                                max_events, st, ev_count, slab_t, slab_p, error,
+                                                                counters);
   return cudaGetLastError();
 }
 

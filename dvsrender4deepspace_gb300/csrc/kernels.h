@@ -42,6 +42,8 @@ struct PhotoParams {
   double electrons_per_radiance, dark_electrons, integration_step;
   int32_t shot_noise;
   int32_t fp32_circuit;  // receptor/contrast arithmetic in FP32 (times and crossing solves stay FP64)
+  int32_t philox;        // counter-based Philox noise keyed by (seed, pixel, cell index) instead of XORWOW
+  uint32_t seed;
 };
 
 // Pixel-circuit state, structure of arrays indexed by Morton rank.
@@ -49,6 +51,7 @@ struct CircuitState {
   double *receptor_log, *reference_log, *refractory_until, *threshold_pos, *threshold_neg;
   int8_t *reset_pending;
   curandStateXORWOW_t *rng;
+  const int32_t *pixel;  // rank -> row-major pixel of the full image (the noise streams' key)
 };
 
 // Generated event before readout, aligned for device stores.

@@ -158,9 +158,10 @@ class EventSensor:
         opt.timing = int(timing)
         opt.row_begin = int(row_begin)
         opt.row_end = int(row_end)
-        if circuit_precision not in ("fp64", "fp32"):
-            raise ValueError("circuit_precision must be fp64 or fp32")
-        opt.circuit_precision = 1 if circuit_precision == "fp32" else 0
+        modes = {"fp64": 0, "fp32": 1, "fp32-philox": 2}
+        if circuit_precision not in modes:
+            raise ValueError("circuit_precision must be fp64, fp32 or fp32-philox")
+        opt.circuit_precision = modes[circuit_precision]
         h = C.c_void_p()
         check(lib.dvs_sensor_create(scene.handle, C.byref(physic_struct(physic)), C.byref(opt), C.byref(h)))
         self.handle = h

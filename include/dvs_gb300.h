@@ -102,7 +102,9 @@ typedef struct {
   int32_t row_begin, row_end; /* rows [row_begin, row_end) only (one GPU's share); 0,0 = all */
   int32_t circuit_precision;  /* 0: FP64 pixel circuit (reference arithmetic); 1: FP32 receptor and
                                  contrast arithmetic, FP64 times, refractory deadlines and crossing-time
-                                 solves (precision mode; no counterpart in the reference) */
+                                 solves (precision mode; no counterpart in the reference); 2: as 1 with
+                                 counter-based Philox noise keyed by (seed, pixel, cell index) instead of
+                                 the reference's XORWOW stream (native solver only) */
 } dvs_sensor_options;
 
 typedef struct {

@@ -252,6 +252,44 @@ def test_sensor_batch_invariance(shot):
         np.testing.assert_array_equal(allev[f], individual[f])
 
 
+def test_philox_precision_mode_noise():
+    """circuit_precision = 2 (FP32 circuit, counter-based Philox noise keyed
+    by seed, pixel and cell index): batching cannot change the draws, a seed
+    repeats, row bands reproduce the full sensor, and the event rate agrees
+    with the XORWOW stream's within sampling error."""
+    from dvsrender4deepspace_gb300 import shard
+    scene, phys = plane_sensor(photon_shot_noise=1, threshold_pos=0.03, threshold_neg=0.03, refractory_time=0,
+                               threshold_std=0.02)
+    dim = dict(POSE, intensity=20)  # about 1e-2 photo-electrons per 1 us cell: shot noise dominates
+    ivs = [(dim, dim, 0, 0.0005), (dim, dim, 0.0005, 0.001), (dim, dim, 0.001, 0.002)]
+
+    def run(mode, split, seed=42, rows=(0, 0)):
+        s = EventSensor(scene, dict(phys, random_seed=seed), circuit_precision=mode, row_begin=rows[0],
+                        row_end=rows[1])
+        s.initialize(dim, 0)
+        ev = np.concatenate([s.process(iv) for iv in ivs]) if split else s.process_many(ivs)
+        return np.concatenate([ev, s.drain()])
+
+    a, b = run("fp32-philox", False), run("fp32-philox", True)
+    assert len(a) == len(b) > 1000
+    for f in ("timestamp", "x", "y", "polarity"):
+        np.testing.assert_array_equal(a[f], b[f])
+    c = run("fp32-philox", False, seed=43)
+    assert len(c) != len(a) or not np.array_equal(c["timestamp"], a["timestamp"])
+    bands = [run("fp32-philox", False, rows=r) for r in shard.row_bands(DAVIS["height"], 2)]
+    merged = pixel_sorted(shard.merge_runs(bands))
+    want = pixel_sorted(a)
+    assert len(merged) == len(want)
+    for f in ("timestamp", "x", "y", "polarity"):
+        np.testing.assert_array_equal(merged[f], want[f])
+    x = run("fp32", False)
+    assert abs(len(x) - len(a)) < 6 * math.sqrt(len(x)) + 0.05 * len(x), (len(x), len(a))
+    with pytest.raises(ValueError):
+        s = EventSensor(scene, phys, circuit_precision="fp32-philox")
+        s.initialize(dim, 0)
+        s.process_adaptive(ivs, 1e-2)
+
+
 def test_seeded_shot_noise_repeatable():
     # tests/test_sensor.cu:168-173
     scene, phys = plane_sensor(photon_shot_noise=1, threshold_pos=0.03, threshold_neg=0.03, refractory_time=0)
