@@ -54,13 +54,24 @@ __device__ __forceinline__ double probe(const SceneView &S, int pixel, bool want
 
 __device__ __forceinline__ double segment_fraction(const OpticalKnot *values, int a) { return fabs(values[a].fraction); }
 
-// refine_pixels (optical_sampler.cu:39-84), one pixel per lane.
+// The poses of the five initial probes (0, 1/4, 1/2, 3/4, 1 of the window).
+__global__ void probe_poses_kernel(const dvs_optical_interval *ivs, int n_ivs, double start, double end,
+                                   CellPose *out) {
+  const int j = threadIdx.x;
+  if (j < 5) out[j] = native_pose(ivs, n_ivs, start + (end - start) * j * .25);
+}
+
+// refine_pixels (optical_sampler.cu:39-84), one pixel per lane.  The five
+// initial probes come traced by the native trace kernel (initial[j * n +
+// rank]: every pixel is probed at the same five times, so they are five
+// circuit cells of a temporal warp packet); the bisection probes, which only
+// some pixels need, are traced here.
 __global__ void __launch_bounds__(128) refine_kernel(SceneView S, int n, const dvs_optical_interval *ivs, int n_ivs,
                                                      double start, double end, PhotoParams photo, double tolerance,
                                                      CircuitState st, double charge, int capacity,
-                                                     OpticalKnot *knots, int32_t *counts,
-                                                     unsigned long long *ref_stats, int32_t *error,
-                                                     unsigned long long *counters) {
+                                                     const double *initial_radiance, OpticalKnot *knots,
+                                                     int32_t *counts, unsigned long long *ref_stats,
+                                                     int32_t *error, unsigned long long *counters) {
   __shared__ int s_code[4][kStackSlots];
   __shared__ float s_t[4][kStackSlots];
   const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -73,9 +84,11 @@ __global__ void __launch_bounds__(128) refine_kernel(SceneView S, int n, const d
   bool bad = false;
   unsigned rays = 0;
   double initial[5];
-#pragma unroll 1
-  for (int j = 0; j < 5; ++j)
-    initial[j] = probe(S, pixel, mine, ivs, n_ivs, start + (end - start) * j * .25, sc, stt, bad, rays);
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    initial[j] = mine ? initial_radiance[(size_t)j * n + rank] : 0.0;
+    if (mine && !isfinite(initial[j])) bad = true;
+  }
   RefineEntry stack[kRefineStack];
   int top = 0, written = 0;
   bool fallback = false;
@@ -320,10 +333,18 @@ int sm_count() {
 
 cudaError_t launch_refine(const SceneView &scene, int n, const dvs_optical_interval *ivs, int n_ivs, double start,
                           double end, PhotoParams photo, double tolerance, CircuitState st, double charge,
-                          int capacity, OpticalKnot *knots, int32_t *counts, unsigned long long *ref_stats,
-                          int32_t *error, unsigned long long *counters, cudaStream_t s) {
+                          int capacity, CellPose *probe_poses, double *probe_radiance, OpticalKnot *knots,
+                          int32_t *counts, unsigned long long *ref_stats, int32_t *error,
+                          unsigned long long *counters, cudaStream_t s) {
+  // the five initial probes of every pixel: five cells of the native trace
+  // kernel (8 cells per warp packet: 4 pixels x 5 probe times)
+  probe_poses_kernel<<<1, 32, 0, s>>>(ivs, n_ivs, start, end, probe_poses);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_trace_cells(scene, n, probe_poses, 0, 5, 3, probe_radiance, nullptr, counters, s);
+  if (e != cudaSuccess) return e;
   refine_kernel<<<blocks_of(n, 128), 128, 0, s>>>(scene, n, ivs, n_ivs, start, end, photo, tolerance, st, charge,
-                                                  capacity, knots, counts, ref_stats, error, counters);
+                                                  capacity, probe_radiance, knots, counts, ref_stats, error,
+                                                  counters);
   return cudaGetLastError();
 }
 

@@ -244,6 +244,7 @@ struct dvs_sensor {
   int32_t *own_order = nullptr;      // allocated when the sensor covers a row band
   std::vector<int32_t> band_rank_of_pixel;  // band-local row-major pixel -> rank
   int pixels() const { return n_pix; }
+  CellPose *probe_poses = nullptr;  // the five initial adaptive probe poses
   int rays_per_lane = 2;  // traversal tuning: 1, 2 or 4 sub-rays per lane (dvs_sensor_set_tuning / autotune)
   SceneView view() const {
     SceneView v = scene->view();
@@ -687,6 +688,7 @@ int dvs_sensor_destroy(dvs_sensor *s) {
   cudaFree(s->ivs);
   cudaFree(s->cells);
   cudaFree(s->poses);
+  cudaFree(s->probe_poses);
   cudaFree(s->d_state);
   if (s->h_ivs) cudaFreeHost(s->h_ivs);
   if (s->h_cells) cudaFreeHost(s->h_cells);
@@ -1058,8 +1060,11 @@ int dvs_sensor_process_adaptive(dvs_sensor *s, const dvs_optical_interval *ivs, 
   CUDA_TRY(cudaMemsetAsync(s->ref_stats, 0, sizeof(unsigned long long) * kRefSlots, s->stream), "clear statistics");
   CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream), "clear refinement errors");
   record_timer(s, 0);
+  CUDA_TRY(ensure_radiance(s, 5), "initial probe radiance");
+  if (!s->probe_poses) CUDA_TRY(cudaMalloc(&s->probe_poses, sizeof(CellPose) * 5), "probe poses");
   CUDA_TRY(launch_refine(view, n, s->ivs, (int)count, start, end, s->photo, tolerance, s->st, s->p.charge_scale, cap,
-                         s->knots, s->knot_counts, s->ref_stats, s->error_word, s->counters, s->stream),
+                         s->probe_poses, s->radiance, s->knots, s->knot_counts, s->ref_stats, s->error_word,
+                         s->counters, s->stream),
            "refine pixel optical launch");
   s->stats.launches += 1;
   CUDA_TRY(cudaMemcpyAsync(s->h_ref, s->ref_stats, sizeof(unsigned long long) * kRefSlots, cudaMemcpyDeviceToHost,

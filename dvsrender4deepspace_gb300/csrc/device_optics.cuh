@@ -1008,6 +1008,114 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
   return out;
 }
 
+// One pixel at one pose sampled by a whole warp (sub-ray packets): the lanes
+// carry the pixel's sub-rays, two each, so a packet spans one pixel's
+// footprint -- the coherent shape when a pixel is wanted at only a few times
+// (camera frames, the initial pose, adaptive probes).  Lane 0 forms the FP64
+// radiance and depth sums in sub-ray order through shuffles, so the result is
+// the same double as the serial loop of sample_pixel_packet.  Called by all
+// 32 lanes with warp-uniform arguments; the result is valid in lane 0.
+template <int kMode>
+__device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const CellPose &pose, int *stack_code,
+                                            float *stack_t) {
+  constexpr int R = 2;
+  const int lane = threadIdx.x & 31;
+  PixelSample out{0.0, -1.0f, true, 0u, 0u};
+  double depth = 0;
+  int valid_depth = 0;
+  const float3 light = f3(pose.lx, pose.ly, pose.lz);
+  const float3 origin = f3(pose.px, pose.py, pose.pz);
+  const int ss = S.samples, n_sub = ss * ss;
+  const int px_i = pixel % S.width, py_i = pixel / S.width;
+  const HapkeConst hc = hapke_const(S.hapke);
+  bool valid = true;
+  for (int g = 0; g < n_sub; g += 32 * R) {
+    float px[R], py[R];
+    float3 ray[R], org[R];
+    bool live[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int j = g + lane * R + r;
+      live[r] = valid && j < n_sub;
+      const int jj = j < n_sub ? j : 0;
+      px[r] = subray_x(S, px_i, jj % ss);
+      py[r] = subray_y(S, py_i, jj / ss);
+      ray[r] = normalize(rotate_ray(pose, f3(px[r], -py[r], -1)));
+      org[r] = origin;
+    }
+    HitRecord hit[R];
+    trace_nearest_packet_r<R>(S, org, ray, live, stack_code, stack_t, hit);
+    bool ovf = false, lit[R], hitp[R];
+    float3 normal[R], sorigin[R];
+    float albedo[R], r0[R];
+    int self[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      ovf = ovf || (live[r] && hit[r].hit < 0);
+      hitp[r] = live[r] && hit[r].hit == 1;
+      lit[r] = false;
+      normal[r] = f3(0, 0, 0);
+      sorigin[r] = f3(0, 0, 0);
+      albedo[r] = S.hapke.w;
+      r0[r] = hc.r0_w;
+      self[r] = hit[r].tri;
+      if (hitp[r] && kMode != kDepthOnly) {
+        const float4 *q = reinterpret_cast<const float4 *>(S.shade + hit[r].tri);
+        const float4 s0 = __ldg(q), s1 = __ldg(q + 1), s2 = __ldg(q + 2);
+        const float w = 1 - hit[r].u - hit[r].v;
+        normal[r] = normalize(f3(s0.x, s0.y, s0.z) * w + f3(s1.x, s1.y, s1.z) * hit[r].u +
+                              f3(s2.x, s2.y, s2.z) * hit[r].v);
+        lit[r] = !(dot(normal[r], light) <= 0 || dot(normal[r], -ray[r]) <= 0);
+        if (lit[r]) {
+          const float4 *t4 = reinterpret_cast<const float4 *>(S.tris + hit[r].tri);
+          const float4 a = __ldg(t4), b = __ldg(t4 + 1), c = __ldg(t4 + 2);
+          sorigin[r] = shadow_origin(f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, c.x), hit[r].u, hit[r].v,
+                                     light);
+          if (S.has_albedo) {
+            albedo[r] = s0.w * w + s1.w * hit[r].u + s2.w * hit[r].v;
+            r0[r] = hfunc_r0(albedo[r]);
+          }
+        }
+      }
+    }
+    double term[R] = {0.0, 0.0};
+    if (kMode != kDepthOnly && __any_sync(kFull, lit[0] || lit[1])) {
+      bool occ[R];
+      trace_shadow_packet_r<R>(S, sorigin, light, lit, self, stack_code, stack_t, occ);
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if (lit[r] && !occ[r]) {
+          const double cos4 = cos4_of(px[r], py[r]);
+          const float3 n = normalize(normal[r]), l = normalize(light), v = normalize(-ray[r]);
+          const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo[r], r0[r], S.hapke, hc);
+          term[r] = fmaxf(0, n_h * pose.intensity) * cos4;
+        }
+    }
+    out.primary += __popc(__ballot_sync(kFull, live[0])) + __popc(__ballot_sync(kFull, live[1]));
+    out.shadow += __popc(__ballot_sync(kFull, lit[0])) + __popc(__ballot_sync(kFull, lit[1]));
+    // sums in sub-ray order j = g + src * R + r, formed by lane 0
+    for (int src = 0; src < 32; ++src)
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const double tv = __shfl_sync(kFull, term[r], src);
+        const float dv = __shfl_sync(kFull, hit[r].t, src);
+        const bool hv = __shfl_sync(kFull, hitp[r] ? 1 : 0, src) != 0;
+        if (lane == 0) {
+          out.radiance += tv;
+          if (kMode != kRadiance && hv) {
+            depth += dv;
+            ++valid_depth;
+          }
+        }
+      }
+    if (__any_sync(kFull, ovf)) valid = false;
+  }
+  out.valid = valid;
+  out.radiance /= ss * ss;
+  out.depth = valid_depth ? float(depth / valid_depth) : -1.0f;
+  return out;
+}
+
 __device__ __forceinline__ unsigned warp_sum(unsigned v) { return __reduce_add_sync(kFull, v); }
 
 }  // namespace

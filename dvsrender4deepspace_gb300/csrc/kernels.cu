@@ -131,6 +131,33 @@ __global__ void __launch_bounds__(128, kRays == 4   ? DVS_TRACE_QUAD_MIN_BLOCKS
   }
 }
 
+// Few poses per pixel: one warp per (pixel, pose), lanes carrying the
+// pixel's sub-rays (sample_pixel_subrays).  Item w = (rank, cell) with
+// consecutive warps on the same pixel.
+template <int kMode>
+__global__ void __launch_bounds__(128, DVS_TRACE_PAIR_MIN_BLOCKS)
+    trace_subray_kernel(SceneView S, int n_pix, const int32_t *rank_list, const CellPose *poses, int c0, int nc,
+                        double *radiance, float *depth_out, unsigned long long *counters) {
+  __shared__ int s_code[kWarpsPerBlock][kStackSlots];
+  __shared__ float s_t[kWarpsPerBlock][kStackSlots];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const long long warp = (long long)(blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= (long long)n_pix * nc) return;  // warp-uniform
+  const int rank = (int)(warp / nc), cell = (int)(warp % nc);
+  const int pixel = __ldg(S.pixel_of_rank + (rank_list ? rank_list[rank] : rank));
+  const CellPose pose = poses[c0 + cell];
+  const PixelSample s = sample_pixel_subrays<kMode>(S, pixel, pose, s_code[wib], s_t[wib]);
+  if (lane == 0) {
+    const size_t o = (size_t)cell * n_pix + rank;
+    radiance[o] = s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll);
+    if (depth_out) depth_out[o] = s.depth;
+    if (counters) {
+      atomicAdd(counters + kCntPrimary, (unsigned long long)s.primary);
+      atomicAdd(counters + kCntShadow, (unsigned long long)s.shadow);
+    }
+  }
+}
+
 template <class Rng>
 __global__ void init_pixels_kernel(int n, const int32_t *pixel_of_rank, const double *radiance, PixelParams p,
                                    PhotoParams photo, double stddev, double minimum, unsigned seed, CircuitState st,
@@ -359,6 +386,17 @@ cudaError_t launch_trace_list(const SceneView &scene, int n_pix, const int32_t *
                               int c0, int nc, int cw_log2, double *radiance, float *depth, unsigned long long *counters,
                               cudaStream_t s) {
   if (n_pix <= 0 || nc <= 0) return cudaSuccess;
+  if (scene.samples * scene.samples >= 32 && nc <= 8) {
+    // few poses per pixel: sub-ray packets (one warp per pixel and pose)
+    const int grid = blocks((long long)n_pix * nc * 32, 128);
+    if (depth)
+      trace_subray_kernel<kRadianceDepth><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, radiance, depth,
+                                                               counters);
+    else
+      trace_subray_kernel<kRadiance><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, radiance, nullptr,
+                                                          counters);
+    return cudaGetLastError();
+  }
   const int cw = 1 << cw_log2, ppw = 32 >> cw_log2;
   const long long warps = (long long)((n_pix + ppw - 1) / ppw) * ((nc + cw - 1) / cw);
   const int ss2 = scene.samples * scene.samples;

@@ -113,10 +113,12 @@ cudaError_t launch_circuit_list(int n, const int32_t *rank_list, const Cell *cel
                                 CircuitState st, int32_t *ev_count, double *slab_t, int8_t *slab_p, int32_t *error,
                                 unsigned long long *counters, cudaStream_t s);
 // Adaptive optical refinement (adaptive.cu).
+// probe_poses: 5 poses of scratch; probe_radiance: 5 x n doubles of scratch.
 cudaError_t launch_refine(const SceneView &scene, int n, const dvs_optical_interval *ivs, int n_ivs, double start,
                           double end, PhotoParams photo, double tolerance, CircuitState st, double charge,
-                          int capacity, OpticalKnot *knots, int32_t *counts, unsigned long long *ref_stats,
-                          int32_t *error, unsigned long long *counters, cudaStream_t s);
+                          int capacity, CellPose *probe_poses, double *probe_radiance, OpticalKnot *knots,
+                          int32_t *counts, unsigned long long *ref_stats, int32_t *error,
+                          unsigned long long *counters, cudaStream_t s);
 cudaError_t launch_identify_exact(int n, const Cell *cells, int n_cells, double start, double end,
                                   const OpticalKnot *knots, int32_t *knot_counts, int capacity, int32_t *exact_cells,
                                   int32_t *exact_counts, int32_t *queue, int32_t *total,

@@ -144,6 +144,24 @@ def test_motion_blur_exposure_is_the_weighted_sum_of_renders():
         cam.render_blur([poses[0]], np.array([np.nan], np.float32))
 
 
+def test_subray_packets_equal_temporal_packets():
+    """A single-pose render (sub-ray packets: one warp per pixel, lanes on its
+    sub-rays, ordered FP64 sums) and a nine-pose exposure (temporal packets:
+    one warp over a pixel's poses) give bit-identical radiance for the same
+    pose."""
+    V, N, I, camera, hap, scene = terrain_scene(ss=8)
+    cam = CamRayCaster(scene)
+    pose = dict(position=(13.0, -7.0, 700.0), rotation=(0.02, -0.01, 0.3, math.sqrt(1 - 0.02**2 - 0.01**2 - 0.09)),
+                light=trajectory.sun_direction(30, 40), intensity=1000)
+    single, _ = cam.render_state(pose)
+    for k in (0, 4, 8):
+        w = np.zeros(9, np.float32)
+        w[k] = 1
+        blur = cam.render_blur([pose] * 9, w)
+        assert np.array_equal(blur, single), k
+    assert (single > 0).mean() > 0.5
+
+
 # ---- sensor path (tests/test_sensor.cu:66-93,160-173) ----------------------------------
 
 def plane_sensor(**over):
