@@ -35,14 +35,28 @@ __device__ __forceinline__ float3 normalize(float3 v) {
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
 
 // ---- Hapke (include/dvs/hapke.hpp:14-157), FP32 --------------------------------
-__device__ __forceinline__ float safe_tan(float x) {
-  return tanf(clampf(x, -kPi / 2.0f + 1e-6f, kPi / 2.0f - 1e-6f));
-}
-__device__ __forceinline__ float safe_acos(float x) { return acosf(clampf(x, -1.0f, 1.0f)); }
+// The reference's formulas evaluated through trigonometric identities
+// ("identity form"): every transcendental of the phase and azimuth angles
+// except acos(cos psi) becomes a square root of a ratio, which the CUDA
+// compiler turns into far fewer instructions than tanf/sinf/cosf/powf:
+//   tan(acos(c) / 2) = sqrt((1 - c) / (1 + c))      (hapke.hpp:135, :82-84)
+//   sin(psi / 2)     = sqrt((1 - cos psi) / 2)       (hapke.hpp:92)
+//   cos(psi)         = cos psi (the clamped argument of acos, hapke.hpp:96,123)
+//   y^1.5            = y * sqrt(y)                   (hapke.hpp:22-29)
+//   e1(y) = exp(-2/pi * q), e2(y) = exp(-1/pi * q^2) with the one quotient
+//   q = cot(thetap) cos(y) / sin(y)                  (hapke.hpp:64-73)
+// Each is exact in real arithmetic; in FP32 the result stays within a few
+// ulp of the reference's own order (bounded against the FP64 oracle in
+// tests/test_oracle_golden.py).  The clamps and the one non-finite case keep
+// the reference's values: tan(phase/2) is capped at tan(pi/2 - 1e-6)
+// (safe_tan, hapke.hpp:14-16), and psi == acos(-1) keeps the reference's
+// tan(pi_f / 2) < 0, whose exp overflows and makes the sample NaN (dropped by
+// the caller's fmaxf) -- here tan(psi/2) = -inf there.
+__device__ __forceinline__ float pow15(float y) { return y * sqrtf(y); }
 __device__ __forceinline__ float hg_double_lobe(float cosg, float b, float c) {
   const float one_minus_bb = 1.0f - b * b;
-  const float term1 = ((1.0f + c) * 0.5f) * one_minus_bb / powf(1.0f - 2.0f * b * cosg + b * b, 1.5f);
-  const float term2 = ((1.0f - c) * 0.5f) * one_minus_bb / powf(1.0f + 2.0f * b * cosg + b * b, 1.5f);
+  const float term1 = ((1.0f + c) * 0.5f) * one_minus_bb / pow15(1.0f - 2.0f * b * cosg + b * b);
+  const float term2 = ((1.0f - c) * 0.5f) * one_minus_bb / pow15(1.0f + 2.0f * b * cosg + b * b);
   return term1 + term2;
 }
 __device__ __forceinline__ float b_s(float tg, float h) {
@@ -69,15 +83,14 @@ __device__ __forceinline__ float porosity_k(float phi) {
   const float p = 1.209f * powf(phi, 2.0f / 3.0f);
   return -logf(1.0f - p) / p;
 }
-__device__ __forceinline__ float f_psi(float psi) { return expf(-2.0f * tanf(psi * 0.5f)); }
 
 // The parts of hapke.hpp that depend on the material only: porosity K,
-// tan(thetap), 1/tan(thetap), chi(thetap) and the r0 of the H-function for
-// the scene's single-scattering albedo.  Each is the value hapke.hpp
-// recomputes inside every call (same operations, same rounding), evaluated
-// once per pixel sample loop instead of up to fourteen times per shaded ray.
+// tan(thetap), 1/tan(thetap), chi(thetap), the r0 of the H-function for the
+// scene's single-scattering albedo and the cap of tan(phase/2).  Each is the
+// value hapke.hpp recomputes inside every call (same operations, same
+// rounding), evaluated once per pixel sample loop instead of per shaded ray.
 struct HapkeConst {
-  float K, tan_t, cot_t, chi, r0_w;
+  float K, tan_t, cot_t, chi, r0_w, tg_max;
   bool rough;
 };
 __device__ __forceinline__ HapkeConst hapke_const(const dvs_hapke &p) {
@@ -88,17 +101,12 @@ __device__ __forceinline__ HapkeConst hapke_const(const dvs_hapke &p) {
   h.cot_t = 1.0f / h.tan_t;
   h.chi = 1.0f / sqrtf(1.0f + kPi * h.tan_t * h.tan_t);
   h.r0_w = hfunc_r0(p.w);
+  h.tg_max = tanf(kPi / 2.0f - 1e-6f);
   return h;
 }
-// e1(thetap, y), e2(thetap, y) of hapke.hpp (with 1/tan(thetap) = cot_t).
-__device__ __forceinline__ float e1_c(float cot_t, float cosy, float siny) {
-  const float s = fmaxf(siny, 1e-6f);
-  return expf((-2.0f / kPi) * cot_t * cosy / s);
-}
-__device__ __forceinline__ float e2_c(float cot_t, float cosy, float siny) {
-  const float s = fmaxf(siny, 1e-6f);
-  const float v = cot_t * cosy / s;
-  return expf((-1.0f / kPi) * v * v);
+// The quotient q = cot(thetap) cos(y) / max(sin(y), 1e-6) shared by e1 and e2.
+__device__ __forceinline__ float e_quot(float cot_t, float cosy, float siny) {
+  return cot_t * cosy / fmaxf(siny, 1e-6f);
 }
 
 // Inlining policy of the large shading and traversal bodies (instruction-cache pressure).
@@ -107,7 +115,8 @@ __device__ __forceinline__ float e2_c(float cot_t, float cosy, float siny) {
 #else
 #define DVS_SHADE_INLINE
 #endif
-// hapke_reflectance (hapke.hpp:131-152); r0 is hfunc's r0 for this albedo.
+// hapke_reflectance (hapke.hpp:131-152) in the identity form above; r0 is
+// hfunc's r0 for this albedo.
 DVS_SHADE_INLINE __device__ float hapke_reflectance(float cosi, float cose, float cosg, float albedo, float r0,
                                                     const dvs_hapke &p, const HapkeConst &h) {
   if (cosi <= 0 || cose <= 0) return 0;
@@ -115,8 +124,9 @@ DVS_SHADE_INLINE __device__ float hapke_reflectance(float cosi, float cose, floa
   cose = clampf(cose, 0, 1);
   cosg = clampf(cosg, -1, 1);
   const float sini = sqrtf(fmaxf(0, 1 - cosi * cosi)), sine = sqrtf(fmaxf(0, 1 - cose * cose));
-  const float tg = safe_tan(safe_acos(cosg) * 0.5f);
-  const float psi = safe_acos((cosg - cosi * cose) / (sini * sine + 1e-6f));
+  const float tg = fminf(sqrtf((1.0f - cosg) / (1.0f + cosg)), h.tg_max);
+  const float cpsi = clampf((cosg - cosi * cose) / (sini * sine + 1e-6f), -1.0f, 1.0f);
+  const float psi = acosf(cpsi);
   const float p_g = hg_double_lobe(cosg, p.b, p.c);
   const float BS = b_s(tg, p.hS);
   // b_c is finite, so with B_C0 == 0 the factor (1 + BC * B_C0) is exactly 1
@@ -129,21 +139,22 @@ DVS_SHADE_INLINE __device__ float hapke_reflectance(float cosi, float cose, floa
   } else {
     const float ch = h.chi;
     const float tan_thetap = h.tan_t;
-    const float sh = sinf(psi * 0.5f);
-    const float s2 = sh * sh;
-    const float e2e = e2_c(h.cot_t, cose, sine), e2i = e2_c(h.cot_t, cosi, sini);
-    const float e1e = e1_c(h.cot_t, cose, sine), e1i = e1_c(h.cot_t, cosi, sini);
+    const float s2 = (1.0f - cpsi) * 0.5f;              // sin^2(psi / 2)
+    const float qe = e_quot(h.cot_t, cose, sine), qi = e_quot(h.cot_t, cosi, sini);
+    const float e2e = expf((-1.0f / kPi) * qe * qe), e2i = expf((-1.0f / kPi) * qi * qi);
+    const float e1e = expf((-2.0f / kPi) * qe), e1i = expf((-2.0f / kPi) * qi);
     // eta(y) = chi * (cos y + sin y * tan(thetap) * e2(y) / (2 - e1(y)))
     const float eta_e = ch * (cose + sine * tan_thetap * e2e / (2.0f - e1e));
     const float eta_i = ch * (cosi + sini * tan_thetap * e2i / (2.0f - e1i));
-    const float fp = f_psi(psi);
+    const float tpsi = cpsi > -1.0f ? sqrtf((1.0f - cpsi) / (1.0f + cpsi)) : -kInf();  // tan(psi / 2)
+    const float fp = expf(-2.0f * tpsi);
     if (cosi >= cose) {
-      mu0 = ch * (cosi + sini * tan_thetap * (cosf(psi) * e2e + s2 * e2i) / (2.0f - e1e - (psi / kPi) * e1i));
+      mu0 = ch * (cosi + sini * tan_thetap * (cpsi * e2e + s2 * e2i) / (2.0f - e1e - (psi / kPi) * e1i));
       mue = ch * (cose + sine * tan_thetap * (e2e - s2 * e2i) / (2.0f - e1e - (psi / kPi) * e1i));
       S = mue / eta_e * cosi / eta_i * ch / (1.0f - fp + fp * ch * (cosi / eta_i));
     } else {
       mu0 = ch * (cosi + sini * tan_thetap * (e2i - s2 * e2e) / (2.0f - e1i - (psi / kPi) * e1e));
-      mue = ch * (cose + sine * tan_thetap * (cosf(psi) * e2i + s2 * e2e) / (2.0f - e1i - (psi / kPi) * e1e));
+      mue = ch * (cose + sine * tan_thetap * (cpsi * e2i + s2 * e2e) / (2.0f - e1i - (psi / kPi) * e1e));
       S = mue / eta_e * cosi / eta_i * ch / (1.0f - fp + fp * ch * (cose / eta_e));
     }
   }

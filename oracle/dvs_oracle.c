@@ -169,19 +169,114 @@ static real hapke_reflectance_r(real cosi, real cose, real cosg, real albedo, co
          (R(1.0) + BC * (real)p->B_C0) * rst.S;
 }
 
+/* ---- Hapke, identity form ------------------------------------------------
+ * hapke_reflectance_r above is hapke.hpp:131-151 in the reference's own
+ * operation order.  The CUDA kernels evaluate the same reflectance through
+ * identities that are exact in real arithmetic:
+ *   tan(acos(c) / 2) = sqrt((1 - c) / (1 + c)), capped at tan(pi/2 - 1e-6)
+ *                      (safe_tan, hapke.hpp:14-16);
+ *   sin^2(psi / 2)   = (1 - cos psi) / 2;  cos(psi) = cos psi;
+ *   tan(psi / 2)     = sqrt((1 - cos psi) / (1 + cos psi)), and -inf at
+ *                      cos psi = -1, where the reference's tan(pi_f / 2) is
+ *                      negative and its exp overflows (a NaN sample);
+ *   y^1.5            = y * sqrt(y)  (hg_double_lobe, hapke.hpp:22-29);
+ *   e1 = exp(-2/pi q), e2 = exp(-1/pi q^2) with one q = cot(thetap) cos y /
+ *                      max(sin y, 1e-6)  (hapke.hpp:64-73).
+ * hapke_reflectance_id_r restates that form in the kernels' operation order
+ * (material constants hoisted as the kernels do, same values), so the
+ * kernels' radiance is compared with it up to the ulps of acos/exp/log.  The
+ * reference form stays the pinned one (golden vectors of hapke.hpp), and the
+ * tests bound both forms against the FP64 oracle. */
+static real pow15_r(real y) { return y * sqrt(y); }
+static real hapke_reflectance_id_r(real cosi, real cose, real cosg, real albedo, const ohapke *p) {
+  if (cosi <= 0 || cose <= 0) return 0;
+  cosi = clampr(cosi, 0, 1); cose = clampr(cose, 0, 1); cosg = clampr(cosg, -1, 1);
+  const real sini = sqrt(fmax(R(0.0), 1 - cosi * cosi)), sine = sqrt(fmax(R(0.0), 1 - cose * cose));
+  const real tg_max = tan(kPi / R(2.0) - R(1e-6));
+  const real tg = fmin(sqrt((R(1.0) - cosg) / (R(1.0) + cosg)), tg_max);
+  const real cpsi = clampr((cosg - cosi * cose) / (sini * sine + R(1e-6)), R(-1.0), R(1.0));
+  const real psi = acos(cpsi);
+  const real b = (real)p->b, c = (real)p->c;
+  const real one_minus_bb = R(1.0) - b * b;
+  const real p_g = ((R(1.0) + c) * R(0.5)) * one_minus_bb / pow15_r(R(1.0) - R(2.0) * b * cosg + b * b) +
+                   ((R(1.0) - c) * R(0.5)) * one_minus_bb / pow15_r(R(1.0) + R(2.0) * b * cosg + b * b);
+  const real BS = b_s(tg, (real)p->hS);
+  const real BC = (real)p->B_C0 != R(0.0) ? b_c(tg, (real)p->hC) : R(0.0);
+  const real K = porosity_k((real)p->phi);
+  real mu0, mue, S;
+  if ((real)p->thetap <= R(1e-8)) {
+    mu0 = cosi; mue = cose; S = R(1.0);
+  } else {
+    const real tan_thetap = tan((real)p->thetap);
+    const real cot_t = R(1.0) / tan_thetap;
+    const real ch = R(1.0) / sqrt(R(1.0) + kPi * tan_thetap * tan_thetap);
+    const real s2 = (R(1.0) - cpsi) * R(0.5);
+    const real qe = cot_t * cose / fmax(sine, R(1e-6)), qi = cot_t * cosi / fmax(sini, R(1e-6));
+    const real e2e = exp((R(-1.0) / kPi) * qe * qe), e2i = exp((R(-1.0) / kPi) * qi * qi);
+    const real e1e = exp((R(-2.0) / kPi) * qe), e1i = exp((R(-2.0) / kPi) * qi);
+    const real eta_e = ch * (cose + sine * tan_thetap * e2e / (R(2.0) - e1e));
+    const real eta_i = ch * (cosi + sini * tan_thetap * e2i / (R(2.0) - e1i));
+#ifdef ORACLE_FP64
+    /* pi_d / 2 < pi / 2: the reference's tan(psi / 2) at psi = acos(-1) is
+     * +huge and its exp underflows to 0, as sqrt(2 / 0) = +inf gives. */
+    const real tpsi = sqrt((R(1.0) - cpsi) / (R(1.0) + cpsi));
+#else
+    const real tpsi = cpsi > R(-1.0) ? sqrt((R(1.0) - cpsi) / (R(1.0) + cpsi)) : -(real)INFINITY;
+#endif
+    const real fp = exp(R(-2.0) * tpsi);
+    if (cosi >= cose) {
+      mu0 = ch * (cosi + sini * tan_thetap * (cpsi * e2e + s2 * e2i) / (R(2.0) - e1e - (psi / kPi) * e1i));
+      mue = ch * (cose + sine * tan_thetap * (e2e - s2 * e2i) / (R(2.0) - e1e - (psi / kPi) * e1i));
+      S = mue / eta_e * cosi / eta_i * ch / (R(1.0) - fp + fp * ch * (cosi / eta_i));
+    } else {
+      mu0 = ch * (cosi + sini * tan_thetap * (e2i - s2 * e2e) / (R(2.0) - e1i - (psi / kPi) * e1e));
+      mue = ch * (cose + sine * tan_thetap * (cpsi * e2i + s2 * e2e) / (R(2.0) - e1i - (psi / kPi) * e1e));
+      S = mue / eta_e * cosi / eta_i * ch / (R(1.0) - fp + fp * ch * (cose / eta_e));
+    }
+  }
+  const real M = hfunc(mu0 / K, albedo) * hfunc(mue / K, albedo) - R(1.0);
+  const real LS = mu0 / (mu0 + mue + R(1e-6));
+  return (albedo / (R(4.0) * kPi)) * LS * K * (p_g * (R(1.0) + BS * (real)p->B_S0) + M) *
+         (R(1.0) + BC * (real)p->B_C0) * S;
+}
+
+/* Form of the sampler's Hapke: 1 = identity form (the FP32 oracle's default,
+ * the kernels' arithmetic), 0 = the reference's order (the FP64 oracle's
+ * default).  Set before sampling; read-only while the sampler runs. */
+#ifdef ORACLE_FP64
+static int g_hapke_form = 0;
+#else
+static int g_hapke_form = 1;
+#endif
+void oracle_set_hapke_form(int form) { g_hapke_form = form ? 1 : 0; }
+int oracle_hapke_form(void) { return g_hapke_form; }
+
+static real hapke_form_r(int form, real cosi, real cose, real cosg, real albedo, const ohapke *p) {
+  return form ? hapke_reflectance_id_r(cosi, cose, cosg, albedo, p)
+              : hapke_reflectance_r(cosi, cose, cosg, albedo, p);
+}
+
 static real hapke_directional_r(rv3 normal, rv3 light, rv3 view, real albedo, const ohapke *p) {
   /* hapke.hpp:153-157 */
   rv3 n = normalize3(normal), l = normalize3(light), v = normalize3(view);
-  return hapke_reflectance_r(dot3(n, l), dot3(n, v), dot3(l, v), albedo, p);
+  return hapke_form_r(g_hapke_form, dot3(n, l), dot3(n, v), dot3(l, v), albedo, p);
 }
 
+/* The reference form (pinned bit for bit against hapke.hpp). */
 float oracle_hapke_reflectance(float cosi, float cose, float cosg, float albedo, const ohapke *p) {
   return (float)hapke_reflectance_r(cosi, cose, cosg, albedo, p);
 }
+/* Either form, in this library's precision, returned in double. */
+double oracle_hapke_reflectance_form(int form, double cosi, double cose, double cosg, double albedo,
+                                     const ohapke *p) {
+  return (double)hapke_form_r(form, (real)cosi, (real)cose, (real)cosg, (real)albedo, p);
+}
 float oracle_hapke_directional(const float *n, const float *l, const float *v, float albedo,
                                const ohapke *p) {
-  return (float)hapke_directional_r(mk(n[0], n[1], n[2]), mk(l[0], l[1], l[2]),
-                                    mk(v[0], v[1], v[2]), albedo, p);
+  /* hapke.hpp:153-157 in the reference form (pinned against the reference). */
+  rv3 nn = normalize3(mk(n[0], n[1], n[2])), ll = normalize3(mk(l[0], l[1], l[2])),
+      vv = normalize3(mk(v[0], v[1], v[2]));
+  return (float)hapke_reflectance_r(dot3(nn, ll), dot3(nn, vv), dot3(ll, vv), albedo, p);
 }
 
 /* ---- pixel circuit (include/dvs/pixel_model.hpp:18-102), always FP64 ------ */

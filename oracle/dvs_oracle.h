@@ -10,8 +10,13 @@
  * The same source is compiled twice:
  *   liboracle_f32.so  -- the reference's own arithmetic: FP32 rays, triangle
  *                        test and Hapke, FP64 radiance sums, cos^4 and circuit.
+ *                        Its sampler evaluates Hapke in the identity form of
+ *                        the CUDA kernels (exact trigonometric identities,
+ *                        see dvs_oracle.c); oracle_set_hapke_form(0) selects
+ *                        the reference's own operation order.
  *   liboracle_f64.so  -- the same model with FP64 rays, geometry and Hapke
- *                        (the "FP64 oracle" used for error reports).
+ *                        in the reference's order (the "FP64 oracle" used
+ *                        for error reports).
  * Both are compiled with -ffp-contract=off so x86 and Arm give the same bits.
  *
  * Pinning: the circuit, Hapke, BVH build and FIFO readout are compared with
@@ -117,6 +122,13 @@ int oracle_is_fp64(void);
 float oracle_hapke_reflectance(float cosi, float cose, float cosg, float albedo, const ohapke *p);
 float oracle_hapke_directional(const float *normal, const float *light, const float *view,
                                float albedo, const ohapke *p);
+/* The Hapke form of the sampler: 1 = identity form (the CUDA kernels'
+ * arithmetic; FP32 default), 0 = the reference's operation order (FP64
+ * default).  oracle_hapke_reflectance/_directional always use form 0. */
+void oracle_set_hapke_form(int form);
+int oracle_hapke_form(void);
+double oracle_hapke_reflectance_form(int form, double cosi, double cose, double cosg, double albedo,
+                                     const ohapke *p);
 double oracle_receptor_log_at(double u, double rate, double dt, double charge);
 /* advance_pixel with a normal() draw that returns 0 (deterministic reset). */
 int oracle_advance_pixel(opixel_state *s, const opixel_params *p, double rate, double t0, double t1,

@@ -3,8 +3,9 @@
 Imported only by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg
 of ``bench.py``.  The oracle (``dvs_oracle.c``) restates the reference
 algorithm of BugBubbles/DvsRender4DeepSpace; ``liboracle_f32.so`` keeps the
-reference's FP32 ray/Hapke arithmetic, ``liboracle_f64.so`` is the FP64
-oracle.  ``load_reference()`` opens ``_ref/libdvsref.so``, the reference's own
+reference's FP32 ray arithmetic and evaluates Hapke in the identity form the
+CUDA kernels use (``oracle_set_hapke_form(0)`` selects the reference's own
+operation order), ``liboracle_f64.so`` is the FP64 oracle (reference order).  ``load_reference()`` opens ``_ref/libdvsref.so``, the reference's own
 host-compilable code built here by ``make ref`` (absent on machines without
 the reference checkout).
 """
@@ -116,6 +117,10 @@ def _declare(lib):
     lib.oracle_hapke_reflectance.argtypes = [C.c_float] * 4 + [C.POINTER(ohapke)]
     lib.oracle_hapke_directional.restype = C.c_float
     lib.oracle_hapke_directional.argtypes = [c_f_p, c_f_p, c_f_p, C.c_float, C.POINTER(ohapke)]
+    lib.oracle_set_hapke_form.argtypes = [C.c_int]
+    lib.oracle_hapke_form.restype = C.c_int
+    lib.oracle_hapke_reflectance_form.restype = C.c_double
+    lib.oracle_hapke_reflectance_form.argtypes = [C.c_int] + [C.c_double] * 4 + [C.POINTER(ohapke)]
     lib.oracle_receptor_log_at.restype = C.c_double
     lib.oracle_receptor_log_at.argtypes = [C.c_double] * 4
     lib.oracle_advance_pixel.restype = C.c_int

@@ -176,6 +176,51 @@ def test_hapke_known_answers(oracle32):
     assert math.isfinite(oracle32.oracle_hapke_directional(O.fptr(n), O.fptr(n), O.fptr(n), hp["w"], C.byref(hs)))
 
 
+def test_hapke_identity_form_against_the_fp64_reference_form(oracle32):
+    """The CUDA kernels evaluate hapke.hpp:131-151 through exact identities
+    (tan(acos(c)/2) = sqrt((1-c)/(1+c)), sin^2(psi/2) = (1-cos psi)/2,
+    y^1.5 = y sqrt(y), one quotient for e1/e2).  In FP64 the two forms agree to
+    rounding; in FP32 the identity form is as close to the FP64 reference as the
+    reference's own FP32 order is, and within 1e-5 of it except where both are."""
+    o64 = O.load(True)
+    rng = np.random.default_rng(7)
+
+    def unit(k):
+        v = rng.normal(size=(k, 3))
+        return v / np.linalg.norm(v, axis=1, keepdims=True)
+    k = 4000
+    l, v = unit(k), unit(k)
+    l[:, 2], v[:, 2] = np.abs(l[:, 2]), np.abs(v[:, 2])
+    geo = np.stack([l[:, 2], v[:, 2], (l * v).sum(1)], 1).astype(np.float32)
+    mats = [dict(b=.3, c=.4, hS=.06, hC=1.0, thetap=0.349066, w=.25, B_S0=1.0, B_C0=0.0, phi=0.3),
+            dict(b=0.24, c=0.305, hS=0.08, hC=1.0, thetap=26.0 * float(np.float32(math.pi)) / 180.0, w=0.324,
+                 B_S0=2.42, B_C0=0.0, phi=0.3),
+            dict(b=.2, c=.5, hS=.05, hC=.05, thetap=0.0, w=.5, B_S0=1.5, B_C0=1.0, phi=0.0)]
+    for m in mats:
+        hs = O.hapke_struct(m)
+
+        def ev(lib, form, rows=geo):
+            return np.array([lib.oracle_hapke_reflectance_form(form, *map(float, g), m["w"], C.byref(hs))
+                             for g in rows])
+        r32, i32, r64, i64 = ev(oracle32, 0), ev(oracle32, 1), ev(o64, 0), ev(o64, 1)
+        ok = np.isfinite(r64) & (np.abs(r64) > 1e-30)
+        assert ok.mean() > 0.2
+        assert np.array_equal(np.isnan(r32), np.isnan(i32))
+        err = lambda a: np.abs(a[ok] - r64[ok]) / np.abs(r64[ok])
+        assert err(i64).max() < 1e-13                                   # the identities are exact
+        e_ref, e_id = err(r32), err(i32)
+        assert np.quantile(e_id, 0.999) <= 1.1 * np.quantile(e_ref, 0.999) + 1e-7
+        assert e_id.max() <= 1.1 * e_ref.max() + 1e-7
+        assert np.mean(e_id > 1e-5) <= np.mean(e_ref > 1e-5) + 1e-3
+        # cos psi clamped to -1: the FP32 reference's tan(pi_f / 2) < 0 overflows exp and
+        # makes the sample NaN (dropped by the sampler); FP64 gives a finite value.
+        if m["thetap"] > 0:
+            corner = np.float32([[0.5, 0.5, -0.51]])
+            assert math.isnan(ev(oracle32, 0, corner)[0]) and math.isnan(ev(oracle32, 1, corner)[0])
+            a, b = ev(o64, 0, corner)[0], ev(o64, 1, corner)[0]
+            assert math.isfinite(a) and abs(a - b) <= 1e-13 * abs(a)
+
+
 def test_shadow_origins_above_tilted_plane(oracle32):
     # tests/test_render.cu:18-30,95-106: 10000 origins at km coordinates lie outside the plane
     V = np.array([[13000, -13000, 4000], [13005, -13000, 4001.5], [13000, -12995, 4000.75]], np.float32)
