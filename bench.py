@@ -33,6 +33,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# dvs_bvh_params.precision flags: 1 = FP16 child bounds, 2 = watertight triangle test
+GEOMETRY = {"reference": 0, "half": 1, "watertight": 2, "half+watertight": 3}
+
 WORKLOADS = {
     # configs: precision (1280x720), small (346x260 DAVIS, plain method)
     "precision": dict(grid=4096, seed=20260003, camera=dict(width=1280, height=720, fx=1000.0, fy=1000.0, cx=640.0,
@@ -200,7 +203,8 @@ def run_gb300(args):
         torch.distributed.barrier()
     w, V, N, I, traj = make_workload(args.workload, rank)
     t_setup = time.time()
-    scene = DeviceScene(V, N, I, w["camera"], w["ss"], HAPKE, leaf_size=args.leaf)
+    scene = DeviceScene(V, N, I, w["camera"], w["ss"], HAPKE, leaf_size=args.leaf,
+                        geometry=GEOMETRY[args.geometry])
     info = scene.info()
     sensor = EventSensor(scene, PHYSIC, timing=True, cells_per_chunk=args.chunk, cells_per_warp=args.cw,
                          circuit_precision=args.circuit)
@@ -327,6 +331,7 @@ def run_gb300(args):
                    w["sun_elevation"], "intensity": w["intensity"], "l2": "inputs larger than L2 (scene %.1f GB)"
                    % (info["device_bytes"] / 1e9), "parallelism": "dp%d (independent jobs)" % world,
                    "bvh": "8-wide Morton radix, leaf %d, depth %d" % (info["leaf_size"], info["depth"]),
+                   "geometry": args.geometry,
                    "circuit_precision": args.circuit},
         "rays_per_step": rays / args.steps,
         "rays": {"primary_per_step": st["primary_rays"] / args.steps, "shadow_per_step": st["shadow_rays"] / args.steps,
@@ -441,6 +446,8 @@ def main():
     ap.add_argument("--serving-jobs", type=int, default=48)
     ap.add_argument("--serving-scale", type=float, default=0.01)
     ap.add_argument("--leaf", type=int, default=0)
+    ap.add_argument("--geometry", default="reference", choices=sorted(GEOMETRY),
+                    help="BVH format: FP32 or FP16 (half) child bounds; Moller-Trumbore or watertight triangles")
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--cw", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -43,10 +43,11 @@ __device__ __forceinline__ CellPose native_pose(const dvs_optical_interval *ivs,
 }
 
 // One lock-step probe: lanes with `want` trace their pixel at their time.
+template <int kGeo>
 __device__ __forceinline__ double probe(const SceneView &S, int pixel, bool want, const dvs_optical_interval *ivs,
                                         int n_ivs, double t, int *sc, float *stt, bool &bad, unsigned &rays) {
   const CellPose pose = native_pose(ivs, n_ivs, want ? t : ivs[0].t0);
-  const PixelSample s = sample_pixel_packet<kRadiance>(S, pixel, want, pose, sc, stt, nullptr);
+  const PixelSample s = sample_pixel_packet<kRadiance, kGeo>(S, pixel, want, pose, sc, stt, nullptr);
   if (want && (!s.valid || !isfinite(s.radiance))) bad = true;
   rays += s.primary + s.shadow;
   return s.radiance;
@@ -66,6 +67,7 @@ __global__ void probe_poses_kernel(const dvs_optical_interval *ivs, int n_ivs, d
 // rank]: every pixel is probed at the same five times, so they are five
 // circuit cells of a temporal warp packet); the bisection probes, which only
 // some pixels need, are traced here.
+template <int kGeo>
 __global__ void __launch_bounds__(128) refine_kernel(SceneView S, int n, const dvs_optical_interval *ivs, int n_ivs,
                                                      double start, double end, PhotoParams photo, double tolerance,
                                                      CircuitState st, double charge, int capacity,
@@ -143,8 +145,8 @@ __global__ void __launch_bounds__(128) refine_kernel(SceneView S, int n, const d
       }
     }
     if (__any_sync(kFull, need)) {
-      const double left_mid = probe(S, pixel, need, ivs, n_ivs, ta, sc, stt, bad, rays);
-      const double right_mid = probe(S, pixel, need, ivs, n_ivs, tb, sc, stt, bad, rays);
+      const double left_mid = probe<kGeo>(S, pixel, need, ivs, n_ivs, ta, sc, stt, bad, rays);
+      const double right_mid = probe<kGeo>(S, pixel, need, ivs, n_ivs, tb, sc, stt, bad, rays);
       if (need) {
         queries += 2;
         stack[top] = {mid, e.b, e.middle, right_mid, e.right};
@@ -198,6 +200,7 @@ __global__ void identify_exact_kernel(int n, const Cell *cells, int n_cells, dou
 
 // sample_exact_queries (optical_sampler.cu:132-138): one queued cell per lane,
 // grid-stride over the device-side queue length.
+template <int kGeo>
 __global__ void __launch_bounds__(128) sample_exact_kernel(SceneView S, const CellPose *poses,
                                                            const int32_t *exact_cells, const int32_t *queue,
                                                            const int32_t *total, int capacity, double *exact_radiance,
@@ -214,7 +217,7 @@ __global__ void __launch_bounds__(128) sample_exact_kernel(SceneView S, const Ce
     const int rank = slot / capacity;
     const int pixel = active ? S.pixel_of_rank[rank] : 0;
     const CellPose pose = poses[active ? exact_cells[slot] : 0];
-    const PixelSample s = sample_pixel_packet<kRadiance>(S, pixel, active, pose, s_code[wib], s_t[wib], nullptr);
+    const PixelSample s = sample_pixel_packet<kRadiance, kGeo>(S, pixel, active, pose, s_code[wib], s_t[wib], nullptr);
     if (active) {
       if (!s.valid || !isfinite(s.radiance)) atomicOr(error, kErrOptical);
       exact_radiance[slot] = s.radiance;
@@ -342,9 +345,17 @@ cudaError_t launch_refine(const SceneView &scene, int n, const dvs_optical_inter
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = launch_trace_cells(scene, n, probe_poses, 0, 5, 3, probe_radiance, nullptr, counters, s);
   if (e != cudaSuccess) return e;
-  refine_kernel<<<blocks_of(n, 128), 128, 0, s>>>(scene, n, ivs, n_ivs, start, end, photo, tolerance, st, charge,
-                                                  capacity, probe_radiance, knots, counts, ref_stats, error,
-                                                  counters);
+#define DVS_REFINE(G)                                                                                         \
+  refine_kernel<G><<<blocks_of(n, 128), 128, 0, s>>>(scene, n, ivs, n_ivs, start, end, photo, tolerance, st, charge, \
+                                                     capacity, probe_radiance, knots, counts, ref_stats, error,     \
+                                                     counters)
+  switch (scene.geometry) {
+    case kGeoHalfBounds: DVS_REFINE(kGeoHalfBounds); break;
+    case kGeoWatertight: DVS_REFINE(kGeoWatertight); break;
+    case kGeoHalfBounds | kGeoWatertight: DVS_REFINE(kGeoHalfBounds | kGeoWatertight); break;
+    default: DVS_REFINE(kGeoReference);
+  }
+#undef DVS_REFINE
   return cudaGetLastError();
 }
 
@@ -360,8 +371,16 @@ cudaError_t launch_identify_exact(int n, const Cell *cells, int n_cells, double 
 cudaError_t launch_sample_exact(const SceneView &scene, const CellPose *poses, const int32_t *exact_cells,
                                 const int32_t *queue, const int32_t *total, int capacity, double *exact_radiance,
                                 int32_t *error, unsigned long long *counters, cudaStream_t s) {
-  sample_exact_kernel<<<sm_count() * 8, 128, 0, s>>>(scene, poses, exact_cells, queue, total, capacity,
-                                                     exact_radiance, error, counters);
+#define DVS_EXACT(G)                                                                                       \
+  sample_exact_kernel<G><<<sm_count() * 8, 128, 0, s>>>(scene, poses, exact_cells, queue, total, capacity,     \
+                                                        exact_radiance, error, counters)
+  switch (scene.geometry) {
+    case kGeoHalfBounds: DVS_EXACT(kGeoHalfBounds); break;
+    case kGeoWatertight: DVS_EXACT(kGeoWatertight); break;
+    case kGeoHalfBounds | kGeoWatertight: DVS_EXACT(kGeoHalfBounds | kGeoWatertight); break;
+    default: DVS_EXACT(kGeoReference);
+  }
+#undef DVS_EXACT
   return cudaGetLastError();
 }
 

@@ -303,4 +303,99 @@ bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf
   return true;
 }
 
+// ---- precision-format nodes -------------------------------------------------------
+namespace {
+// FP16 bits of the largest half <= x (up = false) or the smallest half >= x
+// (up = true), for finite x >= 0.  Beyond the largest finite half (65504) the
+// lower bound saturates and the upper bound becomes +inf, both conservative.
+uint16_t half_directed(double x, bool up) {
+  if (!(x > 0.0)) return 0;
+  if (x > 65504.0) return up ? 0x7c00 : 0x7bff;
+  int e = 0;
+  std::frexp(x, &e);          // x in [2^(e-1), 2^e)
+  const int E = e + 14;       // biased half exponent of that binade
+  uint32_t bits;
+  if (E <= 0) {               // subnormal: units of 2^-24
+    const double u = std::ldexp(x, 24);
+    bits = (uint32_t)(up ? std::ceil(u) : std::floor(u));
+  } else {                    // normal: (1024 + mantissa) * 2^(E - 25)
+    const double u = std::ldexp(x, 25 - E);
+    bits = ((uint32_t)E << 10) + ((uint32_t)(up ? std::ceil(u) : std::floor(u)) - 1024u);  // 2048 carries
+  }
+  if (bits >= 0x7c00u) bits = up ? 0x7c00u : 0x7bffu;
+  return (uint16_t)bits;
+}
+double half_value(uint16_t h) {
+  const int E = (h >> 10) & 31, m = h & 1023;
+  if (E == 31) return m ? std::numeric_limits<double>::quiet_NaN() : std::numeric_limits<double>::infinity();
+  return E == 0 ? std::ldexp((double)m, -24) : std::ldexp((double)(1024 + m), E - 25);
+}
+// origin + offset rounded to float toward -inf / +inf, as __fadd_rd/__fadd_ru.
+// The exact sum is s + err (Knuth's TwoSum in double).
+float add_directed(float origin, uint16_t off, bool up) {
+  const double a = origin, b = half_value(off);
+  const double s = a + b;
+  if (std::isinf(s)) return (float)s;
+  const double bb = s - a, err = (a - (s - bb)) + (b - bb);
+  float f = (float)s;
+  const double fd = f;
+  if (!up && (fd > s || (fd == s && err < 0))) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+  if (up && (fd < s || (fd == s && err > 0))) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+  return f;
+}
+}  // namespace
+
+bool quantize_bvh(const std::vector<BvhNode> &nodes, std::vector<BvhQNode> &out, std::string &error) {
+  out.assign(nodes.size(), BvhQNode{});
+  std::atomic<bool> bad_link{false}, bad_box{false};
+  const long long n = (long long)nodes.size();
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; ++i) {
+    const BvhNode &src = nodes[i];
+    BvhQNode &q = out[i];
+    float origin[3] = {0.0f, 0.0f, 0.0f};
+    bool any = false;
+    for (int k = 0; k < kBvhWidth; ++k) {
+      if (src.c[k].count < 0) continue;
+      for (int d = 0; d < 3; ++d) origin[d] = any ? std::min(origin[d], src.c[k].lo[d]) : src.c[k].lo[d];
+      any = true;
+    }
+    for (int d = 0; d < 3; ++d) q.origin[d] = origin[d];
+    q.pad = 0;
+    for (int k = 0; k < kBvhWidth; ++k) {
+      const BvhChild &c = src.c[k];
+      BvhQChild &qc = q.c[k];
+      if (c.count < 0) {
+        for (int d = 0; d < 3; ++d) qc.lo[d] = qc.hi[d] = 0x7c00;
+        qc.link = kQLinkEmpty;
+        continue;
+      }
+      for (int d = 0; d < 3; ++d) {
+        qc.lo[d] = half_directed((double)c.lo[d] - (double)origin[d], false);
+        qc.hi[d] = half_directed((double)c.hi[d] - (double)origin[d], true);
+        if (!(add_directed(origin[d], qc.lo[d], false) <= c.lo[d]) ||
+            !(add_directed(origin[d], qc.hi[d], true) >= c.hi[d]))
+          bad_box = true;
+      }
+      if (c.count == 0) {
+        qc.link = (uint32_t)c.child;
+      } else if (c.count > 16 || (uint64_t)c.child + (uint64_t)c.count > (uint64_t)kQLinkFirstMask + 1) {
+        bad_link = true;
+        qc.link = kQLinkEmpty;
+      } else {
+        qc.link = kQLinkLeaf | ((uint32_t)(c.count - 1) << kQLinkCountShift) | (uint32_t)c.child;
+      }
+    }
+  }
+  if (bad_link) {
+    error = "mesh too large for the precision BVH format (more than 2^27 triangles)";
+    return false;
+  }
+  if (bad_box) {
+    error = "quantised BVH bounds do not enclose the FP32 bounds";
+    return false;
+  }
+  return true;
+}
+
 }  // namespace dvsgb

@@ -131,6 +131,8 @@ struct dvs_scene {
   std::shared_ptr<void> geometry;
   size_t arena_bytes = 0;
   BvhNode *nodes = nullptr;
+  BvhQNode *qnodes = nullptr;  // FP16 child bounds (nodes is then null)
+  int geometry_kind = 0;       // dvs_bvh_params.precision bits
   TriRecord *tris = nullptr;
   ShadeRecord *shade = nullptr;
   int32_t *pixel_of_rank = nullptr;
@@ -156,6 +158,8 @@ struct dvs_scene {
   SceneView view() const {
     SceneView v;
     v.nodes = nodes;
+    v.qnodes = qnodes;
+    v.geometry = geometry_kind;
     v.tris = tris;
     v.shade = shade;
     v.pixel_of_rank = pixel_of_rank;
@@ -304,6 +308,9 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   // tree would be too deep for the traversal stack, wider leaves.  A leaf
   // size given by the caller is used as given.
   const bool leaf_given = params && params->leaf_size > 0;
+  const int precision = params ? params->precision : 0;
+  if (precision < 0 || precision > 3) return fail(DVS_ERR_INVALID, "invalid BVH precision flags (0..3)");
+  const bool half_bounds = precision & DVS_BVH_HALF_BOUNDS, watertight = precision & DVS_BVH_WATERTIGHT;
   BvhBuild bvh;
   std::string err;
   bool built = false;
@@ -314,6 +321,8 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
     if (built || leaf_given || leaf >= 8) break;
   }
   if (!built) return fail(DVS_ERR_INVALID, err);
+  std::vector<BvhQNode> qnodes;
+  if (half_bounds && !quantize_bvh(bvh.nodes, qnodes, err)) return fail(DVS_ERR_INVALID, err);
 
   // leaf-order records
   std::vector<TriRecord> tris(n_triangles);
@@ -327,8 +336,13 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
     std::memset(&t, 0, sizeof(t));
     for (int d = 0; d < 3; ++d) {
       t.v0[d] = vertices[3 * (size_t)a + d];
-      t.e1[d] = vertices[3 * (size_t)b + d] - vertices[3 * (size_t)a + d];
-      t.e2[d] = vertices[3 * (size_t)c + d] - vertices[3 * (size_t)a + d];
+      if (watertight) {  // the vertices themselves, for the watertight test
+        t.e1[d] = vertices[3 * (size_t)b + d];
+        t.e2[d] = vertices[3 * (size_t)c + d];
+      } else {
+        t.e1[d] = vertices[3 * (size_t)b + d] - vertices[3 * (size_t)a + d];
+        t.e2[d] = vertices[3 * (size_t)c + d] - vertices[3 * (size_t)a + d];
+      }
     }
     t.original = src;
     ShadeRecord &s = shade[i];
@@ -356,6 +370,7 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   s->n_vertices = n_vertices;
   s->depth = bvh.depth;
   s->leaf_size = leaf;
+  s->geometry_kind = precision;
   s->build_seconds = bvh.seconds;
   {
     float lo[3] = {vertices[0], vertices[1], vertices[2]}, hi[3] = {vertices[0], vertices[1], vertices[2]};
@@ -368,7 +383,8 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   }
   cudaGetDevice(&s->device);
   const size_t off_nodes = 0;
-  const size_t off_tris = align_up(off_nodes + sizeof(BvhNode) * s->n_nodes, 256);
+  const size_t node_bytes = half_bounds ? sizeof(BvhQNode) : sizeof(BvhNode);
+  const size_t off_tris = align_up(off_nodes + node_bytes * s->n_nodes, 256);
   const size_t off_shade = align_up(off_tris + sizeof(TriRecord) * n_triangles, 256);
   const size_t total = align_up(off_shade + sizeof(ShadeRecord) * n_triangles, 256);
   void *arena = nullptr;
@@ -383,12 +399,18 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   }
   s->arena_bytes = total + sizeof(int32_t) * order.size();
   char *base = static_cast<char *>(arena);
-  s->nodes = reinterpret_cast<BvhNode *>(base + off_nodes);
+  if (half_bounds)
+    s->qnodes = reinterpret_cast<BvhQNode *>(base + off_nodes);
+  else
+    s->nodes = reinterpret_cast<BvhNode *>(base + off_nodes);
   s->tris = reinterpret_cast<TriRecord *>(base + off_tris);
   s->shade = reinterpret_cast<ShadeRecord *>(base + off_shade);
   s->rank_of_pixel.assign(order.size(), 0);
   for (size_t r = 0; r < order.size(); ++r) s->rank_of_pixel[order[r]] = (int32_t)r;
-  e = cudaMemcpy(s->nodes, bvh.nodes.data(), sizeof(BvhNode) * s->n_nodes, cudaMemcpyHostToDevice);
+  if (half_bounds)
+    e = cudaMemcpy(s->qnodes, qnodes.data(), sizeof(BvhQNode) * s->n_nodes, cudaMemcpyHostToDevice);
+  else
+    e = cudaMemcpy(s->nodes, bvh.nodes.data(), sizeof(BvhNode) * s->n_nodes, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(s->tris, tris.data(), sizeof(TriRecord) * n_triangles, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(s->shade, shade.data(), sizeof(ShadeRecord) * n_triangles, cudaMemcpyHostToDevice);
@@ -450,6 +472,8 @@ int dvs_scene_view_create(const dvs_scene *base, const dvs_camera *camera, int32
   s->has_albedo = base->has_albedo;
   s->geometry = base->geometry;
   s->nodes = base->nodes;
+  s->qnodes = base->qnodes;
+  s->geometry_kind = base->geometry_kind;
   s->tris = base->tris;
   s->shade = base->shade;
   s->n_nodes = base->n_nodes;
@@ -483,7 +507,7 @@ int dvs_scene_info_get(const dvs_scene *s, dvs_scene_info *out) {
   out->device_bytes = s->arena_bytes;
   out->build_seconds = s->build_seconds;
   out->leaf_size = s->leaf_size;
-  out->reserved = 0;
+  out->precision = s->geometry_kind;
   return DVS_OK;
 }
 

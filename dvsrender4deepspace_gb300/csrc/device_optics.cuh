@@ -4,6 +4,7 @@
 // internal linkage.  Compiled with -fmad=false (see kernels.cu).
 #pragma once
 #include <cstdint>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "kernels.h"
@@ -217,6 +218,12 @@ __device__ __forceinline__ float3 inverse_direction(float3 d) {  // device_ray.h
   return inv;
 }
 
+// Scene geometry formats, as bit flags: the reference's (FP32 child bounds,
+// Moller-Trumbore on stored edges), kGeoHalfBounds (FP16 child bounds
+// quantised outward against a per-node FP32 origin) and kGeoWatertight (the
+// watertight FP32 triangle test on stored vertices), alone or together.
+enum GeometryKind : int { kGeoReference = 0, kGeoHalfBounds = 1, kGeoWatertight = 2 };
+
 // Moller-Trumbore with precomputed edges (device_ray.hpp:54-80).
 __device__ __forceinline__ bool intersect_tri(float3 ray, float3 o, float3 v0, float3 e1, float3 e2, float &t,
                                               float &u, float &v) {
@@ -235,6 +242,77 @@ __device__ __forceinline__ bool intersect_tri(float3 ray, float3 o, float3 v0, f
   return true;
 }
 
+// Watertight ray/triangle test (Woop, Benthin and Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013) for precision scenes.  The ray
+// is sheared onto +z through its origin (kz = the dominant axis of the
+// direction, kx/ky swapped when it is negative), the vertices are projected,
+// and the signs of the 2-D edge functions U, V, W decide the hit: a ray
+// through a shared edge or vertex hits at least one of the triangles.  An edge
+// function that rounds to exactly zero is recomputed in FP64 (the products of
+// two floats are exact there), as the paper prescribes.  U, V, W weight v0,
+// v1, v2, so the reference's barycentrics (u on v1, v on v2) are V/det, W/det.
+struct WtRay {
+  int kx, ky, kz;
+  float sx, sy, sz;
+};
+__device__ __forceinline__ float comp3(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+__device__ __forceinline__ WtRay wt_setup(float3 d) {
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  WtRay w;
+  w.kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  w.kx = w.kz == 2 ? 0 : w.kz + 1;
+  w.ky = w.kx == 2 ? 0 : w.kx + 1;
+  const float dz = comp3(d, w.kz);
+  if (dz < 0.0f) {
+    const int k = w.kx;
+    w.kx = w.ky;
+    w.ky = k;
+  }
+  w.sx = comp3(d, w.kx) / dz;
+  w.sy = comp3(d, w.ky) / dz;
+  w.sz = 1.0f / dz;
+  return w;
+}
+__device__ __forceinline__ bool intersect_wt(const WtRay &w, float3 o, float3 v0, float3 v1, float3 v2, float &t,
+                                             float &u, float &v) {
+  const float3 A = v0 - o, B = v1 - o, C = v2 - o;
+  const float az = comp3(A, w.kz), bz = comp3(B, w.kz), cz = comp3(C, w.kz);
+  const float ax = comp3(A, w.kx) - w.sx * az, ay = comp3(A, w.ky) - w.sy * az;
+  const float bx = comp3(B, w.kx) - w.sx * bz, by = comp3(B, w.ky) - w.sy * bz;
+  const float cx = comp3(C, w.kx) - w.sx * cz, cy = comp3(C, w.ky) - w.sy * cz;
+  float U = cx * by - cy * bx, V = ax * cy - ay * cx, W = bx * ay - by * ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = (float)((double)cx * (double)by - (double)cy * (double)bx);
+    V = (float)((double)ax * (double)cy - (double)ay * (double)cx);
+    W = (float)((double)bx * (double)ay - (double)by * (double)ax);
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+  const float det = U + V + W;
+  if (det == 0.0f) return false;
+  const float T = U * (w.sz * az) + V * (w.sz * bz) + W * (w.sz * cz);
+  const float rcp = 1.0f / det;
+  t = T * rcp;
+  if (!(t > kRayEps)) return false;
+  u = V * rcp;
+  v = W * rcp;
+  return true;
+}
+// One leaf-order triangle record against one ray.  Records hold (v0, e1, e2),
+// or (v0, v1, v2) in watertight scenes.
+template <int kGeo>
+__device__ __forceinline__ bool tri_hit(const WtRay &w, float3 d, float3 o, float4 a, float4 b, float4 q, float &t,
+                                        float &u, float &v) {
+  if constexpr (!(kGeo & kGeoWatertight))
+    return intersect_tri(d, o, f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, q.x), t, u, v);
+  else
+    return intersect_wt(w, o, f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, q.x), t, u, v);
+}
+template <int kGeo>
+__device__ __forceinline__ WtRay wt_ray(float3 d) {
+  if constexpr (!(kGeo & kGeoWatertight)) return WtRay{0, 0, 0, 0.f, 0.f, 0.f};
+  else return wt_setup(d);
+}
+
 // ---- 8-wide packet traversal ------------------------------------------------------
 // Float min/max across a warp through order-preserving unsigned keys.
 __device__ __forceinline__ unsigned ford(float f) {
@@ -251,14 +329,43 @@ struct ChildRec {
   float3 lo, hi;
   int child, count;
 };
-__device__ __forceinline__ ChildRec load_child(const BvhNode *nodes, int node, int slot) {
-  const float4 *p = reinterpret_cast<const float4 *>(&nodes[node].c[slot]);
-  const float4 a = __ldg(p), b = __ldg(p + 1);
+__device__ __forceinline__ float half_bits_to_float(unsigned bits) {
+  return __half2float(__ushort_as_half((unsigned short)(bits & 0xffffu)));
+}
+// Child record `slot` of node `node`.  Precision nodes decode each bound as
+// origin + offset with the addition rounded toward -inf (lower bounds) or +inf
+// (upper bounds); the builder rounded the offsets the same way, so a decoded
+// box always contains the exact FP32 box and no ray misses a child it would
+// enter (the leaf's triangles are then tested in FP32).
+template <int kGeo>
+__device__ __forceinline__ ChildRec load_child(const SceneView &S, int node, int slot) {
   ChildRec r;
-  r.lo = f3(a.x, a.y, a.z);
-  r.hi = f3(a.w, b.x, b.y);
-  r.child = __float_as_int(b.z);
-  r.count = __float_as_int(b.w);
+  if constexpr (!(kGeo & kGeoHalfBounds)) {
+    const float4 *p = reinterpret_cast<const float4 *>(&S.nodes[node].c[slot]);
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    r.lo = f3(a.x, a.y, a.z);
+    r.hi = f3(a.w, b.x, b.y);
+    r.child = __float_as_int(b.z);
+    r.count = __float_as_int(b.w);
+  } else {
+    const float4 org = __ldg(reinterpret_cast<const float4 *>(S.qnodes + node));
+    const uint4 c = __ldg(reinterpret_cast<const uint4 *>(&S.qnodes[node].c[slot]));
+    r.lo = f3(__fadd_rd(org.x, half_bits_to_float(c.x)), __fadd_rd(org.y, half_bits_to_float(c.x >> 16)),
+              __fadd_rd(org.z, half_bits_to_float(c.y)));
+    r.hi = f3(__fadd_ru(org.x, half_bits_to_float(c.y >> 16)), __fadd_ru(org.y, half_bits_to_float(c.z)),
+              __fadd_ru(org.z, half_bits_to_float(c.z >> 16)));
+    const unsigned link = c.w;
+    if (link == kQLinkEmpty) {
+      r.child = 0;
+      r.count = -1;
+    } else if (link & kQLinkLeaf) {
+      r.child = (int)(link & kQLinkFirstMask);
+      r.count = (int)((link >> kQLinkCountShift) & 15u) + 1;
+    } else {
+      r.child = (int)link;
+      r.count = 0;
+    }
+  }
   return r;
 }
 
@@ -372,7 +479,7 @@ struct HitRecord {
 // all but the nearest go on the stack.  Returns false when none is hit.
 // Coherent packets test one child per lane (lanes 0..7) with interval bounds;
 // others test every child per ray and take the warp minimum as the key.
-template <bool kSorted>
+template <bool kSorted, int kGeo>
 __device__ __forceinline__ bool expand_node(const SceneView &S, int node, const Packet &P, float3 o, float3 idir,
                                             bool lane_live, float t_min, float lane_tmax, float packet_tmax,
                                             Stack &st, int &next, float &next_t, bool &overflow) {
@@ -382,7 +489,7 @@ __device__ __forceinline__ bool expand_node(const SceneView &S, int node, const 
   int code = 0;
   if (P.coherent) {
     if (lane < kBvhWidth) {
-      const ChildRec c = load_child(S.nodes, node, lane);
+      const ChildRec c = load_child<kGeo>(S, node, lane);
       if (c.count >= 0) {
         hit = packet_slab(c, P, t_min, packet_tmax, key);
         code = c.count > 0 ? leaf_code(node, lane) : c.child;
@@ -390,7 +497,7 @@ __device__ __forceinline__ bool expand_node(const SceneView &S, int node, const 
     }
   } else {
     for (int slot = 0; slot < kBvhWidth; ++slot) {
-      const ChildRec c = load_child(S.nodes, node, slot);
+      const ChildRec c = load_child<kGeo>(S, node, slot);
       float tn = kInf();
       const bool h = c.count >= 0 && lane_live && slab(c.lo, c.hi, o, idir, t_min, lane_tmax, tn);
       const float k = wmin(h ? tn : kInf());
@@ -440,9 +547,11 @@ __device__ __forceinline__ bool expand_node(const SceneView &S, int node, const 
 // Nearest hit for the rays of a warp (trace_nearest, device_ray.hpp:136-158).
 // All 32 lanes call converged; inactive lanes never hit.  Each lane tests a
 // leaf's triangles only when its own slab test reaches the leaf.
+template <int kGeo>
 __device__ HitRecord trace_nearest_packet(const SceneView &S, float3 o, float3 d, bool active, int *stack_code,
                                           float *stack_t) {
   const float3 idir = inverse_direction(d);
+  const WtRay wr = wt_ray<kGeo>(d);
   float closest = active ? 1e30f : -1.0f;
   HitRecord h{0, -1, 0.f, 0.f, 0.f};
   const Packet P = make_packet(S, o, d, idir, active);
@@ -456,7 +565,7 @@ __device__ HitRecord trace_nearest_packet(const SceneView &S, float3 o, float3 d
       if (entry >= 0) {
         int next;
         float next_t;
-        if (expand_node<true>(S, entry, P, o, idir, active, kRayEps, closest, packet_tmax, st, next, next_t,
+        if (expand_node<true, kGeo>(S, entry, P, o, idir, active, kRayEps, closest, packet_tmax, st, next, next_t,
                               overflow)) {
           entry = next;
           entry_t = next_t;
@@ -465,15 +574,14 @@ __device__ HitRecord trace_nearest_packet(const SceneView &S, float3 o, float3 d
         if (overflow) break;
       } else {
         const int lc = -entry - 1;
-        const ChildRec c = load_child(S.nodes, lc / kBvhWidth, lc % kBvhWidth);
+        const ChildRec c = load_child<kGeo>(S, lc / kBvhWidth, lc % kBvhWidth);
         float tn;
         const bool need = active && slab(c.lo, c.hi, o, idir, kRayEps, closest, tn);
         for (int i = 0; i < c.count; ++i) {
           const float4 *r = reinterpret_cast<const float4 *>(S.tris + c.child + i);
           const float4 a = __ldg(r), b = __ldg(r + 1), q = __ldg(r + 2);
           float t, u, v;
-          if (need && intersect_tri(d, o, f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, q.x), t, u, v) &&
-              t < closest) {
+          if (need && tri_hit<kGeo>(wr, d, o, a, b, q, t, u, v) && t < closest) {
             closest = t;
             h.hit = 1; h.tri = c.child + i; h.t = t; h.u = u; h.v = v;
           }
@@ -493,10 +601,11 @@ __device__ HitRecord trace_nearest_packet(const SceneView &S, float3 o, float3 d
 
 // Any hit toward the light (trace_shadow_ray_any_hit, device_ray.hpp:81-135):
 // skips the camera-hit triangle, t in (kRayEps, 1e30); overflow counts as occluded.
+template <int kGeo>
 DVS_SHADE_INLINE __device__ bool trace_shadow_packet(const SceneView &S, float3 o, float3 d, bool active, int self,
-                                                     int *stack_code,
-                                    float *stack_t) {
+                                                     int *stack_code, float *stack_t) {
   const float3 idir = inverse_direction(d);
+  const WtRay wr = wt_ray<kGeo>(d);
   bool alive = active;
   bool occluded = false;
   const float t_max = 1e30f;
@@ -509,7 +618,7 @@ DVS_SHADE_INLINE __device__ bool trace_shadow_packet(const SceneView &S, float3 
     if (entry >= 0) {
       int next;
       float next_t;
-      if (expand_node<false>(S, entry, P, o, idir, alive, kRayEps, alive ? t_max : -1.0f, t_max, st, next, next_t,
+      if (expand_node<false, kGeo>(S, entry, P, o, idir, alive, kRayEps, alive ? t_max : -1.0f, t_max, st, next, next_t,
                              overflow)) {
         entry = next;
         entry_t = next_t;
@@ -521,7 +630,7 @@ DVS_SHADE_INLINE __device__ bool trace_shadow_packet(const SceneView &S, float3 
       }
     } else {
       const int lc = -entry - 1;
-      const ChildRec c = load_child(S.nodes, lc / kBvhWidth, lc % kBvhWidth);
+      const ChildRec c = load_child<kGeo>(S, lc / kBvhWidth, lc % kBvhWidth);
       float tn;
       const bool need = alive && slab(c.lo, c.hi, o, idir, kRayEps, t_max, tn);
       for (int i = 0; i < c.count; ++i) {
@@ -530,7 +639,7 @@ DVS_SHADE_INLINE __device__ bool trace_shadow_packet(const SceneView &S, float3 
         const float4 a = __ldg(r), b = __ldg(r + 1), q = __ldg(r + 2);
         float t, u, v;
         if (need && alive && id != self &&
-            intersect_tri(d, o, f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, q.x), t, u, v) && t > kRayEps &&
+            tri_hit<kGeo>(wr, d, o, a, b, q, t, u, v) && t > kRayEps &&
             t < t_max) {
           occluded = true;
           alive = false;
@@ -565,6 +674,16 @@ __device__ float3 shadow_origin(float3 a, float3 e1, float3 e2, float u, float v
   return point;
 }
 
+// shadow_origin from a record (a, b, c = its three float4s): the edges are
+// stored, or v1 - v0, v2 - v0 with the same float subtraction (watertight
+// scenes), so both give the reference's edge bits.
+template <int kGeo>
+__device__ __forceinline__ float3 shadow_origin_rec(float4 a, float4 b, float4 c, float u, float v, float3 light) {
+  const float3 v0 = f3(a.x, a.y, a.z), p = f3(a.w, b.x, b.y), q = f3(b.z, b.w, c.x);
+  if constexpr (!(kGeo & kGeoWatertight)) return shadow_origin(v0, p, q, u, v, light);
+  else return shadow_origin(v0, p - v0, q - v0, u, v, light);
+}
+
 struct PixelSample {
   double radiance;
   float depth;
@@ -590,7 +709,7 @@ __device__ __forceinline__ float subray_y(const SceneView &S, int py_i, int sy) 
 // cos4_table: when every lane of the warp samples the same pixel, the FP64
 // cos^4 of each sub-ray is computed once per warp (shared memory) instead of
 // once per lane; otherwise nullptr.
-template <int kMode>
+template <int kMode, int kGeo = kGeoReference>
 __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool active, const CellPose &pose,
                                            int *stack_code, float *stack_t, const double *cos4_table) {
   PixelSample out{0.0, -1.0f, true, 0u, 0u};
@@ -606,7 +725,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
       const float px = subray_x(S, px_i, sx);
       const float py = subray_y(S, py_i, sy);
       const float3 ray = normalize(rotate_ray(pose, f3(px, -py, -1)));
-      const HitRecord hit = trace_nearest_packet(S, origin, ray, active && out.valid, stack_code, stack_t);
+      const HitRecord hit = trace_nearest_packet<kGeo>(S, origin, ray, active && out.valid, stack_code, stack_t);
       if (active && out.valid) ++out.primary;
       if (hit.hit < 0) out.valid = false;
       const bool hitp = active && out.valid && hit.hit == 1;
@@ -628,7 +747,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
           if (lit) {
             const float4 *r = reinterpret_cast<const float4 *>(S.tris + hit.tri);
             const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
-            sorigin = shadow_origin(f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, c.x), hit.u, hit.v, light);
+            sorigin = shadow_origin_rec<kGeo>(a, b, c, hit.u, hit.v, light);
             if (S.has_albedo) {
               albedo = s0.w * w + s1.w * hit.u + s2.w * hit.v;
               r0 = hfunc_r0(albedo);
@@ -639,7 +758,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
       if (kMode != kDepthOnly) {
         if (__any_sync(kFull, lit)) {
           if (lit) ++out.shadow;
-          const bool occ = trace_shadow_packet(S, sorigin, light, lit, hit.tri, stack_code, stack_t);
+          const bool occ = trace_shadow_packet<kGeo>(S, sorigin, light, lit, hit.tri, stack_code, stack_t);
           if (lit && !occ) {
             const double cos4 = cos4_table ? cos4_table[sy * ss + sx] : cos4_of(px, py);
             // hapke_directional_reflectance (hapke.hpp:153-157)
@@ -711,7 +830,7 @@ __device__ Packet make_packet_r(const SceneView &S, const float3 (&o)[R], const 
   return P;
 }
 
-template <bool kSorted, int R>
+template <bool kSorted, int R, int kGeo>
 __device__ __forceinline__ bool expand_node_r(const SceneView &S, int node, const Packet &P, const float3 (&o)[R],
                                               const float3 (&idir)[R], const bool (&live)[R], float t_min,
                                               const float (&lane_tmax)[R], float packet_tmax, Stack &st, int &next,
@@ -722,7 +841,7 @@ __device__ __forceinline__ bool expand_node_r(const SceneView &S, int node, cons
   int code = 0;
   if (P.coherent) {
     if (lane < kBvhWidth) {
-      const ChildRec c = load_child(S.nodes, node, lane);
+      const ChildRec c = load_child<kGeo>(S, node, lane);
       if (c.count >= 0) {
         hit = packet_slab(c, P, t_min, packet_tmax, key);
         code = c.count > 0 ? leaf_code(node, lane) : c.child;
@@ -730,7 +849,7 @@ __device__ __forceinline__ bool expand_node_r(const SceneView &S, int node, cons
     }
   } else {
     for (int slot = 0; slot < kBvhWidth; ++slot) {
-      const ChildRec c = load_child(S.nodes, node, slot);
+      const ChildRec c = load_child<kGeo>(S, node, slot);
       float near = kInf();
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -790,14 +909,16 @@ __device__ __forceinline__ float lane_reach(const bool (&active)[R], const float
   return m;
 }
 
-template <int R>
+template <int R, int kGeo>
 __device__ void trace_nearest_packet_r(const SceneView &S, const float3 (&o)[R], const float3 (&d)[R],
                                        const bool (&active)[R], int *stack_code, float *stack_t, HitRecord (&h)[R]) {
   float3 idir[R];
   float closest[R];
+  WtRay wr[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     idir[r] = inverse_direction(d[r]);
+    wr[r] = wt_ray<kGeo>(d[r]);
     closest[r] = active[r] ? 1e30f : -1.0f;
     h[r] = HitRecord{0, -1, 0.f, 0.f, 0.f};
   }
@@ -812,7 +933,7 @@ __device__ void trace_nearest_packet_r(const SceneView &S, const float3 (&o)[R],
       if (entry >= 0) {
         int next;
         float next_t;
-        if (expand_node_r<true, R>(S, entry, P, o, idir, active, kRayEps, closest, packet_tmax, st, next, next_t,
+        if (expand_node_r<true, R, kGeo>(S, entry, P, o, idir, active, kRayEps, closest, packet_tmax, st, next, next_t,
                                    overflow)) {
           entry = next;
           entry_t = next_t;
@@ -821,7 +942,7 @@ __device__ void trace_nearest_packet_r(const SceneView &S, const float3 (&o)[R],
         if (overflow) break;
       } else {
         const int lc = -entry - 1;
-        const ChildRec c = load_child(S.nodes, lc / kBvhWidth, lc % kBvhWidth);
+        const ChildRec c = load_child<kGeo>(S, lc / kBvhWidth, lc % kBvhWidth);
         bool need[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -831,11 +952,10 @@ __device__ void trace_nearest_packet_r(const SceneView &S, const float3 (&o)[R],
         for (int i = 0; i < c.count; ++i) {
           const float4 *q4 = reinterpret_cast<const float4 *>(S.tris + c.child + i);
           const float4 a = __ldg(q4), b = __ldg(q4 + 1), q = __ldg(q4 + 2);
-          const float3 v0 = f3(a.x, a.y, a.z), e1 = f3(a.w, b.x, b.y), e2 = f3(b.z, b.w, q.x);
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             float t, u, v;
-            if (need[r] && intersect_tri(d[r], o[r], v0, e1, e2, t, u, v) && t < closest[r]) {
+            if (need[r] && tri_hit<kGeo>(wr[r], d[r], o[r], a, b, q, t, u, v) && t < closest[r]) {
               closest[r] = t;
               h[r].hit = 1; h[r].tri = c.child + i; h[r].t = t; h[r].u = u; h[r].v = v;
             }
@@ -855,10 +975,11 @@ __device__ void trace_nearest_packet_r(const SceneView &S, const float3 (&o)[R],
     for (int r = 0; r < R; ++r) h[r].hit = -1;
 }
 
-template <int R>
+template <int R, int kGeo>
 __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], float3 light, const bool (&active)[R],
                                       const int (&self)[R], int *stack_code, float *stack_t, bool (&occluded)[R]) {
   const float3 idir1 = inverse_direction(light);
+  const WtRay wr = wt_ray<kGeo>(light);
   float3 d[R], idir[R];
   bool alive[R];
   float reach[R];
@@ -884,7 +1005,7 @@ __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], 
       for (int r = 0; r < R; ++r) reach[r] = alive[r] ? t_max : -1.0f;
       int next;
       float next_t;
-      if (expand_node_r<false, R>(S, entry, P, o, idir, alive, kRayEps, reach, t_max, st, next, next_t, overflow)) {
+      if (expand_node_r<false, R, kGeo>(S, entry, P, o, idir, alive, kRayEps, reach, t_max, st, next, next_t, overflow)) {
         entry = next;
         continue;
       }
@@ -895,7 +1016,7 @@ __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], 
       }
     } else {
       const int lc = -entry - 1;
-      const ChildRec c = load_child(S.nodes, lc / kBvhWidth, lc % kBvhWidth);
+      const ChildRec c = load_child<kGeo>(S, lc / kBvhWidth, lc % kBvhWidth);
       bool need[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -906,11 +1027,10 @@ __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], 
         const int id = c.child + i;
         const float4 *q4 = reinterpret_cast<const float4 *>(S.tris + id);
         const float4 a = __ldg(q4), b = __ldg(q4 + 1), q = __ldg(q4 + 2);
-        const float3 v0 = f3(a.x, a.y, a.z), e1 = f3(a.w, b.x, b.y), e2 = f3(b.z, b.w, q.x);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           float t, u, v;
-          if (need[r] && alive[r] && id != self[r] && intersect_tri(light, o[r], v0, e1, e2, t, u, v) &&
+          if (need[r] && alive[r] && id != self[r] && tri_hit<kGeo>(wr, light, o[r], a, b, q, t, u, v) &&
               t > kRayEps && t < t_max) {
             occluded[r] = true;
             alive[r] = false;
@@ -928,7 +1048,7 @@ __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], 
 // sample_pixel_packet with R neighbouring sub-rays per lane (ss^2 a multiple
 // of R).  The per-ray work, the order of the FP64 radiance and depth sums and
 // the ray counts are those of the one-ray loop.
-template <int kMode, int R>
+template <int kMode, int R, int kGeo = kGeoReference>
 __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool active, const CellPose &pose,
                                           int *stack_code, float *stack_t, const double *cos4_table) {
   PixelSample out{0.0, -1.0f, true, 0u, 0u};
@@ -953,7 +1073,7 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
       live[r] = active && out.valid;
     }
     HitRecord hit[R];
-    trace_nearest_packet_r<R>(S, org, ray, live, stack_code, stack_t, hit);
+    trace_nearest_packet_r<R, kGeo>(S, org, ray, live, stack_code, stack_t, hit);
     bool lit[R];
     float3 normal[R], sorigin[R];
     float albedo[R], r0[R];
@@ -984,8 +1104,7 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
           if (lit[r]) {
             const float4 *t4 = reinterpret_cast<const float4 *>(S.tris + hit[r].tri);
             const float4 a = __ldg(t4), b = __ldg(t4 + 1), c = __ldg(t4 + 2);
-            sorigin[r] = shadow_origin(f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, c.x), hit[r].u, hit[r].v,
-                                       light);
+            sorigin[r] = shadow_origin_rec<kGeo>(a, b, c, hit[r].u, hit[r].v, light);
             if (S.has_albedo) {
               albedo[r] = s0.w * w + s1.w * hit[r].u + s2.w * hit[r].v;
               r0[r] = hfunc_r0(albedo[r]);
@@ -1000,7 +1119,7 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
       for (int r = 0; r < R; ++r) any_lit = any_lit || lit[r];
       if (__any_sync(kFull, any_lit)) {
         bool occ[R];
-        trace_shadow_packet_r<R>(S, sorigin, light, lit, self, stack_code, stack_t, occ);
+        trace_shadow_packet_r<R, kGeo>(S, sorigin, light, lit, self, stack_code, stack_t, occ);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           if (lit[r]) ++out.shadow;
@@ -1026,7 +1145,7 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
 // radiance and depth sums in sub-ray order through shuffles, so the result is
 // the same double as the serial loop of sample_pixel_packet.  Called by all
 // 32 lanes with warp-uniform arguments; the result is valid in lane 0.
-template <int kMode>
+template <int kMode, int kGeo = kGeoReference>
 __device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const CellPose &pose, int *stack_code,
                                             float *stack_t) {
   constexpr int R = 2;
@@ -1055,7 +1174,7 @@ __device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const
       org[r] = origin;
     }
     HitRecord hit[R];
-    trace_nearest_packet_r<R>(S, org, ray, live, stack_code, stack_t, hit);
+    trace_nearest_packet_r<R, kGeo>(S, org, ray, live, stack_code, stack_t, hit);
     bool ovf = false, lit[R], hitp[R];
     float3 normal[R], sorigin[R];
     float albedo[R], r0[R];
@@ -1080,8 +1199,7 @@ __device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const
         if (lit[r]) {
           const float4 *t4 = reinterpret_cast<const float4 *>(S.tris + hit[r].tri);
           const float4 a = __ldg(t4), b = __ldg(t4 + 1), c = __ldg(t4 + 2);
-          sorigin[r] = shadow_origin(f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, c.x), hit[r].u, hit[r].v,
-                                     light);
+          sorigin[r] = shadow_origin_rec<kGeo>(a, b, c, hit[r].u, hit[r].v, light);
           if (S.has_albedo) {
             albedo[r] = s0.w * w + s1.w * hit[r].u + s2.w * hit[r].v;
             r0[r] = hfunc_r0(albedo[r]);
@@ -1092,7 +1210,7 @@ __device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const
     double term[R] = {0.0, 0.0};
     if (kMode != kDepthOnly && __any_sync(kFull, lit[0] || lit[1])) {
       bool occ[R];
-      trace_shadow_packet_r<R>(S, sorigin, light, lit, self, stack_code, stack_t, occ);
+      trace_shadow_packet_r<R, kGeo>(S, sorigin, light, lit, self, stack_code, stack_t, occ);
 #pragma unroll
       for (int r = 0; r < R; ++r)
         if (lit[r] && !occ[r]) {

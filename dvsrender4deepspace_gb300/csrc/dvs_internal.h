@@ -29,10 +29,36 @@ struct alignas(256) BvhNode {
 static_assert(sizeof(BvhChild) == 32, "BvhChild layout");
 static_assert(sizeof(BvhNode) == 256, "BvhNode layout");
 
+// Precision-format node (FP16 child bounds), 144 bytes: a 16-byte header with
+// the node's FP32 origin (the minimum corner of its children) and eight
+// 16-byte children.  A child's bounds are FP16 offsets from the origin, lower
+// bounds rounded toward -inf and upper bounds toward +inf; the device adds
+// them to the origin with the same directed rounding (__fadd_rd/__fadd_ru),
+// so a decoded box always encloses the FP32 box.  link: inner child = node
+// index (bit 31 clear); leaf = bit 31 | (triangles - 1) << 27 | first
+// triangle (27 bits); empty slot = all ones.
+struct alignas(16) BvhQChild {
+  uint16_t lo[3];
+  uint16_t hi[3];
+  uint32_t link;
+};
+struct alignas(16) BvhQNode {
+  float origin[3];
+  uint32_t pad;
+  BvhQChild c[kBvhWidth];
+};
+static_assert(sizeof(BvhQChild) == 16, "BvhQChild layout");
+static_assert(sizeof(BvhQNode) == 144, "BvhQNode layout");
+constexpr uint32_t kQLinkEmpty = 0xffffffffu;
+constexpr uint32_t kQLinkLeaf = 0x80000000u;
+constexpr uint32_t kQLinkFirstMask = 0x07ffffffu;
+constexpr int kQLinkCountShift = 27;
+
 // Intersection record in leaf order, 48 bytes = 3 x 16-byte loads.  Edges are
 // precomputed with the same float subtraction the reference performs per test
 // (include/dvs/device_ray.hpp:58-59), so the Moller-Trumbore inputs are
-// bit-identical.
+// bit-identical.  Precision scenes store the vertices instead (v0, v1, v2 in
+// the v0/e1/e2 slots) for the watertight test.
 struct alignas(16) TriRecord {
   float v0[3];
   float e1[3];
@@ -68,6 +94,11 @@ struct BvhBuild {
 // Returns false with a message on invalid input.
 bool build_bvh(const float *vertices, size_t n_vertices, const uint32_t *indices, size_t n_triangles,
                int leaf_size, BvhBuild &out, std::string &error);
+
+// The precision-format copy of a built tree (same node indices).  Fails when a
+// leaf's first triangle or size does not fit the link, or when a decoded box
+// would not enclose its FP32 box (checked for every child).
+bool quantize_bvh(const std::vector<BvhNode> &nodes, std::vector<BvhQNode> &out, std::string &error);
 
 // ---- FIFO readout (src/event_readout.cpp:6-34 semantics) ---------------------
 struct HostEvent {

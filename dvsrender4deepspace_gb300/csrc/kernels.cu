@@ -81,7 +81,7 @@ constexpr int kCos4Table = 256;    // sub-rays per pixel with a shared cos^4 tab
 #define DVS_TRACE_QUAD_MIN_BLOCKS 3
 #endif
 
-template <int kMode, int kRays>
+template <int kMode, int kRays, int kGeo>
 __global__ void __launch_bounds__(128, kRays == 4   ? DVS_TRACE_QUAD_MIN_BLOCKS
                                        : kRays == 2 ? DVS_TRACE_PAIR_MIN_BLOCKS
                                                     : DVS_TRACE_MIN_BLOCKS)
@@ -115,10 +115,10 @@ __global__ void __launch_bounds__(128, kRays == 4   ? DVS_TRACE_QUAD_MIN_BLOCKS
     __syncwarp();
   }
   const PixelSample s =
-      kRays > 1 ? sample_pixel_group<kMode, kRays>(S, pixel, active, pose, s_code[wib], s_t[wib],
-                                                   shared_cos4 ? s_cos4[wib] : nullptr)
-                : sample_pixel_packet<kMode>(S, pixel, active, pose, s_code[wib], s_t[wib],
-                                             shared_cos4 ? s_cos4[wib] : nullptr);
+      kRays > 1 ? sample_pixel_group<kMode, kRays, kGeo>(S, pixel, active, pose, s_code[wib], s_t[wib],
+                                                         shared_cos4 ? s_cos4[wib] : nullptr)
+                : sample_pixel_packet<kMode, kGeo>(S, pixel, active, pose, s_code[wib], s_t[wib],
+                                                   shared_cos4 ? s_cos4[wib] : nullptr);
   if (active) {
     const size_t o = (size_t)cell * n_pix + rank;
     radiance[o] = s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll);
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(128, kRays == 4   ? DVS_TRACE_QUAD_MIN_BLOCKS
 // Few poses per pixel: one warp per (pixel, pose), lanes carrying the
 // pixel's sub-rays (sample_pixel_subrays).  Item w = (rank, cell) with
 // consecutive warps on the same pixel.
-template <int kMode>
+template <int kMode, int kGeo>
 __global__ void __launch_bounds__(128, DVS_TRACE_PAIR_MIN_BLOCKS)
     trace_subray_kernel(SceneView S, int n_pix, const int32_t *rank_list, const CellPose *poses, int c0, int nc,
                         double *radiance, float *depth_out, unsigned long long *counters) {
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(128, DVS_TRACE_PAIR_MIN_BLOCKS)
   const int rank = (int)(warp / nc), cell = (int)(warp % nc);
   const int pixel = __ldg(S.pixel_of_rank + (rank_list ? rank_list[rank] : rank));
   const CellPose pose = poses[c0 + cell];
-  const PixelSample s = sample_pixel_subrays<kMode>(S, pixel, pose, s_code[wib], s_t[wib]);
+  const PixelSample s = sample_pixel_subrays<kMode, kGeo>(S, pixel, pose, s_code[wib], s_t[wib]);
   if (lane == 0) {
     const size_t o = (size_t)cell * n_pix + rank;
     radiance[o] = s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll);
@@ -300,6 +300,7 @@ __global__ void emit_events_kernel(int n, const int32_t *pixel_of_rank, int widt
   }
 }
 
+template <int kGeo>
 __global__ void __launch_bounds__(128) event_depth_kernel(SceneView S, const dvs_optical_interval *ivs, int n_ivs,
                                                           DevEvent *events, const int32_t *count, int32_t *error,
                                                           unsigned long long *counters) {
@@ -323,7 +324,7 @@ __global__ void __launch_bounds__(128) event_depth_kernel(SceneView S, const dvs
     }
     const CellPose pose = pose_at(ivs[lo], ev.t);
     const int pixel = active ? S.pixel_of_rank[ev.rank] : 0;
-    const PixelSample s = sample_pixel_packet<kDepthOnly>(S, pixel, active, pose, s_code[wib], s_t[wib], nullptr);
+    const PixelSample s = sample_pixel_packet<kDepthOnly, kGeo>(S, pixel, active, pose, s_code[wib], s_t[wib], nullptr);
     if (active) {
       if (!s.valid) atomicOr(error, kErrOptical);
       events[e].depth = s.depth;
@@ -382,39 +383,65 @@ cudaError_t launch_cell_poses(const dvs_optical_interval *ivs, const Cell *cells
   return cudaGetLastError();
 }
 
-cudaError_t launch_trace_list(const SceneView &scene, int n_pix, const int32_t *rank_list, const CellPose *poses,
-                              int c0, int nc, int cw_log2, double *radiance, float *depth, unsigned long long *counters,
-                              cudaStream_t s) {
-  if (n_pix <= 0 || nc <= 0) return cudaSuccess;
+namespace {
+template <int kGeo>
+void trace_list_geo(const SceneView &scene, int n_pix, const int32_t *rank_list, const CellPose *poses, int c0, int nc,
+                    int cw_log2, double *radiance, float *depth, unsigned long long *counters, cudaStream_t s) {
   if (scene.samples * scene.samples >= 32 && nc <= 8) {
     // few poses per pixel: sub-ray packets (one warp per pixel and pose)
     const int grid = blocks((long long)n_pix * nc * 32, 128);
     if (depth)
-      trace_subray_kernel<kRadianceDepth><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, radiance, depth,
-                                                               counters);
+      trace_subray_kernel<kRadianceDepth, kGeo><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, radiance,
+                                                                     depth, counters);
     else
-      trace_subray_kernel<kRadiance><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, radiance, nullptr,
-                                                          counters);
-    return cudaGetLastError();
+      trace_subray_kernel<kRadiance, kGeo><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, radiance,
+                                                                nullptr, counters);
+    return;
   }
   const int cw = 1 << cw_log2, ppw = 32 >> cw_log2;
   const long long warps = (long long)((n_pix + ppw - 1) / ppw) * ((nc + cw - 1) / cw);
   const int ss2 = scene.samples * scene.samples;
-  const int rays = (scene.rays >= 4 && ss2 % 4 == 0) ? 4 : (scene.rays >= 2 && ss2 % 2 == 0) ? 2 : 1;
+  // four rays per lane only in the reference format (the others keep two)
+  const int rays = (kGeo == kGeoReference && scene.rays >= 4 && ss2 % 4 == 0) ? 4
+                   : (scene.rays >= 2 && ss2 % 2 == 0)                       ? 2
+                                                                              : 1;
   const int grid = blocks(warps * 32, 128);
-#define DVS_TRACE_LAUNCH(MODE, RAYS, DEPTH)                                                                  \
-  trace_cells_kernel<MODE, RAYS><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2, radiance, \
-                                                      DEPTH, counters)
+#define DVS_TRACE_LAUNCH(MODE, RAYS, DEPTH)                                                                         \
+  trace_cells_kernel<MODE, RAYS, kGeo><<<grid, 128, 0, s>>>(scene, n_pix, rank_list, poses, c0, nc, cw_log2,       \
+                                                            radiance, DEPTH, counters)
   if (depth) {
-    if (rays == 4) DVS_TRACE_LAUNCH(kRadianceDepth, 4, depth);
-    else if (rays == 2) DVS_TRACE_LAUNCH(kRadianceDepth, 2, depth);
+    if constexpr (kGeo == kGeoReference)
+      if (rays == 4) { DVS_TRACE_LAUNCH(kRadianceDepth, 4, depth); return; }
+    if (rays == 2) DVS_TRACE_LAUNCH(kRadianceDepth, 2, depth);
     else DVS_TRACE_LAUNCH(kRadianceDepth, 1, depth);
   } else {
-    if (rays == 4) DVS_TRACE_LAUNCH(kRadiance, 4, nullptr);
-    else if (rays == 2) DVS_TRACE_LAUNCH(kRadiance, 2, nullptr);
+    if constexpr (kGeo == kGeoReference)
+      if (rays == 4) { DVS_TRACE_LAUNCH(kRadiance, 4, nullptr); return; }
+    if (rays == 2) DVS_TRACE_LAUNCH(kRadiance, 2, nullptr);
     else DVS_TRACE_LAUNCH(kRadiance, 1, nullptr);
   }
 #undef DVS_TRACE_LAUNCH
+}
+}  // namespace
+
+cudaError_t launch_trace_list(const SceneView &scene, int n_pix, const int32_t *rank_list, const CellPose *poses,
+                              int c0, int nc, int cw_log2, double *radiance, float *depth, unsigned long long *counters,
+                              cudaStream_t s) {
+  if (n_pix <= 0 || nc <= 0) return cudaSuccess;
+  switch (scene.geometry) {
+    case kGeoHalfBounds:
+      trace_list_geo<kGeoHalfBounds>(scene, n_pix, rank_list, poses, c0, nc, cw_log2, radiance, depth, counters, s);
+      break;
+    case kGeoWatertight:
+      trace_list_geo<kGeoWatertight>(scene, n_pix, rank_list, poses, c0, nc, cw_log2, radiance, depth, counters, s);
+      break;
+    case kGeoHalfBounds | kGeoWatertight:
+      trace_list_geo<kGeoHalfBounds | kGeoWatertight>(scene, n_pix, rank_list, poses, c0, nc, cw_log2, radiance,
+                                                      depth, counters, s);
+      break;
+    default:
+      trace_list_geo<kGeoReference>(scene, n_pix, rank_list, poses, c0, nc, cw_log2, radiance, depth, counters, s);
+  }
   return cudaGetLastError();
 }
 
@@ -473,7 +500,20 @@ cudaError_t launch_event_depth(const SceneView &scene, const dvs_optical_interva
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  event_depth_kernel<<<sms * 4, 128, 0, s>>>(scene, ivs, n_ivs, events, count, error, counters);
+  switch (scene.geometry) {
+    case kGeoHalfBounds:
+      event_depth_kernel<kGeoHalfBounds><<<sms * 4, 128, 0, s>>>(scene, ivs, n_ivs, events, count, error, counters);
+      break;
+    case kGeoWatertight:
+      event_depth_kernel<kGeoWatertight><<<sms * 4, 128, 0, s>>>(scene, ivs, n_ivs, events, count, error, counters);
+      break;
+    case kGeoHalfBounds | kGeoWatertight:
+      event_depth_kernel<kGeoHalfBounds | kGeoWatertight><<<sms * 4, 128, 0, s>>>(scene, ivs, n_ivs, events, count,
+                                                                                 error, counters);
+      break;
+    default:
+      event_depth_kernel<kGeoReference><<<sms * 4, 128, 0, s>>>(scene, ivs, n_ivs, events, count, error, counters);
+  }
   return cudaGetLastError();
 }
 

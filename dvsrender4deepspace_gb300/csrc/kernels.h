@@ -9,7 +9,9 @@
 namespace dvsgb {
 
 struct SceneView {
-  const BvhNode *nodes;
+  const BvhNode *nodes;       // reference geometry (FP32 child bounds)
+  const BvhQNode *qnodes;     // FP16 child bounds (geometry bit 0), same indices
+  int32_t geometry;           // bit 0: qnodes instead of nodes; bit 1: watertight test on vertex records
   const TriRecord *tris;
   const ShadeRecord *shade;
   const int32_t *pixel_of_rank;  // Morton rank -> row-major pixel index

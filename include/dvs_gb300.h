@@ -107,9 +107,18 @@ typedef struct {
                                  the reference's XORWOW stream (native solver only) */
 } dvs_sensor_options;
 
+#define DVS_BVH_HALF_BOUNDS 1
+#define DVS_BVH_WATERTIGHT 2
 typedef struct {
   int32_t leaf_size;          /* triangles per BVH leaf, 1..8 (0: 2, wider when the tree is too deep) */
-  int32_t reserved[3];
+  int32_t precision;          /* geometry flags; 0 = the reference's: FP32 child bounds and its
+                                 Moller-Trumbore test (device_ray.hpp:54-80).  DVS_BVH_HALF_BOUNDS:
+                                 FP16 child bounds quantised outward against a per-node FP32 origin
+                                 (144-byte nodes instead of 256; same hits, meshes of at most 2^27
+                                 triangles).  DVS_BVH_WATERTIGHT: the watertight FP32 triangle test
+                                 (Woop et al. 2013) on stored vertices.  No counterpart in the
+                                 reference. */
+  int32_t reserved[2];
 } dvs_bvh_params;
 
 typedef struct {
@@ -118,7 +127,7 @@ typedef struct {
   uint64_t device_bytes;
   double build_seconds;
   int32_t leaf_size;          /* triangles per leaf the tree was built with */
-  int32_t reserved;
+  int32_t precision;          /* dvs_bvh_params.precision flags of the tree */
 } dvs_scene_info;
 
 typedef struct {

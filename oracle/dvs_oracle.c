@@ -517,11 +517,65 @@ static inline rv3 vtx(const oscene *s, uint32_t i) { return from_f3(s->vertices[
 
 typedef struct { int hit, tri; real t, u, v; } rhit;
 
+/* Watertight ray/triangle test of the precision geometry (no reference
+ * counterpart; the published algorithm of Woop, Benthin and Wald, "Watertight
+ * Ray/Triangle Intersection", JCGT 2(1), 2013), in the operation order of the
+ * CUDA kernels: shear onto +z along the dominant axis kz (kx/ky swapped when
+ * the direction is negative there), 2-D edge functions U, V, W of the
+ * projected vertices, an FP64 recomputation when one rounds to zero, all-same
+ * signs for a hit; (u, v) = (V, W) / det in the reference's convention. */
+typedef struct { int kx, ky, kz; real sx, sy, sz; } wt_ray;
+static real comp3(rv3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+static wt_ray wt_setup(rv3 d) {
+  const real ax = fabs(d.x), ay = fabs(d.y), az = fabs(d.z);
+  wt_ray w;
+  w.kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+  w.kx = w.kz == 2 ? 0 : w.kz + 1;
+  w.ky = w.kx == 2 ? 0 : w.kx + 1;
+  const real dz = comp3(d, w.kz);
+  if (dz < R(0.0)) { const int k = w.kx; w.kx = w.ky; w.ky = k; }
+  w.sx = comp3(d, w.kx) / dz;
+  w.sy = comp3(d, w.ky) / dz;
+  w.sz = R(1.0) / dz;
+  return w;
+}
+static int intersect_watertight(const wt_ray *w, rv3 o, rv3 v0, rv3 v1, rv3 v2, real *out_t, real *out_u,
+                                real *out_v) {
+  const rv3 A = sub3(v0, o), B = sub3(v1, o), C = sub3(v2, o);
+  const real az = comp3(A, w->kz), bz = comp3(B, w->kz), cz = comp3(C, w->kz);
+  const real ax = comp3(A, w->kx) - w->sx * az, ay = comp3(A, w->ky) - w->sy * az;
+  const real bx = comp3(B, w->kx) - w->sx * bz, by = comp3(B, w->ky) - w->sy * bz;
+  const real cx = comp3(C, w->kx) - w->sx * cz, cy = comp3(C, w->ky) - w->sy * cz;
+  real U = cx * by - cy * bx, V = ax * cy - ay * cx, W = bx * ay - by * ax;
+  if (U == R(0.0) || V == R(0.0) || W == R(0.0)) {
+    U = (real)((double)cx * (double)by - (double)cy * (double)bx);
+    V = (real)((double)ax * (double)cy - (double)ay * (double)cx);
+    W = (real)((double)bx * (double)ay - (double)by * (double)ax);
+  }
+  if ((U < R(0.0) || V < R(0.0) || W < R(0.0)) && (U > R(0.0) || V > R(0.0) || W > R(0.0))) return 0;
+  const real det = U + V + W;
+  if (det == R(0.0)) return 0;
+  const real T = U * (w->sz * az) + V * (w->sz * bz) + W * (w->sz * cz);
+  const real rcp = R(1.0) / det;
+  const real t = T * rcp;
+  if (!(t > kRayEps)) return 0;
+  *out_t = t; *out_u = V * rcp; *out_v = W * rcp;
+  return 1;
+}
+/* The scene's triangle test: Moller-Trumbore or, in a precision scene, the
+ * watertight test with the ray's shear w. */
+static int scene_triangle(const oscene *s, const wt_ray *w, rv3 ray, rv3 o, rv3 v0, rv3 v1, rv3 v2, real *t,
+                          real *u, real *v) {
+  return s->watertight ? intersect_watertight(w, o, v0, v1, v2, t, u, v)
+                       : intersect_triangle(ray, o, v0, v1, v2, t, u, v);
+}
+
 static rhit trace_nearest_r(const oscene *s, rv3 origin, rv3 ray) {
   /* device_ray.hpp:136-158 */
   rhit hit = {0, -1, 0, 0, 0};
   real closest = R(1e30);
   rv3 idir = inverse_direction(ray);
+  const wt_ray w = wt_setup(ray);
   int stack[kMaxStackSize], sp = 0;
   stack[sp++] = s->root;
   while (sp > 0) {
@@ -531,7 +585,7 @@ static rhit trace_nearest_r(const oscene *s, rv3 origin, rv3 ray) {
         int id = node->start + i;
         const uint32_t *tri = &s->indices[3 * (size_t)id];
         real t, u, v;
-        if (intersect_triangle(ray, origin, vtx(s, tri[0]), vtx(s, tri[1]), vtx(s, tri[2]), &t, &u, &v) &&
+        if (scene_triangle(s, &w, ray, origin, vtx(s, tri[0]), vtx(s, tri[1]), vtx(s, tri[2]), &t, &u, &v) &&
             t < closest) {
           closest = t; hit.hit = 1; hit.tri = id; hit.t = t; hit.u = u; hit.v = v;
         }
@@ -556,6 +610,7 @@ static rhit trace_nearest_r(const oscene *s, rv3 origin, rv3 ray) {
 static int trace_shadow_r(const oscene *s, rv3 origin, rv3 dir, int self, real t_min, real t_max) {
   /* trace_shadow_ray_any_hit, device_ray.hpp:81-135 */
   rv3 idir = inverse_direction(dir);
+  const wt_ray w = wt_setup(dir);
   int stack[kMaxStackSize], sp = 0;
   stack[sp++] = s->root;
   while (sp > 0) {
@@ -566,7 +621,7 @@ static int trace_shadow_r(const oscene *s, rv3 origin, rv3 dir, int self, real t
         if (id == self) continue;
         const uint32_t *tri = &s->indices[3 * (size_t)id];
         real t, u, v;
-        if (intersect_triangle(dir, origin, vtx(s, tri[0]), vtx(s, tri[1]), vtx(s, tri[2]), &t, &u, &v))
+        if (scene_triangle(s, &w, dir, origin, vtx(s, tri[0]), vtx(s, tri[1]), vtx(s, tri[2]), &t, &u, &v))
           if (t > t_min && t < t_max) return 1;
       }
       continue;

@@ -71,6 +71,8 @@ typedef struct {
   int root, width, height, samples;
   float fx, fy, cx, cy;
   ohapke hapke;
+  int32_t watertight;         /* 0: Moller-Trumbore (reference); 1: watertight test of the
+                                 precision geometry (Woop et al. 2013) */
 } oscene;
 
 /* PixelParameters / PixelState (include/dvs/pixel_model.hpp:7-16). */

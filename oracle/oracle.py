@@ -49,7 +49,7 @@ class oscene(C.Structure):
                 ("indices", C.c_void_p), ("albedos", C.c_void_p),
                 ("root", C.c_int), ("width", C.c_int), ("height", C.c_int), ("samples", C.c_int),
                 ("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
-                ("hapke", ohapke)]
+                ("hapke", ohapke), ("watertight", C.c_int32)]
 
 
 class opixel_params(C.Structure):
@@ -277,7 +277,7 @@ class OracleScene:
     """Binary-BVH scene built by the oracle's restatement of BVHBuilder::build."""
 
     def __init__(self, vertices, normals, indices, camera, samples, hapke, albedos=None, max_leaf=64,
-                 fp64=False):
+                 fp64=False, watertight=False):
         self.lib = load(fp64)
         self.vertices = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
         self.normals = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
@@ -305,6 +305,7 @@ class OracleScene:
         s.samples = self.samples
         s.fx, s.fy, s.cx, s.cy = (float(camera[k]) for k in ("fx", "fy", "cx", "cy"))
         s.hapke = hapke_struct(hapke)
+        s.watertight = 1 if watertight else 0
         self.s = s
 
     @property
