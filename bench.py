@@ -41,15 +41,18 @@ WORKLOADS = {
     "precision": dict(grid=4096, seed=20260003, camera=dict(width=1280, height=720, fx=1000.0, fy=1000.0, cx=640.0,
                                                             cy=360.0),
                       ss=16, z0=3000.0, z1=500.0, duration=2.0, ground_speed=80.0, sun_elevation=30.0,
-                      intensity=1000.0, time_resolution=1e-6, batch=64),
+                      intensity=1000.0, time_resolution=1e-6, batch=64,
+                      # the config's BVH: quantised FP16 child bounds (FP32 triangle tests); Philox noise
+                      geometry="half", circuit="fp32-philox"),
     # one trajectory of the batching config: 1024^2 terrain (2.09M triangles), ss 4, 10 us horizons
     "orbit": dict(grid=1024, seed=20260002, camera=dict(width=346, height=260, fx=300.0, fy=300.0, cx=173.0,
                                                         cy=130.0),
                   ss=4, z0=1500.0, z1=1500.0, duration=2.0, ground_speed=100.0, sun_elevation=30.0,
-                  intensity=1000.0, time_resolution=1e-5, batch=64),
+                  intensity=1000.0, time_resolution=1e-5, batch=64,
+                  geometry="reference", circuit="fp32"),  # FP32 pixel state, FP64 timestamps
     "small": dict(grid=256, seed=20260001, camera=dict(width=346, height=260, fx=300.0, fy=300.0, cx=173.0, cy=130.0),
                   ss=1, z0=1000.0, z1=1000.0, duration=0.49, ground_speed=50.0, sun_elevation=30.0, intensity=1.0,
-                  time_resolution=1e-5, batch=64),
+                  time_resolution=1e-5, batch=64, geometry="reference", circuit="fp64"),
 }
 HAPKE = dict(b=0.3, c=0.4, hS=0.06, hC=1.0, thetap=0.349066, w=0.25, B_S0=1.0, B_C0=0.0, phi=0.3)
 PHYSIC = dict(threshold_pos=0.2, threshold_neg=0.2, refractory_time=200e-6, readout_bandwidth=5e6,
@@ -60,11 +63,14 @@ PHYSIC = dict(threshold_pos=0.2, threshold_neg=0.2, refractory_time=200e-6, read
               photon_shot_noise=1, reset_thermal_noise=0, random_seed=114514, max_events_per_step=16,
               readout_queue_capacity=1000000)
 METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency vs plain path"
-# DRAM bytes (read + write) per pixel-cell of one trace_cells_kernel launch,
-# from the ncu captures summarised in profiles/trace_cells_kernel_orbit_346x260_ss4.md
-# (precision: a 4-cell launch of the same workload, scaled by the cells traced).
-TRACE_DRAM_BYTES_PER_PIXEL_CELL = {"precision": (32344832 + 1251328) / (4 * 921600),
-                                   "orbit": (22470144 + 407428864) / (640 * 89960)}
+# DRAM bytes (read + write) per pixel-cell of one trace_cells_kernel launch, by
+# workload and BVH format, from the ncu captures summarised in
+# profiles/trace_cells_kernel_orbit_346x260_ss4.md and
+# profiles/launches_precision_1280x720_ss16.md (precision: a 16-cell launch of
+# the FP16-bounds tree, a 4-cell launch of the FP32 one, scaled by the cells traced).
+TRACE_DRAM_BYTES_PER_PIXEL_CELL = {("precision", "half"): (33122816 + 75504384) / (16 * 921600),
+                                   ("precision", "reference"): (32344832 + 1251328) / (4 * 921600),
+                                   ("orbit", "reference"): (22470144 + 407428864) / (640 * 89960)}
 
 
 def dist_env():
@@ -265,16 +271,24 @@ def run_gb300(args):
     if args.adaptive_ms > 0:
         ab = 200
         n_calls = int(math.ceil(args.adaptive_ms * 1e-3 / (float(np.float32(dt)) * ab) - 1e-9))
+        asensor, acircuit = sensor, args.circuit
+        if args.circuit == "fp32-philox":
+            # the adaptive solver keeps the reference's XORWOW stream: a sensor with FP32
+            # arithmetic and that stream, started where the native run stopped
+            acircuit = "fp32"
+            asensor = EventSensor(scene, PHYSIC, timing=True, cells_per_chunk=args.chunk, cells_per_warp=args.cw,
+                                  circuit_precision=acircuit)
+            asensor.initialize(traj.state(t_cursor[0]), t_cursor[0])
         sim0, ev_a, rejected = t_cursor[0], 0, 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for k in range(n_calls):
             ivs = trajectory.horizons(traj, t_cursor[0], dt, ab)
             arr = interval_array(ivs)
-            r = sensor.process_adaptive(arr, 1e-2, check_convergence=(k == 0))
+            r = asensor.process_adaptive(arr, 1e-2, check_convergence=(k == 0))
             if r is None:  # rejected window: the native solver takes it
                 rejected += 1
-                r = sensor.process_many(arr)
+                r = asensor.process_many(arr)
             t_cursor[0] = ivs[-1][3]
             ev_a += len(r)
         torch.cuda.synchronize()
@@ -282,8 +296,8 @@ def run_gb300(args):
         adaptive = {"simulated_s": t_cursor[0] - sim0, "wall_s": wall,
                     "simulated_s_per_wall_s": (t_cursor[0] - sim0) / wall, "events": ev_a,
                     "events_per_s": ev_a / wall, "calls": n_calls, "horizons_per_call": ab,
-                    "rejected_windows": rejected, "refinement": sensor.refinement_statistics(),
-                    "knot_capacity": sensor.adaptive_cache_capacity()}
+                    "rejected_windows": rejected, "refinement": asensor.refinement_statistics(),
+                    "knot_capacity": asensor.adaptive_cache_capacity(), "circuit_precision": acircuit}
     # max over ranks
     vals = torch.tensor([dev_ms, e2e_s, rays, rays2, st2["events_delivered"]], dtype=torch.float64, device="cuda")
     if world > 1:
@@ -346,8 +360,9 @@ def run_gb300(args):
                       "events_total": st["events_ms"]},
         "roofline": {"bound": "hbm", "kernel": "trace_cells_kernel", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "traffic": (TRACE_DRAM_BYTES_PER_PIXEL_CELL[args.workload] * n_pix * cells_per_launch
-                                 if args.workload in TRACE_DRAM_BYTES_PER_PIXEL_CELL else None),
+                     "traffic": (TRACE_DRAM_BYTES_PER_PIXEL_CELL[(args.workload, args.geometry)] * n_pix
+                                 * cells_per_launch
+                                 if (args.workload, args.geometry) in TRACE_DRAM_BYTES_PER_PIXEL_CELL else None),
                      "algorithmic_bytes": alg_bytes,
                      "peak_source": "measured" if peaks else "fallback",
                      "note": "traversal is L1-broadcast/ALU bound; bytes = radiance written per launch"},
@@ -446,7 +461,7 @@ def main():
     ap.add_argument("--serving-jobs", type=int, default=48)
     ap.add_argument("--serving-scale", type=float, default=0.01)
     ap.add_argument("--leaf", type=int, default=0)
-    ap.add_argument("--geometry", default="reference", choices=sorted(GEOMETRY),
+    ap.add_argument("--geometry", default=None, choices=sorted(GEOMETRY),
                     help="BVH format: FP32 or FP16 (half) child bounds; Moller-Trumbore or watertight triangles")
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--cw", type=int, default=0)
@@ -455,9 +470,14 @@ def main():
     ap.add_argument("--rays", type=int, default=0, help="sub-rays per lane: 1, 2 or 4 (0 = default)")
     ap.add_argument("--adaptive-ms", type=float, default=2.0,
                     help="also run the adaptive optical solver over this many simulated milliseconds")
-    ap.add_argument("--circuit", default="fp64", choices=["fp64", "fp32", "fp32-philox"],
+    ap.add_argument("--circuit", default=None, choices=["fp64", "fp32", "fp32-philox"],
                     help="pixel-circuit arithmetic: fp64 (reference) or fp32 (precision mode)")
     args = ap.parse_args()
+    w = WORKLOADS.get(args.workload, {})
+    if args.geometry is None:
+        args.geometry = w.get("geometry", "reference")   # each workload's configured BVH format
+    if args.circuit is None:
+        args.circuit = w.get("circuit", "fp64")
     if args.impl == "reference":
         if args.workload == "serving":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving layer"}))
