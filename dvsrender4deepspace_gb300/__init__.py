@@ -2,5 +2,5 @@
 event readout) behind a C-ABI; see include/dvs_gb300.h."""
 from ._capi import (EVENT_DTYPE, INTERVAL_DTYPE, STATE_DTYPE, CapacityError, DvsError, OpticalError,  # noqa: F401
                     library_path, load)
-from .raycast import (CamRayCaster, DeviceScene, DvsRayCaster, EventSensor, derive_parameters,  # noqa: F401
-                      interval_array, state_array)
+from .raycast import (CamRayCaster, DeviceScene, DvsRayCaster, EventSensor, SensorBatch,  # noqa: F401
+                      derive_parameters, interval_array, state_array)

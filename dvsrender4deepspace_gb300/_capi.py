@@ -74,6 +74,14 @@ class SceneInfo(C.Structure):
                 ("leaf_size", C.c_int32), ("precision", C.c_int32)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("steps", C.c_uint64), ("graph_launches", C.c_uint64), ("graph_captures", C.c_uint64),
+                ("persistent_launches", C.c_uint64), ("trace_items", C.c_uint64), ("step_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class SensorStats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("events_generated", C.c_uint64),
                 ("events_delivered", C.c_uint64), ("dropped", C.c_uint64), ("peak_queue", C.c_uint64),
@@ -95,7 +103,8 @@ EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_d
            "dvs_readout_create", "dvs_readout_destroy", "dvs_readout_submit", "dvs_readout_drain", "dvs_readout_read",
            "dvs_readout_counters", "dvs_config_load", "dvs_frames_load", "dvs_trajectory_create",
            "dvs_trajectory_destroy", "dvs_trajectory_range", "dvs_trajectory_evaluate", "dvs_cam_render_blur",
-           "dvs_scene_view_create", "dvs_sensor_device_bytes", "dvs_sensor_set_tuning", "dvs_sensor_autotune")
+           "dvs_scene_view_create", "dvs_sensor_device_bytes", "dvs_sensor_set_tuning", "dvs_sensor_autotune",
+           "dvs_batch_create", "dvs_batch_destroy", "dvs_batch_process", "dvs_batch_stats_get")
 
 
 class Tuning(C.Structure):
@@ -184,6 +193,10 @@ def _declare(lib):
     lib.dvs_trajectory_destroy.argtypes = [vp]
     lib.dvs_trajectory_range.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     lib.dvs_trajectory_evaluate.argtypes = [vp, C.c_float, vp, f_p]
+    lib.dvs_batch_create.argtypes = [vp, sz, C.POINTER(vp)]
+    lib.dvs_batch_destroy.argtypes = [vp]
+    lib.dvs_batch_process.argtypes = [vp, vp, vp, vp]
+    lib.dvs_batch_stats_get.argtypes = [vp, C.POINTER(BatchStats)]
     return lib
 
 

@@ -793,9 +793,9 @@ static void record_timer(dvs_sensor *s, int kind) {
   cudaEventRecord(s->timers[s->timers_used++], s->stream);
 }
 
-// Validates the batch, builds its circuit cells, uploads both and launches
-// the per-cell pose kernel (upload_intervals, event_sensor.cu:274-289).
-static int upload_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, size_t &n_cells_out) {
+// Validates the batch and builds its circuit cells in pinned staging, growing
+// the device buffers they go to (upload_intervals, event_sensor.cu:274-289).
+static int stage_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, size_t &n_cells_out) {
   if (!s || !s->initialized || !ivs || count == 0) return fail(DVS_ERR_INVALID, "sensor not initialized or no intervals");
   if (count > (size_t)std::numeric_limits<int>::max()) return fail(DVS_ERR_INVALID, "too many intervals");
   // upload_intervals (event_sensor.cu:274-289)
@@ -831,14 +831,24 @@ static int upload_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t c
   CUDA_TRY(grow_device(s->ivs, s->ivs_cap, count), "trajectory interval allocation");
   CUDA_TRY(grow_device(s->cells, s->cells_cap, n_cells), "cell allocation");
   CUDA_TRY(grow_device(s->poses, s->poses_cap, n_cells), "pose allocation");
-  CUDA_TRY(cudaMemcpyAsync(s->ivs, s->h_ivs, sizeof(dvs_optical_interval) * count, cudaMemcpyHostToDevice, s->stream),
-           "trajectory interval upload");
-  CUDA_TRY(cudaMemcpyAsync(s->cells, s->h_cells, sizeof(Cell) * n_cells, cudaMemcpyHostToDevice, s->stream),
-           "cell upload");
-  CUDA_TRY(launch_cell_poses(s->ivs, s->cells, (int)n_cells, s->poses, s->stream), "cell poses");
-  s->stats.launches += 1;
   n_cells_out = n_cells;
   return DVS_OK;
+}
+
+// Uploads a staged batch and launches the per-cell pose kernel on `stream`.
+static int upload_staged(dvs_sensor *s, size_t count, size_t n_cells, cudaStream_t stream) {
+  CUDA_TRY(cudaMemcpyAsync(s->ivs, s->h_ivs, sizeof(dvs_optical_interval) * count, cudaMemcpyHostToDevice, stream),
+           "trajectory interval upload");
+  CUDA_TRY(cudaMemcpyAsync(s->cells, s->h_cells, sizeof(Cell) * n_cells, cudaMemcpyHostToDevice, stream),
+           "cell upload");
+  CUDA_TRY(launch_cell_poses(s->ivs, s->cells, (int)n_cells, s->poses, stream), "cell poses");
+  s->stats.launches += 1;
+  return DVS_OK;
+}
+
+static int upload_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, size_t &n_cells_out) {
+  int r = stage_batch(s, ivs, count, n_cells_out);
+  return r ? r : upload_staged(s, count, n_cells_out, s->stream);
 }
 
 // Cells per optics launch and cells per warp packet for a batch.
@@ -854,11 +864,11 @@ static void chunk_shape(const dvs_sensor *s, size_t n_cells, size_t rows, size_t
   }
 }
 
-static int clear_batch_outputs(dvs_sensor *s) {
+static int clear_batch_outputs(dvs_sensor *s, cudaStream_t stream) {
   const int n = s->pixels();
-  CUDA_TRY(cudaMemsetAsync(s->ev_count, 0, sizeof(int32_t) * n, s->stream), "clear events");
-  CUDA_TRY(cudaMemsetAsync(s->event_total, 0, sizeof(int32_t), s->stream), "clear events");
-  CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream), "clear status");
+  CUDA_TRY(cudaMemsetAsync(s->ev_count, 0, sizeof(int32_t) * n, stream), "clear events");
+  CUDA_TRY(cudaMemsetAsync(s->event_total, 0, sizeof(int32_t), stream), "clear events");
+  CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), stream), "clear status");
   return DVS_OK;
 }
 
@@ -873,7 +883,7 @@ static int enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count)
   int cw_log2;
   chunk_shape(s, n_cells, (size_t)n, chunk, cw_log2);
   CUDA_TRY(ensure_radiance(s, chunk), "radiance chunk allocation");
-  if ((r = clear_batch_outputs(s))) return r;
+  if ((r = clear_batch_outputs(s, s->stream))) return r;
   const SceneView view = s->view();
   for (size_t c0 = 0; c0 < n_cells; c0 += chunk) {
     const int nc = (int)std::min(chunk, n_cells - c0);
@@ -1136,7 +1146,7 @@ int dvs_sensor_process_adaptive(dvs_sensor *s, const dvs_optical_interval *ivs, 
     }
   }
   record_timer(s, 1);
-  if ((r = clear_batch_outputs(s))) return r;
+  if ((r = clear_batch_outputs(s, s->stream))) return r;
   CUDA_TRY(launch_integrate_knots(n, s->cells, (int)n_cells, start, end, s->knots, s->knot_counts, cap,
                                   s->exact_cells, s->exact_radiance, queries ? s->exact_counts : nullptr, s->p,
                                   s->photo, s->max_events, s->st, s->ev_count, s->slab_t, s->slab_p, s->error_word,
@@ -1407,6 +1417,284 @@ int dvs_sensor_read_state(dvs_sensor *s, double *state5, int32_t *reset_pending)
       for (int f = 0; f < 5; ++f) state5[(size_t)pix * 5 + f] = buf[(size_t)f * n + k];
     if (reset_pending) reset_pending[pix] = rp[k];
   }
+  return DVS_OK;
+}
+
+}  // extern "C"
+
+// ---- batch: many sensors over one geometry, one persistent trace per step ----------
+struct dvs_batch {
+  std::vector<dvs_sensor *> members;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // per round: job tables (pinned staging and device copies) and the work counter
+  int rounds_cap = 0;
+  TraceJob *h_trace = nullptr, *d_trace = nullptr;
+  CircuitJob *h_circuit = nullptr, *d_circuit = nullptr;
+  unsigned long long *d_next = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_end = nullptr;
+  // the captured step and the shape it was captured for
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uintptr_t> key;
+  dvs_batch_stats stats{};
+};
+
+namespace {
+// Everything a captured step depends on besides the job tables' contents:
+// per member its activity, interval and cell counts, chunking and the device
+// and pinned buffers the captured copies and launches use.
+std::vector<uintptr_t> batch_key(const dvs_batch *b, const std::vector<size_t> &counts,
+                                 const std::vector<size_t> &n_cells, const std::vector<size_t> &chunks,
+                                 const std::vector<int> &cw, int rounds) {
+  std::vector<uintptr_t> k;
+  k.push_back((uintptr_t)rounds);
+  for (size_t m = 0; m < b->members.size(); ++m) {
+    const dvs_sensor *s = b->members[m];
+    k.push_back(counts[m]);
+    k.push_back(n_cells[m]);
+    k.push_back(chunks[m]);
+    k.push_back((uintptr_t)cw[m]);
+    for (const void *ptr : {(const void *)s->h_ivs, (const void *)s->h_cells, (const void *)s->ivs,
+                            (const void *)s->cells, (const void *)s->poses, (const void *)s->radiance,
+                            (const void *)s->events})
+      k.push_back((uintptr_t)ptr);
+  }
+  return k;
+}
+}  // namespace
+
+extern "C" {
+
+int dvs_batch_create(dvs_sensor *const *sensors, size_t n, dvs_batch **out) {
+  if (!out) return fail(DVS_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (!sensors || n == 0 || n > (size_t)kMaxBatchJobs)
+    return fail(DVS_ERR_INVALID, "a batch holds 1 to 256 sensors");
+  const void *geometry = nullptr;
+  for (size_t m = 0; m < n; ++m) {
+    const dvs_sensor *s = sensors[m];
+    if (!s) return fail(DVS_ERR_INVALID, "null sensor in batch");
+    for (size_t q = 0; q < m; ++q)
+      if (sensors[q] == s) return fail(DVS_ERR_INVALID, "a sensor appears twice in the batch");
+    if (m == 0) geometry = s->scene->geometry.get();
+    if (s->scene->geometry.get() != geometry || s->device != sensors[0]->device)
+      return fail(DVS_ERR_INVALID, "batch sensors must share one scene geometry and device");
+    if (s->photo.fp32_circuit != sensors[0]->photo.fp32_circuit || s->photo.philox != sensors[0]->photo.philox)
+      return fail(DVS_ERR_INVALID, "batch sensors must share one circuit precision");
+  }
+  CUDA_TRY(cudaSetDevice(sensors[0]->device), "select device");
+  dvs_batch *b = new dvs_batch;
+  b->members.assign(sensors, sensors + n);
+  b->device = sensors[0]->device;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev_start);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev_end);
+  if (e != cudaSuccess) {
+    dvs_batch_destroy(b);
+    return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in create batch : ") + cudaGetErrorString(e));
+  }
+  *out = b;
+  return DVS_OK;
+}
+
+int dvs_batch_destroy(dvs_batch *b) {
+  if (!b) return DVS_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->h_trace) cudaFreeHost(b->h_trace);
+  if (b->h_circuit) cudaFreeHost(b->h_circuit);
+  cudaFree(b->d_trace);
+  cudaFree(b->d_circuit);
+  cudaFree(b->d_next);
+  if (b->ev_start) cudaEventDestroy(b->ev_start);
+  if (b->ev_end) cudaEventDestroy(b->ev_end);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return DVS_OK;
+}
+
+int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals, const size_t *counts,
+                      size_t *n_ready) {
+  if (!b || !intervals || !counts) return fail(DVS_ERR_INVALID, "null argument");
+  const size_t n = b->members.size();
+  CUDA_TRY(cudaSetDevice(b->device), "select device");
+  std::vector<size_t> n_cells(n, 0), chunks(n, 0);
+  std::vector<int> cw(n, 0);
+  bool any = false;
+  int rounds = 0;
+  // stage every active member's intervals and cells; allocations happen here,
+  // before any capture
+  for (size_t m = 0; m < n; ++m) {
+    if (n_ready) n_ready[m] = 0;
+    dvs_sensor *s = b->members[m];
+    if (counts[m] == 0) continue;
+    if (!intervals[m]) return fail(DVS_ERR_INVALID, "null intervals for an active batch sensor");
+    CUDA_TRY(cudaStreamSynchronize(s->stream), "sensor stream");
+    int r = stage_batch(s, intervals[m], counts[m], n_cells[m]);
+    if (r) return r;
+    chunk_shape(s, n_cells[m], (size_t)s->pixels(), chunks[m], cw[m]);
+    CUDA_TRY(ensure_radiance(s, chunks[m]), "radiance chunk allocation");
+    rounds = std::max(rounds, (int)((n_cells[m] + chunks[m] - 1) / chunks[m]));
+    any = true;
+  }
+  if (!any) return DVS_OK;
+  if (rounds > b->rounds_cap) {
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    b->key.clear();
+    if (b->h_trace) cudaFreeHost(b->h_trace);
+    if (b->h_circuit) cudaFreeHost(b->h_circuit);
+    cudaFree(b->d_trace);
+    cudaFree(b->d_circuit);
+    cudaFree(b->d_next);
+    b->h_trace = nullptr; b->h_circuit = nullptr; b->d_trace = nullptr; b->d_circuit = nullptr; b->d_next = nullptr;
+    const size_t jobs = (size_t)rounds * kMaxBatchJobs;
+    CUDA_TRY(cudaMallocHost(&b->h_trace, sizeof(TraceJob) * jobs), "batch job staging");
+    CUDA_TRY(cudaMallocHost(&b->h_circuit, sizeof(CircuitJob) * jobs), "batch job staging");
+    CUDA_TRY(cudaMalloc(&b->d_trace, sizeof(TraceJob) * jobs), "batch job tables");
+    CUDA_TRY(cudaMalloc(&b->d_circuit, sizeof(CircuitJob) * jobs), "batch job tables");
+    CUDA_TRY(cudaMalloc(&b->d_next, sizeof(unsigned long long) * rounds), "batch work counters");
+    b->rounds_cap = rounds;
+  }
+  // the job tables of every round; rays per lane shared by the batch (2 when
+  // every active member's sub-ray count is even)
+  bool pairs = true;
+  for (size_t m = 0; m < n; ++m)
+    if (counts[m] && (b->members[m]->scene->samples * b->members[m]->scene->samples) % 2) pairs = false;
+  std::vector<int> n_trace(rounds, 0), n_circuit(rounds, 0), blocks(rounds, 0);
+  std::vector<long long> items(rounds, 0);
+  for (int r = 0; r < rounds; ++r) {
+    TraceJob *tj = b->h_trace + (size_t)r * kMaxBatchJobs;
+    CircuitJob *cj = b->h_circuit + (size_t)r * kMaxBatchJobs;
+    for (size_t m = 0; m < n; ++m) {
+      dvs_sensor *s = b->members[m];
+      if (!counts[m]) continue;
+      const size_t c0 = (size_t)r * chunks[m];
+      if (c0 >= n_cells[m]) continue;
+      const int nc = (int)std::min(chunks[m], n_cells[m] - c0);
+      TraceJob &t = tj[n_trace[r]++];
+      t.view = s->view();
+      t.poses = s->poses;
+      t.radiance = s->radiance;
+      t.counters = s->counters;
+      t.first_item = items[r];
+      t.n_pix = s->pixels();
+      t.c0 = (int)c0;
+      t.nc = nc;
+      t.cw_log2 = cw[m];
+      items[r] += trace_job_items(t.n_pix, nc, cw[m]);
+      CircuitJob &c = cj[n_circuit[r]++];
+      c.p = s->p;
+      c.photo = s->photo;
+      c.st = s->st;
+      c.cells = s->cells;
+      c.radiance = s->radiance;
+      c.ev_count = s->ev_count;
+      c.slab_t = s->slab_t;
+      c.slab_p = s->slab_p;
+      c.error = s->error_word;
+      c.counters = s->counters;
+      c.n = s->pixels();
+      c.c0 = (int)c0;
+      c.nc = nc;
+      c.max_events = s->max_events;
+      c.first_block = blocks[r];
+      c.pad = 0;
+      blocks[r] += (c.n + 127) / 128;
+    }
+  }
+  // capture the step once per shape; replays read the refreshed pinned tables
+  std::vector<uintptr_t> key = batch_key(b, std::vector<size_t>(counts, counts + n), n_cells, chunks, cw, rounds);
+  key.push_back(pairs ? 2 : 1);
+  for (int r = 0; r < rounds; ++r) {
+    key.push_back((uintptr_t)n_trace[r]);
+    key.push_back((uintptr_t)items[r]);
+    key.push_back((uintptr_t)blocks[r]);
+  }
+  const SceneView geo = b->members[0]->view();
+  const bool fp32 = b->members[0]->photo.fp32_circuit != 0, philox = b->members[0]->photo.philox != 0;
+  if (!b->exec || key != b->key) {
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    cudaStream_t st = b->stream;
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin batch capture");
+    int rc = DVS_OK;
+    // timing events as event-record nodes of the graph (a plain record inside a
+    // capture only marks a dependency point)
+    cudaError_t e = cudaEventRecordWithFlags(b->ev_start, st, cudaEventRecordExternal);
+    for (size_t m = 0; m < n && rc == DVS_OK && e == cudaSuccess; ++m) {
+      if (!counts[m]) continue;
+      rc = upload_staged(b->members[m], counts[m], n_cells[m], st);
+      if (rc == DVS_OK) rc = clear_batch_outputs(b->members[m], st);
+    }
+    for (int r = 0; r < rounds && rc == DVS_OK && e == cudaSuccess; ++r) {
+      const size_t off = (size_t)r * kMaxBatchJobs;
+      e = cudaMemcpyAsync(b->d_trace + off, b->h_trace + off, sizeof(TraceJob) * n_trace[r], cudaMemcpyHostToDevice,
+                          st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->d_circuit + off, b->h_circuit + off, sizeof(CircuitJob) * n_circuit[r],
+                            cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaMemsetAsync(b->d_next + r, 0, sizeof(unsigned long long), st);
+      if (e == cudaSuccess)
+        e = launch_trace_jobs(b->d_trace + off, n_trace[r], items[r], pairs ? 2 : 1, geo.geometry, b->d_next + r, st);
+      if (e == cudaSuccess) e = launch_circuit_jobs(b->d_circuit + off, n_circuit[r], blocks[r], fp32, philox, st);
+    }
+    for (size_t m = 0; m < n && rc == DVS_OK && e == cudaSuccess; ++m) {
+      if (!counts[m]) continue;
+      dvs_sensor *s = b->members[m];
+      e = launch_emit_events(s->pixels(), s->order, s->scene->camera.width, s->max_events, s->ev_count, s->slab_t,
+                             s->slab_p, s->events, s->event_total, st);
+      if (e == cudaSuccess)
+        e = launch_event_depth(s->view(), s->ivs, (int)counts[m], s->events, s->event_total, s->error_word,
+                               s->counters, st);
+    }
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(b->ev_end, st, cudaEventRecordExternal);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+    if (rc != DVS_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e == cudaSuccess) e = ec;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      b->exec = nullptr;
+      b->key.clear();
+      return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in capture batch step : ") + cudaGetErrorString(e));
+    }
+    b->key = key;
+    b->stats.graph_captures += 1;
+  }
+  CUDA_TRY(cudaGraphLaunch(b->exec, b->stream), "launch batch step");
+  CUDA_TRY(cudaStreamSynchronize(b->stream), "batch step");
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, b->ev_start, b->ev_end) == cudaSuccess)
+    b->stats.step_ms += ms;
+  else
+    cudaGetLastError();  // no timing for this step; leave no error behind for the next launch check
+  b->stats.steps += 1;
+  b->stats.graph_launches += 1;
+  b->stats.persistent_launches += (uint64_t)rounds;
+  for (int r = 0; r < rounds; ++r) b->stats.trace_items += (uint64_t)items[r];
+  // per member: status, events and the readout, as after a one-sensor step
+  int first_error = DVS_OK;
+  for (size_t m = 0; m < n; ++m) {
+    if (!counts[m]) continue;
+    dvs_sensor *s = b->members[m];
+    s->stats.launches += 4;
+    s->stats.optics_launches += 1;
+    s->stats.circuit_launches += 1;
+    s->last_time = intervals[m][counts[m] - 1].t1;
+    s->pending = false;
+    const int r = collect(s, s->last_time, n_ready ? &n_ready[m] : nullptr);
+    if (r && first_error == DVS_OK) first_error = r;
+  }
+  return first_error;
+}
+
+int dvs_batch_stats_get(const dvs_batch *b, dvs_batch_stats *out) {
+  if (!b || !out) return fail(DVS_ERR_INVALID, "null argument");
+  *out = b->stats;
   return DVS_OK;
 }
 

@@ -91,6 +91,46 @@ cudaError_t launch_cell_poses(const dvs_optical_interval *ivs, const Cell *cells
                               cudaStream_t s);
 // Radiance (and optionally depth) of every pixel at every cell in [c0, c0+nc).
 // Output index: cell * n_pix + rank.  Invalid samples store NaN radiance.
+// ---- multi-sensor batch (batch.cu) ----------------------------------------
+// One sensor's share of a batch step's trace: its cells [c0, c0 + nc) traced
+// into its radiance chunk.  first_item: the first work item (warp packet) of
+// this sensor in the batch's item space; items are job-major.
+constexpr int kMaxBatchJobs = 256;
+struct TraceJob {
+  SceneView view;
+  const CellPose *poses;
+  double *radiance;
+  unsigned long long *counters;
+  long long first_item;
+  int32_t n_pix, c0, nc, cw_log2;
+};
+// One sensor's share of a batch step's circuit launch; first_block: its first
+// 128-thread block (blocks never straddle two sensors).
+struct CircuitJob {
+  PixelParams p;
+  PhotoParams photo;
+  CircuitState st;
+  const Cell *cells;
+  const double *radiance;
+  int32_t *ev_count;
+  double *slab_t;
+  int8_t *slab_p;
+  int32_t *error;
+  unsigned long long *counters;
+  int32_t n, c0, nc, max_events, first_block, pad;
+};
+// Work items of one sensor's trace share (warp packets of cw_log2 cells).
+long long trace_job_items(int n_pix, int nc, int cw_log2);
+// Persistent trace of every job's items: a grid of resident blocks whose warps
+// pull items from *next_item (zeroed by the caller on the same stream).
+// rays: 1 or 2 sub-rays per lane for every job; geometry: the jobs' shared
+// SceneView::geometry.
+cudaError_t launch_trace_jobs(const TraceJob *jobs, int n_jobs, long long total_items, int rays, int geometry,
+                              unsigned long long *next_item, cudaStream_t s);
+// One circuit launch over every job's pixels (total_blocks blocks of 128).
+cudaError_t launch_circuit_jobs(const CircuitJob *jobs, int n_jobs, int total_blocks, bool fp32, bool philox,
+                                cudaStream_t s);
+
 cudaError_t launch_trace_cells(const SceneView &scene, int n_pix, const CellPose *poses, int c0, int nc,
                                int cw_log2, double *radiance, float *depth, unsigned long long *counters,
                                cudaStream_t s);

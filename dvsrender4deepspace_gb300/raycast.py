@@ -426,3 +426,46 @@ class CamRayCaster:
         q = quaternion_from_matrix(camera_world)
         return self.render_state(dict(position=camera_origin, rotation=q, light=light_dir,
                                       intensity=light_intensity))
+
+
+class SensorBatch:
+    """Many EventSensors over one scene geometry advanced together
+    (dvs_batch_*): each step traces every member in one persistent launch and
+    integrates every member's circuits in one launch, the step captured into a
+    CUDA graph and replayed while the members' shapes stay the same."""
+
+    def __init__(self, sensors):
+        self.sensors = list(sensors)
+        arr = (C.c_void_p * len(self.sensors))(*[s.handle for s in self.sensors])
+        h = C.c_void_p()
+        check(_capi.load().dvs_batch_create(arr, len(self.sensors), C.byref(h)))
+        self.handle = h
+
+    def process(self, intervals_per_sensor):
+        """intervals_per_sensor[m]: member m's next intervals (empty: idle).
+        Returns the ready events of every member."""
+        n = len(self.sensors)
+        if len(intervals_per_sensor) != n:
+            raise ValueError("one interval list per batch sensor")
+        arrays = [interval_array(ivs) if len(ivs) else None for ivs in intervals_per_sensor]
+        ptrs = (C.c_void_p * n)(*[a.ctypes.data if a is not None else None for a in arrays])
+        counts = (C.c_size_t * n)(*[len(a) if a is not None else 0 for a in arrays])
+        ready = (C.c_size_t * n)()
+        check(_capi.load().dvs_batch_process(self.handle, ptrs, counts, ready))
+        return [s._read(ready[m]) if counts[m] else np.zeros(0, EVENT_DTYPE) for m, s in enumerate(self.sensors)]
+
+    def stats(self):
+        out = _capi.BatchStats()
+        check(_capi.load().dvs_batch_stats_get(self.handle, C.byref(out)))
+        return out.as_dict()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _capi.load().dvs_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

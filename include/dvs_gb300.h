@@ -261,6 +261,34 @@ int dvs_sensor_adaptive_capacity(dvs_sensor *sensor, int32_t *knot_capacity);
 int dvs_sensor_drain(dvs_sensor *sensor, dvs_event *out, size_t capacity, size_t *n_out);
 int dvs_sensor_stats_get(const dvs_sensor *sensor, dvs_sensor_stats *out);
 int dvs_sensor_stats_reset(dvs_sensor *sensor);
+/* ---- batch: many sensors over one scene geometry, advanced together --------------
+ * No counterpart in the reference (its apps run one trajectory per process or GPU).
+ * Each dvs_batch_process step traces every active member's cells in ONE persistent
+ * launch -- resident warps pull work items (one warp packet of one member) from a
+ * device counter, so members of different sizes share the GPU without a tail each --
+ * and integrates every member's pixel circuits in one launch.  The step (uploads,
+ * both launches, per-member event compaction and depth) is captured once into a CUDA
+ * graph and replayed while the members' batch shapes stay the same; a member that
+ * receives no intervals idles (the step is captured anew for the new shape).  Members
+ * must share one scene geometry (dvs_scene_view_create views of one scene), device
+ * and circuit_precision, and must be initialized; their events are read with
+ * dvs_sensor_read as after dvs_sensor_process, and are the same as when each member
+ * is processed alone.  A member may not be used outside the batch during a step. */
+typedef struct dvs_batch dvs_batch;
+typedef struct {
+  uint64_t steps, graph_launches, graph_captures, persistent_launches;
+  uint64_t trace_items;       /* warp packets traced by the persistent launches */
+  double step_ms;             /* device time of the steps (events at both ends of the graph) */
+} dvs_batch_stats;
+/* 1..256 sensors. */
+int dvs_batch_create(dvs_sensor *const *sensors, size_t n, dvs_batch **out);
+int dvs_batch_destroy(dvs_batch *batch);
+/* intervals[m], counts[m]: member m's next contiguous intervals (count 0: idle this
+ * step).  n_ready (optional, n entries): events ready per member afterwards. */
+int dvs_batch_process(dvs_batch *batch, const dvs_optical_interval *const *intervals, const size_t *counts,
+                      size_t *n_ready);
+int dvs_batch_stats_get(const dvs_batch *batch, dvs_batch_stats *out);
+
 /* ---- standalone readout FIFO: EventReadout (include/dvs/event_sensor.hpp:24-37,
  *      src/event_readout.cpp:6-34).  Host only; used to read out event runs
  *      merged from several sensors (one per GPU) through one bus. ----------- */
