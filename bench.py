@@ -451,13 +451,177 @@ def run_serving(args):
     return 0
 
 
+def batching_members(n, seed, light, intensity):
+    """The batching config's trajectories: constant-altitude arcs with altitude
+    U(0.5, 5) km, speed U(10, 200) m/s, heading U(0, 360) deg, yaw rate
+    U(-5, 5) deg/s, starting points spread over the 10 km terrain, and lengths
+    U{20..400} frames (seeded)."""
+    from dvsrender4deepspace_gb300 import trajectory
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        out.append((trajectory.Orbit((rng.uniform(-3000, 3000), rng.uniform(-3000, 3000)), rng.uniform(500, 5000),
+                                     rng.uniform(10, 200), math.radians(rng.uniform(0, 360)),
+                                     math.radians(rng.uniform(-5, 5)), light, intensity),
+                    int(rng.integers(20, 401))))
+    return out
+
+
+def run_batching(args):
+    """Batching config: 64 independent trajectories over one 1024^2 terrain
+    (346x260, 16 sub-rays, 10 us horizons, FP32 pixel state, FP64 timestamps),
+    every step one multi-sensor batch step (one persistent trace launch, one
+    circuit launch, captured into a CUDA graph and replayed).  Trajectory k of
+    F_k frames stays active for ceil(F_k / 400 * K) of the K timed steps, so
+    members drop out unevenly and the step is re-captured for each new shape.
+    Beside it, the same members advanced one sensor at a time (the plain path)."""
+    import torch
+    from dvsrender4deepspace_gb300 import DeviceScene, EventSensor, SensorBatch, interval_array, terrain, trajectory
+    from dvsrender4deepspace_gb300.build import build
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank == 0:
+        build()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+        torch.distributed.barrier()
+    w = WORKLOADS["orbit"]
+    V, N, I = terrain.terrain_mesh(w["grid"], w["seed"])
+    light = trajectory.sun_direction(w["sun_elevation"], 35.0)
+    members = batching_members(args.batch_members, 20260005 + rank, light, w["intensity"])
+    t_setup = time.time()
+    base = DeviceScene(V, N, I, w["camera"], w["ss"], HAPKE, leaf_size=args.leaf, geometry=GEOMETRY[args.geometry])
+    info = base.info()
+    setup_s = time.time() - t_setup
+    dt, H = w["time_resolution"], args.batch_horizons
+    K, Wm = args.steps, args.warmup
+    active_steps = [int(math.ceil(frames / 400.0 * K)) for _, frames in members]
+
+    def make(kind):
+        sensors = []
+        for traj, _ in members:
+            s = EventSensor(base, PHYSIC, cells_per_warp=args.cw, circuit_precision=args.circuit)
+            s.initialize(traj.state(0.0), 0.0)
+            sensors.append(s)
+        return sensors
+
+    def plan(step, cursors, timed):
+        rows = []
+        for m, (traj, _) in enumerate(members):
+            if timed and step >= active_steps[m]:
+                rows.append([])
+                continue
+            ivs = trajectory.horizons(traj, cursors[m], dt, H)
+            cursors[m] = ivs[-1][3]
+            rows.append(interval_array(ivs))
+        return rows
+
+    def rays_of(sensors):
+        return sum(s.stats()["primary_rays"] + s.stats()["shadow_rays"] for s in sensors)
+
+    def events_of(sensors):
+        return sum(s.stats()["events_delivered"] for s in sensors)
+
+    results = {}
+    for mode in ("batch", "loop"):
+        sensors = make(mode)
+        batch = SensorBatch(sensors) if mode == "batch" else None
+        cursors = [0.0] * len(members)
+        for k in range(Wm):
+            rows = plan(k, cursors, False)
+            if batch:
+                batch.process(rows)
+            else:
+                for s, r in zip(sensors, rows):
+                    s.process_many(r)
+        rays0, ev0 = rays_of(sensors), events_of(sensors)
+        st0 = batch.stats() if batch else None
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with ClockSampler(local) as clocks:
+            for k in range(K):
+                rows = plan(k, cursors, True)
+                if batch:
+                    batch.process(rows)
+                else:
+                    for s, r in zip(sensors, rows):
+                        if len(r):
+                            s.process_many(r)
+            torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        if world > 1:
+            torch.distributed.barrier()
+        rays, events = rays_of(sensors) - rays0, events_of(sensors) - ev0
+        res = {"wall_s": wall, "rays": rays, "events": events, "mrays_per_s_wall": rays / wall / 1e6,
+               "events_per_s": events / wall, "clocks": clocks.summary()}
+        if batch:
+            st = batch.stats()
+            dev_ms = st["step_ms"] - st0["step_ms"]
+            res.update({"device_ms": dev_ms, "mrays_per_s_device": rays / (dev_ms / 1e3) / 1e6,
+                        "graph_launches": st["graph_launches"] - st0["graph_launches"],
+                        "graph_captures": st["graph_captures"] - st0["graph_captures"],
+                        "persistent_launches": st["persistent_launches"] - st0["persistent_launches"],
+                        "trace_items": st["trace_items"] - st0["trace_items"]})
+            batch.close()
+        results[mode] = res
+        for s in sensors:
+            s.close()
+    b, l = results["batch"], results["loop"]
+    vals = torch.tensor([b["device_ms"], b["wall_s"], b["rays"], l["wall_s"], l["rays"], b["events"]],
+                        dtype=torch.float64, device="cuda")
+    if world > 1:
+        mx = vals.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        sm = vals.clone()
+        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
+        dev_ms, b_wall, l_wall = mx[0].item(), mx[1].item(), mx[3].item()
+        b_rays, l_rays, b_events = sm[2].item(), sm[4].item(), sm[5].item()
+    else:
+        dev_ms, b_wall, l_wall = b["device_ms"], b["wall_s"], l["wall_s"]
+        b_rays, l_rays, b_events = b["rays"], l["rays"], b["events"]
+    if rank != 0:
+        return 0
+    from dvsrender4deepspace_gb300 import INTERVAL_DTYPE
+    n_launch = sum(min(K, a) for a in active_steps)
+    cells_per_horizon = int(round(float(np.float32(dt)) / float(np.float32(PHYSIC["circuit_step"]))))
+    cb = None
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline("orbit", V, N, I, members[0][0], w, budget_s=15.0)
+    line = {"metric": METRIC, "value": b_rays / (dev_ms / 1e3) / 1e6, "unit": "Mrays/s", "n_gpus": world,
+            "steps": K, "warmup": Wm, "ms_per_step": dev_ms / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "batching", "members": len(members), "frames": [f for _, f in members],
+                       "active_steps": active_steps, "width": w["camera"]["width"], "height": w["camera"]["height"],
+                       "supersample": w["ss"], "terrain_grid": w["grid"], "triangles": int(info["triangles"]),
+                       "horizons_per_step": H, "time_resolution": dt, "circuit_precision": args.circuit,
+                       "geometry": args.geometry, "parallelism": "dp%d (independent batches)" % world,
+                       "l2": "inputs larger than L2 (radiance chunks %.1f GB)"
+                             % (len(members) * H * 10 * w["camera"]["width"] * w["camera"]["height"] * 8 / 1e9)},
+            # per active member-step: its intervals and their circuit cells (24 B each) in, its
+            # events (24 B each on the device side) and status words out
+            "e2e": {"value": b_rays / b_wall / 1e6, "unit": "Mrays/s",
+                    "h2d_bytes_per_step": int(n_launch * H * (INTERVAL_DTYPE.itemsize + cells_per_horizon * 24) / K),
+                    "d2h_bytes_per_step": int((b_events * 24 + n_launch * 8) / K)},
+            "events_per_s": b_events / b_wall,
+            "batch": results["batch"], "per_sensor_loop": results["loop"],
+            "batch_vs_loop_wall": (b_rays / b_wall) / max(1e-9, l_rays / l_wall),
+            "gpu_launches": int(2 * K + 3 * n_launch),
+            "clocks": results["batch"]["clocks"], "setup_s": setup_s, "cpu_baseline": cb}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="precision", choices=sorted(WORKLOADS) + ["serving"])
+    ap.add_argument("--workload", default="precision", choices=sorted(WORKLOADS) + ["serving", "batching"])
+    ap.add_argument("--batch-members", type=int, default=64)
+    ap.add_argument("--batch-horizons", type=int, default=16, help="horizons per member per batching step")
     ap.add_argument("--serving-jobs", type=int, default=48)
     ap.add_argument("--serving-scale", type=float, default=0.01)
     ap.add_argument("--leaf", type=int, default=0)
@@ -473,18 +637,21 @@ def main():
     ap.add_argument("--circuit", default=None, choices=["fp64", "fp32", "fp32-philox"],
                     help="pixel-circuit arithmetic: fp64 (reference) or fp32 (precision mode)")
     args = ap.parse_args()
-    w = WORKLOADS.get(args.workload, {})
+    w = WORKLOADS.get("orbit" if args.workload == "batching" else args.workload, {})
     if args.geometry is None:
         args.geometry = w.get("geometry", "reference")   # each workload's configured BVH format
     if args.circuit is None:
         args.circuit = w.get("circuit", "fp64")
     if args.impl == "reference":
-        if args.workload == "serving":
-            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving layer"}))
+        if args.workload in ("serving", "batching"):
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving or multi-sensor "
+                                                                  "batching layer"}))
             return 0
         return run_reference(args)
     if args.workload == "serving":
         return run_serving(args)
+    if args.workload == "batching":
+        return run_batching(args)
     return run_gb300(args)
 
 

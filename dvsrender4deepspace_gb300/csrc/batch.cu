@@ -3,9 +3,9 @@
 // A batch advances many sensors over one shared scene geometry in lockstep
 // (the batching workload: many uneven trajectories over one terrain).  Each
 // step traces every sensor's cells in ONE persistent launch: a grid of
-// resident blocks whose warps pull work items -- one warp packet (32/CW
-// pixels x CW cells of one sensor) each -- from a device counter, so sensors
-// of different sizes share the GPU without a tail per sensor; then one
+// resident blocks that pull runs of work items -- one warp packet (32/CW
+// pixels x CW cells of one sensor) per warp -- from a device counter, so
+// sensors of different sizes share the GPU without a tail per sensor; then one
 // circuit launch integrates every sensor's pixels.  The host captures the
 // whole step (uploads, these launches, the per-sensor event compaction and
 // status copies) into a CUDA graph and replays it while the sensors' batch
@@ -32,37 +32,36 @@ __device__ __forceinline__ int job_of(const T *first, int n_jobs, T x) {
   return lo;
 }
 
+// The job table travels as the launch's parameter block (__grid_constant__: no
+// copy), so a warp reads its job's view -- the same job for all its lanes --
+// through the constant cache, as the one-sensor kernel reads its view.
 template <int kRays, int kGeo>
 __global__ void __launch_bounds__(128, kRays == 2 ? DVS_TRACE_PAIR_MIN_BLOCKS : DVS_TRACE_MIN_BLOCKS)
-    trace_jobs_kernel(const TraceJob *__restrict__ jobs, int n_jobs, long long total_items,
-                      unsigned long long *next_item) {
+    trace_jobs_kernel(const __grid_constant__ TraceJobs P) {
   __shared__ int s_code[kWarpsPerBlock][kStackSlots];
   __shared__ float s_t[kWarpsPerBlock][kStackSlots];
   __shared__ double s_cos4[kWarpsPerBlock][kCos4Table];
-  __shared__ SceneView s_view[kWarpsPerBlock];
   __shared__ long long s_first[kMaxBatchJobs];
-  for (int j = threadIdx.x; j < n_jobs; j += blockDim.x) s_first[j] = jobs[j].first_item;
-  __syncthreads();
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  int cur = -1;
+  __shared__ long long s_base;
+  for (int j = threadIdx.x; j < P.n_jobs; j += blockDim.x) s_first[j] = P.jobs[j].first_item;
+  const int wib = threadIdx.x >> 5;
+  // A block takes kWarpsPerBlock consecutive items at a time (one per warp),
+  // as a block of the one-sensor kernel holds consecutive packets: the warps
+  // of an SM then trace neighbouring pixels, whose nodes stay in its L1.
   while (true) {
-    unsigned long long item = 0;
-    if (lane == 0) item = atomicAdd(next_item, 1ull);
-    item = __shfl_sync(kFull, item, 0);
-    if ((long long)item >= total_items) break;  // warp-uniform
-    const int j = job_of<long long>(s_first, n_jobs, (long long)item);
-    if (j != cur) {  // this warp's copy of the job's camera view
-      __syncwarp();
-      const int *src = reinterpret_cast<const int *>(&jobs[j].view);
-      int *dst = reinterpret_cast<int *>(&s_view[wib]);
-      for (int w = lane; w < (int)(sizeof(SceneView) / sizeof(int)); w += 32) dst[w] = src[w];
-      __syncwarp();
-      cur = j;
+    __syncthreads();  // every warp is done with the previous s_base
+    if (threadIdx.x == 0) s_base = (long long)atomicAdd(P.next_item, (unsigned long long)kWarpsPerBlock);
+    __syncthreads();
+    const long long base = s_base;
+    if (base >= P.total_items) break;  // block-uniform
+    const long long item = base + wib;
+    if (item < P.total_items) {        // warp-uniform
+      const int j = job_of<long long>(s_first, P.n_jobs, item);
+      const TraceJob &J = P.jobs[j];
+      trace_cells_item<kRadiance, kRays, kGeo>(J.view, J.n_pix, nullptr, J.poses, J.c0, J.nc, J.cw_log2,
+                                               J.radiance, nullptr, J.counters, item - s_first[j], s_code[wib],
+                                               s_t[wib], s_cos4[wib]);
     }
-    const TraceJob &J = jobs[j];
-    trace_cells_item<kRadiance, kRays, kGeo>(s_view[wib], J.n_pix, nullptr, J.poses, J.c0, J.nc, J.cw_log2,
-                                             J.radiance, nullptr, J.counters, (long long)item - s_first[j],
-                                             s_code[wib], s_t[wib], s_cos4[wib]);
   }
 }
 
@@ -79,29 +78,26 @@ __global__ void __launch_bounds__(128) circuit_jobs_kernel(const CircuitJob *__r
 }
 
 template <int kRays, int kGeo>
-cudaError_t trace_jobs_geo(const TraceJob *jobs, int n_jobs, long long total_items, unsigned long long *next_item,
-                           cudaStream_t s) {
+cudaError_t trace_jobs_geo(const TraceJobs &jobs, cudaStream_t s) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_jobs_kernel<kRays, kGeo>, 128, 0);
   // resident blocks only (a persistent grid), fewer when there are fewer items than warps
   const long long resident = (long long)sms * (per_sm > 0 ? per_sm : 1);
-  const long long needed = (total_items + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  const long long needed = (jobs.total_items + kWarpsPerBlock - 1) / kWarpsPerBlock;
   const long long grid = needed < resident ? needed : resident;
-  trace_jobs_kernel<kRays, kGeo><<<(int)grid, 128, 0, s>>>(jobs, n_jobs, total_items, next_item);
+  trace_jobs_kernel<kRays, kGeo><<<(int)grid, 128, 0, s>>>(jobs);
   return cudaGetLastError();
 }
 
 template <int kRays>
-cudaError_t trace_jobs_rays(const TraceJob *jobs, int n_jobs, long long total_items, int geometry,
-                            unsigned long long *next_item, cudaStream_t s) {
+cudaError_t trace_jobs_rays(const TraceJobs &jobs, int geometry, cudaStream_t s) {
   switch (geometry) {
-    case kGeoHalfBounds: return trace_jobs_geo<kRays, kGeoHalfBounds>(jobs, n_jobs, total_items, next_item, s);
-    case kGeoWatertight: return trace_jobs_geo<kRays, kGeoWatertight>(jobs, n_jobs, total_items, next_item, s);
-    case kGeoHalfBounds | kGeoWatertight:
-      return trace_jobs_geo<kRays, kGeoHalfBounds | kGeoWatertight>(jobs, n_jobs, total_items, next_item, s);
-    default: return trace_jobs_geo<kRays, kGeoReference>(jobs, n_jobs, total_items, next_item, s);
+    case kGeoHalfBounds: return trace_jobs_geo<kRays, kGeoHalfBounds>(jobs, s);
+    case kGeoWatertight: return trace_jobs_geo<kRays, kGeoWatertight>(jobs, s);
+    case kGeoHalfBounds | kGeoWatertight: return trace_jobs_geo<kRays, kGeoHalfBounds | kGeoWatertight>(jobs, s);
+    default: return trace_jobs_geo<kRays, kGeoReference>(jobs, s);
   }
 }
 
@@ -112,12 +108,10 @@ long long trace_job_items(int n_pix, int nc, int cw_log2) {
   return (long long)((n_pix + ppw - 1) / ppw) * ((nc + cw - 1) / cw);
 }
 
-cudaError_t launch_trace_jobs(const TraceJob *jobs, int n_jobs, long long total_items, int rays, int geometry,
-                              unsigned long long *next_item, cudaStream_t s) {
-  if (n_jobs <= 0 || total_items <= 0) return cudaSuccess;
-  if (n_jobs > kMaxBatchJobs) return cudaErrorInvalidValue;
-  return rays == 2 ? trace_jobs_rays<2>(jobs, n_jobs, total_items, geometry, next_item, s)
-                   : trace_jobs_rays<1>(jobs, n_jobs, total_items, geometry, next_item, s);
+cudaError_t launch_trace_jobs(const TraceJobs &jobs, int rays, int geometry, cudaStream_t s) {
+  if (jobs.n_jobs <= 0 || jobs.total_items <= 0) return cudaSuccess;
+  if (jobs.n_jobs > kMaxBatchJobs) return cudaErrorInvalidValue;
+  return rays == 2 ? trace_jobs_rays<2>(jobs, geometry, s) : trace_jobs_rays<1>(jobs, geometry, s);
 }
 
 cudaError_t launch_circuit_jobs(const CircuitJob *jobs, int n_jobs, int total_blocks, bool fp32, bool philox,

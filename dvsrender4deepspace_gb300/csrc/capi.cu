@@ -156,7 +156,7 @@ struct dvs_scene {
   double *blur_radiance = nullptr;
 
   SceneView view() const {
-    SceneView v;
+    SceneView v{};  // zeroed padding: batch steps compare job tables byte for byte
     v.nodes = nodes;
     v.qnodes = qnodes;
     v.geometry = geometry_kind;
@@ -1427,9 +1427,10 @@ struct dvs_batch {
   std::vector<dvs_sensor *> members;
   int device = 0;
   cudaStream_t stream = nullptr;
-  // per round: job tables (pinned staging and device copies) and the work counter
+  // per round: the trace job table (the launch's parameter block), the circuit
+  // job table (pinned staging and device copy) and the work counter
   int rounds_cap = 0;
-  TraceJob *h_trace = nullptr, *d_trace = nullptr;
+  std::vector<TraceJobs> trace_tables;
   CircuitJob *h_circuit = nullptr, *d_circuit = nullptr;
   unsigned long long *d_next = nullptr;
   cudaEvent_t ev_start = nullptr, ev_end = nullptr;
@@ -1469,7 +1470,7 @@ int dvs_batch_create(dvs_sensor *const *sensors, size_t n, dvs_batch **out) {
   if (!out) return fail(DVS_ERR_INVALID, "null output handle");
   *out = nullptr;
   if (!sensors || n == 0 || n > (size_t)kMaxBatchJobs)
-    return fail(DVS_ERR_INVALID, "a batch holds 1 to 256 sensors");
+    return fail(DVS_ERR_INVALID, "a batch holds 1 to 128 sensors");
   const void *geometry = nullptr;
   for (size_t m = 0; m < n; ++m) {
     const dvs_sensor *s = sensors[m];
@@ -1502,9 +1503,7 @@ int dvs_batch_destroy(dvs_batch *b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->h_trace) cudaFreeHost(b->h_trace);
   if (b->h_circuit) cudaFreeHost(b->h_circuit);
-  cudaFree(b->d_trace);
   cudaFree(b->d_circuit);
   cudaFree(b->d_next);
   if (b->ev_start) cudaEventDestroy(b->ev_start);
@@ -1542,16 +1541,13 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
   if (rounds > b->rounds_cap) {
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     b->key.clear();
-    if (b->h_trace) cudaFreeHost(b->h_trace);
     if (b->h_circuit) cudaFreeHost(b->h_circuit);
-    cudaFree(b->d_trace);
     cudaFree(b->d_circuit);
     cudaFree(b->d_next);
-    b->h_trace = nullptr; b->h_circuit = nullptr; b->d_trace = nullptr; b->d_circuit = nullptr; b->d_next = nullptr;
+    b->h_circuit = nullptr; b->d_circuit = nullptr; b->d_next = nullptr;
     const size_t jobs = (size_t)rounds * kMaxBatchJobs;
-    CUDA_TRY(cudaMallocHost(&b->h_trace, sizeof(TraceJob) * jobs), "batch job staging");
+    b->trace_tables.assign((size_t)rounds, TraceJobs{});
     CUDA_TRY(cudaMallocHost(&b->h_circuit, sizeof(CircuitJob) * jobs), "batch job staging");
-    CUDA_TRY(cudaMalloc(&b->d_trace, sizeof(TraceJob) * jobs), "batch job tables");
     CUDA_TRY(cudaMalloc(&b->d_circuit, sizeof(CircuitJob) * jobs), "batch job tables");
     CUDA_TRY(cudaMalloc(&b->d_next, sizeof(unsigned long long) * rounds), "batch work counters");
     b->rounds_cap = rounds;
@@ -1564,7 +1560,8 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
   std::vector<int> n_trace(rounds, 0), n_circuit(rounds, 0), blocks(rounds, 0);
   std::vector<long long> items(rounds, 0);
   for (int r = 0; r < rounds; ++r) {
-    TraceJob *tj = b->h_trace + (size_t)r * kMaxBatchJobs;
+    TraceJob *tj = b->trace_tables[r].jobs;
+    std::memset(tj, 0, sizeof(TraceJob) * kMaxBatchJobs);
     CircuitJob *cj = b->h_circuit + (size_t)r * kMaxBatchJobs;
     for (size_t m = 0; m < n; ++m) {
       dvs_sensor *s = b->members[m];
@@ -1607,9 +1604,17 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
   std::vector<uintptr_t> key = batch_key(b, std::vector<size_t>(counts, counts + n), n_cells, chunks, cw, rounds);
   key.push_back(pairs ? 2 : 1);
   for (int r = 0; r < rounds; ++r) {
+    TraceJobs &t = b->trace_tables[r];
+    t.total_items = items[r];
+    t.next_item = b->d_next + r;
+    t.n_jobs = n_trace[r];
+    t.pad = 0;
     key.push_back((uintptr_t)n_trace[r]);
     key.push_back((uintptr_t)items[r]);
     key.push_back((uintptr_t)blocks[r]);
+    // the trace table is captured by value: any change in it means a new capture
+    const uintptr_t *words = reinterpret_cast<const uintptr_t *>(t.jobs);
+    key.insert(key.end(), words, words + sizeof(TraceJob) * n_trace[r] / sizeof(uintptr_t));
   }
   const SceneView geo = b->members[0]->view();
   const bool fp32 = b->members[0]->photo.fp32_circuit != 0, philox = b->members[0]->photo.philox != 0;
@@ -1628,14 +1633,10 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
     }
     for (int r = 0; r < rounds && rc == DVS_OK && e == cudaSuccess; ++r) {
       const size_t off = (size_t)r * kMaxBatchJobs;
-      e = cudaMemcpyAsync(b->d_trace + off, b->h_trace + off, sizeof(TraceJob) * n_trace[r], cudaMemcpyHostToDevice,
-                          st);
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(b->d_circuit + off, b->h_circuit + off, sizeof(CircuitJob) * n_circuit[r],
-                            cudaMemcpyHostToDevice, st);
+      e = cudaMemcpyAsync(b->d_circuit + off, b->h_circuit + off, sizeof(CircuitJob) * n_circuit[r],
+                          cudaMemcpyHostToDevice, st);
       if (e == cudaSuccess) e = cudaMemsetAsync(b->d_next + r, 0, sizeof(unsigned long long), st);
-      if (e == cudaSuccess)
-        e = launch_trace_jobs(b->d_trace + off, n_trace[r], items[r], pairs ? 2 : 1, geo.geometry, b->d_next + r, st);
+      if (e == cudaSuccess) e = launch_trace_jobs(b->trace_tables[r], pairs ? 2 : 1, geo.geometry, st);
       if (e == cudaSuccess) e = launch_circuit_jobs(b->d_circuit + off, n_circuit[r], blocks[r], fp32, philox, st);
     }
     for (size_t m = 0; m < n && rc == DVS_OK && e == cudaSuccess; ++m) {

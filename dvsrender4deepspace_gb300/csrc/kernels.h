@@ -95,7 +95,7 @@ cudaError_t launch_cell_poses(const dvs_optical_interval *ivs, const Cell *cells
 // One sensor's share of a batch step's trace: its cells [c0, c0 + nc) traced
 // into its radiance chunk.  first_item: the first work item (warp packet) of
 // this sensor in the batch's item space; items are job-major.
-constexpr int kMaxBatchJobs = 256;
+constexpr int kMaxBatchJobs = 128;
 struct TraceJob {
   SceneView view;
   const CellPose *poses;
@@ -103,6 +103,14 @@ struct TraceJob {
   unsigned long long *counters;
   long long first_item;
   int32_t n_pix, c0, nc, cw_log2;
+};
+// A trace launch's whole job table, passed as the kernel's parameter block
+// (22.5 KB at 128 jobs, within the 32 KB parameter limit).
+struct TraceJobs {
+  TraceJob jobs[kMaxBatchJobs];
+  long long total_items;
+  unsigned long long *next_item;  // work counter, zeroed before the launch
+  int32_t n_jobs, pad;
 };
 // One sensor's share of a batch step's circuit launch; first_block: its first
 // 128-thread block (blocks never straddle two sensors).
@@ -122,11 +130,10 @@ struct CircuitJob {
 // Work items of one sensor's trace share (warp packets of cw_log2 cells).
 long long trace_job_items(int n_pix, int nc, int cw_log2);
 // Persistent trace of every job's items: a grid of resident blocks whose warps
-// pull items from *next_item (zeroed by the caller on the same stream).
+// pull items from jobs.next_item (zeroed by the caller on the same stream).
 // rays: 1 or 2 sub-rays per lane for every job; geometry: the jobs' shared
 // SceneView::geometry.
-cudaError_t launch_trace_jobs(const TraceJob *jobs, int n_jobs, long long total_items, int rays, int geometry,
-                              unsigned long long *next_item, cudaStream_t s);
+cudaError_t launch_trace_jobs(const TraceJobs &jobs, int rays, int geometry, cudaStream_t s);
 // One circuit launch over every job's pixels (total_blocks blocks of 128).
 cudaError_t launch_circuit_jobs(const CircuitJob *jobs, int n_jobs, int total_blocks, bool fp32, bool philox,
                                 cudaStream_t s);

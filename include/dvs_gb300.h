@@ -264,8 +264,9 @@ int dvs_sensor_stats_reset(dvs_sensor *sensor);
 /* ---- batch: many sensors over one scene geometry, advanced together --------------
  * No counterpart in the reference (its apps run one trajectory per process or GPU).
  * Each dvs_batch_process step traces every active member's cells in ONE persistent
- * launch -- resident warps pull work items (one warp packet of one member) from a
- * device counter, so members of different sizes share the GPU without a tail each --
+ * launch -- resident blocks pull runs of work items (one warp packet of one member
+ * per warp) from a device counter, so members of different sizes share the GPU
+ * without a tail each --
  * and integrates every member's pixel circuits in one launch.  The step (uploads,
  * both launches, per-member event compaction and depth) is captured once into a CUDA
  * graph and replayed while the members' batch shapes stay the same; a member that
@@ -280,7 +281,7 @@ typedef struct {
   uint64_t trace_items;       /* warp packets traced by the persistent launches */
   double step_ms;             /* device time of the steps (events at both ends of the graph) */
 } dvs_batch_stats;
-/* 1..256 sensors. */
+/* 1..128 sensors. */
 int dvs_batch_create(dvs_sensor *const *sensors, size_t n, dvs_batch **out);
 int dvs_batch_destroy(dvs_batch *batch);
 /* intervals[m], counts[m]: member m's next contiguous intervals (count 0: idle this
