@@ -720,6 +720,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
   const int ss = S.samples;
   const int px_i = pixel % S.width, py_i = pixel / S.width;
   const HapkeConst hc = hapke_const(S.hapke);
+  const float3 lnorm = normalize(light);  // as in sample_pixel_group
   for (int sy = 0; sy < ss; ++sy)
     for (int sx = 0; sx < ss; ++sx) {
       const float px = subray_x(S, px_i, sx);
@@ -762,7 +763,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
           if (lit && !occ) {
             const double cos4 = cos4_table ? cos4_table[sy * ss + sx] : cos4_of(px, py);
             // hapke_directional_reflectance (hapke.hpp:153-157)
-            const float3 n = normalize(normal), l = normalize(light), v = normalize(-ray);
+            const float3 n = normalize(normal), l = lnorm, v = normalize(-ray);
             const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo, r0, S.hapke, hc);
             out.radiance += fmaxf(0, n_h * pose.intensity) * cos4;
           }
@@ -1059,6 +1060,9 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
   const int ss = S.samples, n_sub = ss * ss;
   const int px_i = pixel % S.width, py_i = pixel / S.width;
   const HapkeConst hc = hapke_const(S.hapke);
+  // hapke_directional_reflectance normalizes the light for every shaded ray
+  // (hapke.hpp:153-157); it is the same vector for all of this lane's rays
+  const float3 lnorm = normalize(light);
   for (int j = 0; j < n_sub; j += R) {
     float px[R], py[R];
     float3 ray[R], org[R];
@@ -1125,7 +1129,7 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
           if (lit[r]) ++out.shadow;
           if (lit[r] && !occ[r]) {
             const double cos4 = cos4_table ? cos4_table[j + r] : cos4_of(px[r], py[r]);
-            const float3 n = normalize(normal[r]), l = normalize(light), v = normalize(-ray[r]);
+            const float3 n = normalize(normal[r]), l = lnorm, v = normalize(-ray[r]);
             const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo[r], r0[r], S.hapke, hc);
             out.radiance += fmaxf(0, n_h * pose.intensity) * cos4;
           }
@@ -1158,6 +1162,7 @@ __device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const
   const int ss = S.samples, n_sub = ss * ss;
   const int px_i = pixel % S.width, py_i = pixel / S.width;
   const HapkeConst hc = hapke_const(S.hapke);
+  const float3 lnorm = normalize(light);  // as in sample_pixel_group
   bool valid = true;
   for (int g = 0; g < n_sub; g += 32 * R) {
     float px[R], py[R];
@@ -1215,7 +1220,7 @@ __device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const
       for (int r = 0; r < R; ++r)
         if (lit[r] && !occ[r]) {
           const double cos4 = cos4_of(px[r], py[r]);
-          const float3 n = normalize(normal[r]), l = normalize(light), v = normalize(-ray[r]);
+          const float3 n = normalize(normal[r]), l = lnorm, v = normalize(-ray[r]);
           const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo[r], r0[r], S.hapke, hc);
           term[r] = fmaxf(0, n_h * pose.intensity) * cos4;
         }
