@@ -170,6 +170,75 @@ def cpu_baseline(name, V, N, I, traj, w, budget_s=15.0, threads=0):
                       "binary BVH (leaf 64) built in %.1f s" % (batch * cells, batch, cells, w["ss"], total_t, build_s)}
 
 
+def precision_errors(V, N, I, traj, w, scene, geometry, circuit, budget_pixels=2048, threads=0):
+    """The precision config's accuracy statement, measured: the GPU path's
+    radiance and depth on a seeded sample of the config's pixels (one pose,
+    all sub-rays) against the FP64 oracle, and its events on a crop of the
+    config's camera through a light pulse against the FP64 oracle sensor
+    (deterministic physics: no shot noise, no threshold mismatch, no FIFO
+    delay -- the oracle cannot reproduce device random streams)."""
+    from dvsrender4deepspace_gb300 import CamRayCaster, EventSensor
+    from oracle import oracle as O
+    nthreads = threads or os.cpu_count()
+    cam = w["camera"]
+    t_build = time.time()
+    o64 = O.OracleScene(V, N, I, cam, w["ss"], HAPKE, max_leaf=64, fp64=True,
+                        watertight=bool(GEOMETRY[geometry] & 2))
+    build_s = time.time() - t_build
+    out = {"oracle": "FP64 (geometry, rays, Hapke in double; binary BVH leaf 64, built in %.1f s)" % build_s,
+           "geometry": geometry, "circuit_precision": circuit}
+    # radiance and depth: one pose, seeded pixel sample
+    pose = traj.state(0.0)
+    img, dep = CamRayCaster(scene).render_state(pose)
+    rng = np.random.default_rng(11)
+    pix = rng.choice(cam["width"] * cam["height"], size=budget_pixels, replace=False).astype(np.int32)
+    orad, odep, _, _ = o64.render_pixels(pose, pix, nthreads)
+    g_rad, g_dep = img.reshape(-1)[pix].astype(np.float64), dep.reshape(-1)[pix].astype(np.float64)
+    lit = orad > 0
+    rel = np.abs(g_rad[lit] - orad[lit]) / orad[lit]
+    hit = odep > 0
+    drel = np.abs(g_dep[hit] - odep[hit]) / odep[hit]
+    out["radiance"] = {"pixels": int(lit.sum()), "max_rel": float(rel.max()), "p99_rel": float(np.quantile(rel, .99)),
+                       "frac_above_1e-5": float(np.mean(rel > 1e-5))}
+    out["depth"] = {"pixels": int(hit.sum()), "max_rel": float(drel.max()), "p99_rel": float(np.quantile(drel, .99)),
+                    "frac_above_1e-5": float(np.mean(drel > 1e-5)), "misses_agree": bool(np.all((g_dep[~hit] < 0)))}
+    # events: a 16x12 crop at the image centre, 0.5 ms light pulse (500 cells of 1 us)
+    x0, y0 = cam["width"] // 2 - 8, cam["height"] // 2 - 6
+    crop = dict(cam, width=16, height=12, cx=cam["cx"] - x0, cy=cam["cy"] - y0)
+    phys = dict(PHYSIC, photon_shot_noise=0, threshold_std=0, readout_bandwidth=0, readout_latency=0,
+                max_events_per_step=64)
+    sensor = EventSensor(scene.view(crop, w["ss"]), phys, circuit_precision=circuit)
+    ors = O.OracleSensor(o64.with_camera(crop), phys)
+    sensor.initialize(pose, 0.0)
+    ors.initialize(pose, 0.0, nthreads)
+    a, b = dict(pose, intensity_rate=1.6e8), dict(traj.state(5e-4), intensity_rate=-1.6e8)
+    ivs = [(a, b, 0.0, 5e-4)]
+    t0 = time.time()
+    gev = np.concatenate([sensor.process_many(ivs), sensor.drain()])
+    oev = np.concatenate([ors.process(ivs, nthreads), ors.drain()])
+    cpu_s = time.time() - t0
+
+    def per_pixel(ev):
+        d = {}
+        for e in ev:
+            d.setdefault((int(e["x"]), int(e["y"])), []).append((float(e["timestamp"]), int(e["polarity"])))
+        return d
+    pg, po = per_pixel(gev), per_pixel(oev)
+    same, worst = 0, 0.0
+    for key in set(pg) | set(po):
+        x, y = pg.get(key, []), po.get(key, [])
+        if [p for _, p in x] == [p for _, p in y]:
+            same += 1
+            if x:
+                worst = max(worst, max(abs(u - v) for (u, _), (v, _) in zip(x, y)))
+    n_px = len(set(pg) | set(po))
+    out["events"] = {"crop": "16x12 at (%d, %d)" % (x0, y0), "interval": "0.5 ms pulse, 500 cells",
+                     "gpu_events": int(len(gev)), "oracle_events": int(len(oev)), "pixels_with_events": n_px,
+                     "pixels_same_polarity_sequence": same, "max_timestamp_error_s": worst,
+                     "oracle_seconds": cpu_s}
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -318,7 +387,7 @@ def run_gb300(args):
     optics_ms = st["optics_ms"] / max(1, st["optics_launches"])
     # dominant kernel: trace_cells (optics).  Algorithmic bytes per launch: the
     # per-pixel-cell radiance it must write (8 B) -- the HBM-minimal traffic of
-    # a latency/ALU-bound traversal; see the design doc for the accounting.
+    # a latency/ALU-bound traversal (the scene is read from L1/L2).
     cells_per_launch = st["circuit_cells"] / max(1, st["circuit_launches"]) / max(1, n_pix)
     alg_bytes = n_pix * cells_per_launch * 8.0
     peaks = {}
@@ -333,6 +402,9 @@ def run_gb300(args):
     cb = None
     if not args.no_cpu_baseline:
         cb = cpu_baseline(args.workload, V, N, I, traj, w, budget_s=15.0)
+    errors = None
+    if args.workload == "precision" and not args.no_precision_report and rank == 0:
+        errors = precision_errors(V, N, I, traj, w, scene, args.geometry, args.circuit)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -372,6 +444,7 @@ def run_gb300(args):
         "clocks": clocks.summary(), "setup_s": setup_s, "bvh_build_s": info["build_seconds"], "tuning": tuning,
         "adaptive": adaptive,
         "cpu_baseline": cb,
+        "precision_errors": errors,
     }
     if line["roofline_circuit"]["achieved"]:
         line["roofline_circuit"]["frac"] = line["roofline_circuit"]["achieved"] / peak
@@ -630,6 +703,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--cw", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision-report", action="store_true",
+                    help="skip the precision workload's error report against the FP64 oracle")
     ap.add_argument("--autotune", action="store_true", help="time the packet shapes on the first warm-up batch")
     ap.add_argument("--rays", type=int, default=0, help="sub-rays per lane: 1, 2 or 4 (0 = default)")
     ap.add_argument("--adaptive-ms", type=float, default=2.0,

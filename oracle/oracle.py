@@ -312,6 +312,19 @@ class OracleScene:
     def pixels(self):
         return self.s.width * self.s.height
 
+    def with_camera(self, camera, samples=None):
+        """The same tree and mesh seen by another camera (no rebuild)."""
+        v = OracleScene.__new__(OracleScene)
+        v.__dict__.update(self.__dict__)
+        v.camera = dict(camera)
+        v.samples = int(samples if samples is not None else self.samples)
+        t = oscene.from_buffer_copy(self.s)
+        t.width, t.height = int(camera["width"]), int(camera["height"])
+        t.samples = v.samples
+        t.fx, t.fy, t.cx, t.cy = (float(camera[k]) for k in ("fx", "fy", "cx", "cy"))
+        v.s = t
+        return v
+
     def render(self, pose, nthreads=0):
         n = self.pixels
         rad = np.zeros(n, np.float64)
