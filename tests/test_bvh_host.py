@@ -1,0 +1,36 @@
+"""Host-side wide-BVH checks (CPU): the builder's leaves cover every triangle
+once inside their boxes, and the FP16 child bounds of the precision geometry
+decode -- origin + offset with the device's directed rounding, re-done here
+through the floating-point environment -- to boxes that enclose the FP32 ones,
+including beyond the FP16 range (saturated lower bounds, infinite upper ones).
+Drives tests/bvh_selftest.cpp linked against libdvs_gb300.so."""
+import os
+import subprocess
+
+import pytest
+
+from dvsrender4deepspace_gb300 import build as B
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def selftest(tmp_path_factory):
+    B.build()
+    exe = str(tmp_path_factory.mktemp("bvh") / "bvh_selftest")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-frounding-math", "-I", os.path.join(B.PKG, "csrc"),
+                    "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "bvh_selftest.cpp"), "-o", exe,
+                    "-L", B.PKG, "-ldvs_gb300", "-Wl,-rpath," + B.PKG], check=True)
+    return exe
+
+
+@pytest.mark.parametrize("seed,n,scale,slack", [(1, 64, 1000.0, 2e-3),       # a 1 km tile
+                                                (2, 160, 40960.0, 2e-3),     # the 4096^2 terrain's extent
+                                                (3, 40, 300000.0, None)])    # offsets beyond 65504
+def test_quantised_bounds_enclose_the_fp32_tree(selftest, seed, n, scale, slack):
+    out = subprocess.run([selftest, str(seed), str(n), str(scale)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    fields = out.stdout.split()
+    assert fields[0] == "nodes" and int(fields[1]) > 0 and int(fields[5]) > 0
+    if slack is not None:
+        assert float(fields[7]) < slack, out.stdout   # FP16 offsets widen a box by well under 0.2 % of its node
