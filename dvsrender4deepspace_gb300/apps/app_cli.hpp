@@ -16,6 +16,15 @@ class Options {
   std::string config_path = "./config/davis346.yaml";
   std::string event_format = "bin";
   std::string event_solver = "auto";
+  // GB300 additions (no reference counterpart): BVH format and pixel-circuit arithmetic
+  std::string bvh = "fp32";        // fp32 | half | watertight | half+watertight
+  std::string circuit = "fp64";    // fp64 | fp32 | fp32-philox
+
+  int bvh_flags() const {  // dvs_bvh_params.precision
+    return (bvh == "half" || bvh == "half+watertight" ? 1 : 0) |
+           (bvh == "watertight" || bvh == "half+watertight" ? 2 : 0);
+  }
+  int circuit_precision() const { return circuit == "fp32" ? 1 : circuit == "fp32-philox" ? 2 : 0; }
 
   static void print_usage(const char *prog) {
     std::cout << "Usage: " << prog << "[options]\n"
@@ -27,7 +36,9 @@ class Options {
               << "  --output <path>            output images file (default: ./)\n"
               << "  --config <path>            path to YAML config file (default: ./config/davis346.yaml)\n"
               << "  --event_format <bin|hdf5>  event stream output format (default: bin)\n"
-              << "  --solver <auto|native|adaptive-optics>  auto selects adaptive optics for physical HDF5 output"
+              << "  --solver <auto|native|adaptive-optics>  auto selects adaptive optics for physical HDF5 output\n"
+              << "  --bvh <fp32|half|watertight|half+watertight>  BVH child bounds and triangle test (default: fp32)\n"
+              << "  --circuit <fp64|fp32|fp32-philox>  pixel-circuit arithmetic and noise stream (default: fp64)"
               << std::endl;
   }
 
@@ -62,6 +73,14 @@ class Options {
         event_solver = value(arg.c_str());
         if (event_solver != "auto" && event_solver != "native" && event_solver != "adaptive-optics")
           throw std::runtime_error("solver must be auto, native, or adaptive-optics");
+      } else if (arg == "--bvh") {
+        bvh = value(arg.c_str());
+        if (bvh != "fp32" && bvh != "half" && bvh != "watertight" && bvh != "half+watertight")
+          throw std::runtime_error("bvh must be fp32, half, watertight, or half+watertight");
+      } else if (arg == "--circuit") {
+        circuit = value(arg.c_str());
+        if (circuit != "fp64" && circuit != "fp32" && circuit != "fp32-philox")
+          throw std::runtime_error("circuit must be fp64, fp32, or fp32-philox");
       } else if (arg == "--help" || arg == "-h") {
         print_usage(argv[0]);
         std::exit(0);

@@ -37,7 +37,8 @@ int main(int argc, char **argv) {
     dvs_app::CameraTrajectory traj(frames, config.scene);
     auto scene = std::make_shared<dvs_gb300::DeviceScene>(mesh.vertices, mesh.normals, mesh.indices,
                                                           config.c_camera(), config.scene.supersample_factor,
-                                                          config.c_hapke(), mesh.albedos.empty() ? nullptr : &mesh.albedos);
+                                                          config.c_hapke(), mesh.albedos.empty() ? nullptr : &mesh.albedos,
+                                                          0, opts.bvh_flags());
     dvs_gb300::CamRayCaster raycaster(scene);
     const std::filesystem::path image_dir(opts.output_dir + "/blur_images");
     std::filesystem::create_directories(image_dir);

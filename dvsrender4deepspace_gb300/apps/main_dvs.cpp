@@ -53,6 +53,8 @@ int main(int argc, char **argv) {
     if (adaptive && opts.event_format != "hdf5")
       throw std::runtime_error(
           "adaptive optics exports HDF5 x/y/t/p; per-event auxiliary binary depth requires --solver native");
+    if (adaptive && opts.circuit == "fp32-philox")
+      throw std::runtime_error("the adaptive solver keeps the XORWOW noise stream: use --circuit fp32 or --solver native");
     dvs_app::MeshBundle mesh;
     std::vector<dvs_app::FrameData> frames;
     dvs_app::load_app_inputs(opts, config, mesh, frames);
@@ -60,9 +62,11 @@ int main(int argc, char **argv) {
     dvs_app::CameraTrajectory traj(frames, config.scene);
     auto scene = std::make_shared<dvs_gb300::DeviceScene>(mesh.vertices, mesh.normals, mesh.indices,
                                                           config.c_camera(), config.scene.supersample_factor,
-                                                          config.c_hapke(), mesh.albedos.empty() ? nullptr : &mesh.albedos);
+                                                          config.c_hapke(), mesh.albedos.empty() ? nullptr : &mesh.albedos,
+                                                          0, opts.bvh_flags());
     dvs_sensor_options options;
     dvs_sensor_options_default(&options);
+    options.circuit_precision = opts.circuit_precision();
     dvs_gb300::DvsRayCaster raycaster(scene, config.c_physic(), &options);
     std::filesystem::create_directories(opts.output_dir);
     std::unique_ptr<dvs_app::EventStreamWriter> events_out = make_event_writer(opts);

@@ -380,6 +380,10 @@ def test_cli_errors(built, tmp_path):
         (("--dem", "a.tif", "--traj", "t.txt", "--config", str(cfg)), "needs GDAL"),
         (("--scene_dir", "x", "--config", str(cfg), "--solver", "adaptive-optics"), "adaptive optics exports HDF5"),
         (("--scene_dir", "x", "--config", str(cfg), "--output"), "missing value for --output"),
+        (("--scene_dir", "x", "--config", str(cfg), "--bvh", "fp16"), "bvh must be fp32, half"),
+        (("--scene_dir", "x", "--config", str(cfg), "--circuit", "fp16"), "circuit must be fp64, fp32"),
+        (("--scene_dir", "x", "--config", str(cfg), "--event_format", "hdf5", "--circuit", "fp32-philox"),
+         "adaptive solver keeps the XORWOW"),
     ]
     for args, msg in cases:
         r = run_app("dvs", *args)

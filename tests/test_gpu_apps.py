@@ -50,14 +50,14 @@ def run_app(name, bundle, out, *extra):
     return r.stdout
 
 
-def api_events(bundle):
+def api_events(bundle, geometry=0, circuit="fp64"):
     """The same run through the library API with the app's batches."""
     cfg = inputs.load_config(bundle / "config.yaml")
     frames = inputs.load_frames(bundle / "scene")
     V, N, I = inputs.load_mesh(bundle / "scene")
     traj = inputs.Trajectory(frames, cfg["scene"])
-    scene = DeviceScene(V, N, I, cfg["camera"], cfg["scene"]["supersample_factor"], cfg["hapke"])
-    sensor = EventSensor(scene, cfg["physic"])
+    scene = DeviceScene(V, N, I, cfg["camera"], cfg["scene"]["supersample_factor"], cfg["hapke"], geometry=geometry)
+    sensor = EventSensor(scene, cfg["physic"], circuit_precision=circuit)
     (state0, t0), batches, end_time = inputs.app_intervals(traj, frames, cfg["scene"], cfg["physic"])
     sensor.initialize(state0, t0)
     evs = [sensor.process_many(b) for b in batches]
@@ -92,6 +92,16 @@ def test_dvs_app_events_match_the_library(bundle, tmp_path):
     ms = h5["t"] // 1000
     for m in range(len(idx)):
         assert idx[m] == np.searchsorted(ms, m, side="left")
+
+
+def test_dvs_app_precision_flags_match_the_library(bundle, tmp_path):
+    """bin/dvs --bvh / --circuit (GB300 additions) run the library's formats."""
+    run_app("dvs", bundle, tmp_path, "--event_format", "bin", "--bvh", "half+watertight", "--circuit", "fp32-philox")
+    got = np.fromfile(tmp_path / "events.bin", EVENT_BIN)
+    want, _ = api_events(bundle, geometry=3, circuit="fp32-philox")
+    assert len(want) > 50 and len(got) == len(want)
+    assert np.array_equal(got["t"], want["timestamp"].astype(np.float32))
+    assert np.array_equal(got["x"], want["x"]) and np.array_equal(got["p"], want["polarity"])
 
 
 def test_dvs_app_adaptive_hdf5(bundle, tmp_path):
