@@ -570,21 +570,21 @@ def run_batching(args):
     K, Wm = args.steps, args.warmup
     active_steps = [int(math.ceil(frames / 400.0 * K)) for _, frames in members]
 
-    def make(kind):
+    def make(view):
         sensors = []
         for traj, _ in members:
-            s = EventSensor(base, PHYSIC, cells_per_warp=args.cw, circuit_precision=args.circuit)
+            s = EventSensor(view, PHYSIC, cells_per_warp=args.cw, circuit_precision=args.circuit)
             s.initialize(traj.state(0.0), 0.0)
             sensors.append(s)
         return sensors
 
-    def plan(step, cursors, timed):
+    def plan(step, cursors, timed, horizons):
         rows = []
         for m, (traj, _) in enumerate(members):
             if timed and step >= active_steps[m]:
                 rows.append([])
                 continue
-            ivs = trajectory.horizons(traj, cursors[m], dt, H)
+            ivs = trajectory.horizons(traj, cursors[m], dt, horizons)
             cursors[m] = ivs[-1][3]
             rows.append(interval_array(ivs))
         return rows
@@ -595,52 +595,65 @@ def run_batching(args):
     def events_of(sensors):
         return sum(s.stats()["events_delivered"] for s in sensors)
 
-    results = {}
-    for mode in ("batch", "loop"):
-        sensors = make(mode)
-        batch = SensorBatch(sensors) if mode == "batch" else None
-        cursors = [0.0] * len(members)
-        for k in range(Wm):
-            rows = plan(k, cursors, False)
-            if batch:
-                batch.process(rows)
-            else:
-                for s, r in zip(sensors, rows):
-                    s.process_many(r)
-        rays0, ev0 = rays_of(sensors), events_of(sensors)
-        st0 = batch.stats() if batch else None
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        with ClockSampler(local) as clocks:
-            for k in range(K):
-                rows = plan(k, cursors, True)
+    def measure(view, horizons):
+        results = {}
+        for mode in ("batch", "loop"):
+            sensors = make(view)
+            batch = SensorBatch(sensors) if mode == "batch" else None
+            cursors = [0.0] * len(members)
+            for k in range(Wm):
+                rows = plan(k, cursors, False, horizons)
                 if batch:
                     batch.process(rows)
                 else:
                     for s, r in zip(sensors, rows):
-                        if len(r):
-                            s.process_many(r)
-            torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        if world > 1:
-            torch.distributed.barrier()
-        rays, events = rays_of(sensors) - rays0, events_of(sensors) - ev0
-        res = {"wall_s": wall, "rays": rays, "events": events, "mrays_per_s_wall": rays / wall / 1e6,
-               "events_per_s": events / wall, "clocks": clocks.summary()}
-        if batch:
-            st = batch.stats()
-            dev_ms = st["step_ms"] - st0["step_ms"]
-            res.update({"device_ms": dev_ms, "mrays_per_s_device": rays / (dev_ms / 1e3) / 1e6,
-                        "graph_launches": st["graph_launches"] - st0["graph_launches"],
-                        "graph_captures": st["graph_captures"] - st0["graph_captures"],
-                        "persistent_launches": st["persistent_launches"] - st0["persistent_launches"],
-                        "trace_items": st["trace_items"] - st0["trace_items"]})
-            batch.close()
-        results[mode] = res
-        for s in sensors:
-            s.close()
+                        s.process_many(r)
+            rays0, ev0 = rays_of(sensors), events_of(sensors)
+            st0 = batch.stats() if batch else None
+            # the timed steps' intervals, generated beforehand (host Python, not the path)
+            timed_rows = [plan(k, cursors, True, horizons) for k in range(K)]
+            if world > 1:
+                torch.distributed.barrier()
+            with ClockSampler(local) as clocks:  # started before and stopped after the timed region
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for k in range(K):
+                    rows = timed_rows[k]
+                    if batch:
+                        batch.process(rows)
+                    else:
+                        for s, r in zip(sensors, rows):
+                            if len(r):
+                                s.process_many(r)
+                torch.cuda.synchronize()
+                wall = time.perf_counter() - t0
+            if world > 1:
+                torch.distributed.barrier()
+            rays, events = rays_of(sensors) - rays0, events_of(sensors) - ev0
+            res = {"wall_s": wall, "rays": rays, "events": events, "mrays_per_s_wall": rays / wall / 1e6,
+                   "events_per_s": events / wall, "clocks": clocks.summary()}
+            if batch:
+                st = batch.stats()
+                dev_ms = st["step_ms"] - st0["step_ms"]
+                res.update({"device_ms": dev_ms, "mrays_per_s_device": rays / (dev_ms / 1e3) / 1e6,
+                            "graph_launches": st["graph_launches"] - st0["graph_launches"],
+                            "graph_captures": st["graph_captures"] - st0["graph_captures"],
+                            "persistent_launches": st["persistent_launches"] - st0["persistent_launches"],
+                            "host_ms": st["host_ms"] - st0["host_ms"],
+                            "capture_ms": st["capture_ms"] - st0["capture_ms"],
+                            "trace_items": st["trace_items"] - st0["trace_items"]})
+                batch.close()
+            results[mode] = res
+            for s in sensors:
+                s.close()
+        return results
+
+    results = measure(base, H)
+    # the same trajectories as small members (64x48, one sub-ray, 64 horizons a step):
+    # per-member work is then a few launches' worth, where one persistent launch and
+    # one graph per step replace per-member launches and synchronisations
+    small_cam = dict(width=64, height=48, fx=60.0, fy=60.0, cx=32.0, cy=24.0)
+    small = measure(base.view(small_cam, 1), 64) if args.batch_small else None
     b, l = results["batch"], results["loop"]
     vals = torch.tensor([b["device_ms"], b["wall_s"], b["rays"], l["wall_s"], l["rays"], b["events"]],
                         dtype=torch.float64, device="cuda")
@@ -679,6 +692,11 @@ def run_batching(args):
                     "d2h_bytes_per_step": int((b_events * 24 + n_launch * 8) / K)},
             "events_per_s": b_events / b_wall,
             "batch": results["batch"], "per_sensor_loop": results["loop"],
+            "small_members": None if small is None else {
+                "camera": "64x48", "supersample": 1, "horizons_per_step": 64, "batch": small["batch"],
+                "per_sensor_loop": small["loop"],
+                "batch_vs_loop_wall": small["batch"]["mrays_per_s_wall"] / max(1e-9, small["loop"]["mrays_per_s_wall"]),
+                "events_batch_vs_loop": small["batch"]["events_per_s"] / max(1e-9, small["loop"]["events_per_s"])},
             "batch_vs_loop_wall": (b_rays / b_wall) / max(1e-9, l_rays / l_wall),
             "gpu_launches": int(2 * K + 3 * n_launch),
             "clocks": results["batch"]["clocks"], "setup_s": setup_s, "cpu_baseline": cb}
@@ -695,6 +713,8 @@ def main():
     ap.add_argument("--workload", default="precision", choices=sorted(WORKLOADS) + ["serving", "batching"])
     ap.add_argument("--batch-members", type=int, default=64)
     ap.add_argument("--batch-horizons", type=int, default=16, help="horizons per member per batching step")
+    ap.add_argument("--no-batch-small", dest="batch_small", action="store_false",
+                    help="skip the batching workload's small-member leg (64x48, one sub-ray)")
     ap.add_argument("--serving-jobs", type=int, default=48)
     ap.add_argument("--serving-scale", type=float, default=0.01)
     ap.add_argument("--leaf", type=int, default=0)

@@ -76,7 +76,8 @@ class SceneInfo(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("steps", C.c_uint64), ("graph_launches", C.c_uint64), ("graph_captures", C.c_uint64),
-                ("persistent_launches", C.c_uint64), ("trace_items", C.c_uint64), ("step_ms", C.c_double)]
+                ("persistent_launches", C.c_uint64), ("trace_items", C.c_uint64), ("step_ms", C.c_double),
+                ("host_ms", C.c_double), ("capture_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -1516,6 +1516,14 @@ int dvs_batch_destroy(dvs_batch *b) {
 int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals, const size_t *counts,
                       size_t *n_ready) {
   if (!b || !intervals || !counts) return fail(DVS_ERR_INVALID, "null argument");
+  const auto t_enter = std::chrono::steady_clock::now();
+  struct HostTimer {  // host time of this call, on every return path
+    dvs_batch *b;
+    std::chrono::steady_clock::time_point t0;
+    ~HostTimer() {
+      b->stats.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+  } host_timer{b, t_enter};
   const size_t n = b->members.size();
   CUDA_TRY(cudaSetDevice(b->device), "select device");
   std::vector<size_t> n_cells(n, 0), chunks(n, 0);
@@ -1619,6 +1627,7 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
   const SceneView geo = b->members[0]->view();
   const bool fp32 = b->members[0]->photo.fp32_circuit != 0, philox = b->members[0]->photo.philox != 0;
   if (!b->exec || key != b->key) {
+    const auto t_capture = std::chrono::steady_clock::now();
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     cudaStream_t st = b->stream;
     CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin batch capture");
@@ -1665,6 +1674,8 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
     }
     b->key = key;
     b->stats.graph_captures += 1;
+    b->stats.capture_ms +=
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_capture).count();
   }
   CUDA_TRY(cudaGraphLaunch(b->exec, b->stream), "launch batch step");
   CUDA_TRY(cudaStreamSynchronize(b->stream), "batch step");

@@ -280,6 +280,8 @@ typedef struct {
   uint64_t steps, graph_launches, graph_captures, persistent_launches;
   uint64_t trace_items;       /* warp packets traced by the persistent launches */
   double step_ms;             /* device time of the steps (events at both ends of the graph) */
+  double host_ms;             /* wall time inside dvs_batch_process */
+  double capture_ms;          /* of which capturing and instantiating graphs */
 } dvs_batch_stats;
 /* 1..128 sensors. */
 int dvs_batch_create(dvs_sensor *const *sensors, size_t n, dvs_batch **out);
