@@ -144,14 +144,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(name, V, N, I, traj, w, budget_s=15.0, threads=0):
+def cpu_baseline(name, V, N, I, traj, w, budget_s=15.0, threads=0, osc=None, build_s=None):
     """Oracle port (reference arithmetic, FP32 rays) on a bounded sample of the
     workload's pixel-cells; returns Mrays/s and the sample description."""
     from oracle import oracle as O
     cam = w["camera"]
-    t_build = time.time()
-    osc = O.OracleScene(V, N, I, cam, w["ss"], HAPKE, max_leaf=64)
-    build_s = time.time() - t_build
+    if osc is None:
+        t_build = time.time()
+        osc = O.OracleScene(V, N, I, cam, w["ss"], HAPKE, max_leaf=64)
+        build_s = time.time() - t_build
     rng = np.random.default_rng(7)
     n_pix = cam["width"] * cam["height"]
     nthreads = threads or os.cpu_count()
@@ -239,14 +240,32 @@ def precision_errors(V, N, I, traj, w, scene, geometry, circuit, budget_pixels=2
     return out
 
 
+def bench_config(args, w, n_triangles, world):
+    """The workload's `config` block, the same for both arms."""
+    return {"workload": args.workload, "pixels": w["camera"]["width"] * w["camera"]["height"],
+            "width": w["camera"]["width"], "height": w["camera"]["height"], "supersample": w["ss"],
+            "terrain_grid": w["grid"], "triangles": int(n_triangles), "horizons_per_step": w["batch"],
+            "time_resolution": w["time_resolution"], "circuit_step": PHYSIC["circuit_step"],
+            "shot_noise": "philox" if args.circuit == "fp32-philox" else "curand_xorwow",
+            "sun_elevation_deg": w["sun_elevation"], "intensity": w["intensity"],
+            "l2": "inputs larger than L2 (the scene: GBs of BVH and triangle records)",
+            "parallelism": "dp%d (independent jobs)" % world, "geometry": args.geometry,
+            "circuit_precision": args.circuit}
+
+
 def run_reference(args):
+    from oracle import oracle as O
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     w, V, N, I, traj = make_workload(args.workload)
+    t_build = time.time()
+    osc = O.OracleScene(V, N, I, w["camera"], w["ss"], HAPKE, max_leaf=64)   # built once for all steps
+    build_s = time.time() - t_build
     res = []
     for step in range(args.warmup + args.steps):
-        cb = cpu_baseline(args.workload, V, N, I, traj, w, budget_s=max(2.0, 60.0 / (args.warmup + args.steps)))
+        cb = cpu_baseline(args.workload, V, N, I, traj, w, budget_s=max(2.0, 60.0 / (args.warmup + args.steps)),
+                          osc=osc, build_s=build_s)
         if step >= args.warmup:
             res.append(cb)
     value = statistics.median(r["value"] for r in res)
@@ -255,8 +274,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, **{k: v for k, v in w.items() if k != "camera"},
-                       "camera": w["camera"]},
+            "config": bench_config(args, w, len(I), world),
             "cpu_baseline": cbl, "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                                          "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -409,16 +427,9 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": args.workload, "pixels": n_pix, "width": w["camera"]["width"],
-                   "height": w["camera"]["height"], "supersample": w["ss"], "terrain_grid": w["grid"],
-                   "triangles": int(info["triangles"]), "horizons_per_step": B, "time_resolution": dt,
-                   "circuit_step": PHYSIC["circuit_step"],
-                   "shot_noise": "philox" if args.circuit == "fp32-philox" else "curand_xorwow", "sun_elevation_deg":
-                   w["sun_elevation"], "intensity": w["intensity"], "l2": "inputs larger than L2 (scene %.1f GB)"
-                   % (info["device_bytes"] / 1e9), "parallelism": "dp%d (independent jobs)" % world,
-                   "bvh": "8-wide Morton radix, leaf %d, depth %d" % (info["leaf_size"], info["depth"]),
-                   "geometry": args.geometry,
-                   "circuit_precision": args.circuit},
+        "config": bench_config(args, w, len(I), world),
+        "scene": {"device_gb": info["device_bytes"] / 1e9,
+                  "bvh": "8-wide Morton radix, leaf %d, depth %d" % (info["leaf_size"], info["depth"])},
         "rays_per_step": rays / args.steps,
         "rays": {"primary_per_step": st["primary_rays"] / args.steps, "shadow_per_step": st["shadow_rays"] / args.steps,
                  "primary_mrays_s": st["primary_rays"] / (dev_ms / 1e3) / 1e6 if world == 1 else None,
