@@ -248,7 +248,8 @@ def bench_config(args, w, n_triangles, world):
             "time_resolution": w["time_resolution"], "circuit_step": PHYSIC["circuit_step"],
             "shot_noise": "philox" if args.circuit == "fp32-philox" else "curand_xorwow",
             "sun_elevation_deg": w["sun_elevation"], "intensity": w["intensity"],
-            "l2": "inputs larger than L2 (the scene: GBs of BVH and triangle records)",
+            "l2": "inputs larger than L2 (129 MB): the triangle and shading records alone are %.2f GB"
+                  % (n_triangles * 112 / 1e9),
             "parallelism": "dp%d (independent jobs)" % world, "geometry": args.geometry,
             "circuit_precision": args.circuit}
 
