@@ -194,6 +194,11 @@ struct dvs_sensor {
   double last_time = 0;
   bool pending = false;  // an enqueued batch awaits collect
   double pending_end = 0;
+  // The last upload's copies out of the pinned staging (h_ivs, h_cells) run
+  // when the stream reaches them; the next batch waits for them before it
+  // overwrites the staging (back-to-back enqueues stay correct).
+  cudaEvent_t staged = nullptr;
+  bool staged_pending = false;
   cudaStream_t stream = nullptr;
   // device state
   CircuitState st{};
@@ -684,6 +689,7 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
   if ((e = cudaMallocHost(&s->h_status, sizeof(int32_t) * 4)) != cudaSuccess) return bail(e, "status staging");
   if ((e = cudaMallocHost(&s->h_state, sizeof(dvs_optical_state))) != cudaSuccess) return bail(e, "pose staging");
   if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(e, "stream");
+  if ((e = cudaEventCreateWithFlags(&s->staged, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
   if ((e = cudaMemsetAsync(s->counters, 0, sizeof(unsigned long long) * kCntSlots, s->stream)) != cudaSuccess)
     return bail(e, "clear counters");
   *out = s;
@@ -694,6 +700,7 @@ int dvs_sensor_destroy(dvs_sensor *s) {
   if (!s) return DVS_OK;
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->staged) cudaEventDestroy(s->staged);
   cudaFree(s->st.receptor_log);
   cudaFree(s->st.reference_log);
   cudaFree(s->st.refractory_until);
@@ -809,6 +816,10 @@ static int stage_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t co
   }
   if (cells_f > 1000000) return fail(DVS_ERR_INVALID, "optical horizon too long; reduce batch size");
   CUDA_TRY(cudaSetDevice(s->device), "select device");
+  if (s->staged_pending) {  // the previous upload still reads the staging
+    CUDA_TRY(cudaEventSynchronize(s->staged), "staging reuse");
+    s->staged_pending = false;
+  }
   // circuit cells, generate_pixels' loop bounds (event_sensor.cu:37-40)
   size_t n_cells = 0;
   for (size_t i = 0; i < count; ++i) n_cells += (size_t)std::ceil((ivs[i].t1 - ivs[i].t0) / s->photo.integration_step);
@@ -836,11 +847,17 @@ static int stage_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t co
 }
 
 // Uploads a staged batch and launches the per-cell pose kernel on `stream`.
-static int upload_staged(dvs_sensor *s, size_t count, size_t n_cells, cudaStream_t stream) {
+// track: record when the copies have run (not inside a graph capture, where
+// the batch synchronizes each step itself).
+static int upload_staged(dvs_sensor *s, size_t count, size_t n_cells, cudaStream_t stream, bool track) {
   CUDA_TRY(cudaMemcpyAsync(s->ivs, s->h_ivs, sizeof(dvs_optical_interval) * count, cudaMemcpyHostToDevice, stream),
            "trajectory interval upload");
   CUDA_TRY(cudaMemcpyAsync(s->cells, s->h_cells, sizeof(Cell) * n_cells, cudaMemcpyHostToDevice, stream),
            "cell upload");
+  if (track) {
+    CUDA_TRY(cudaEventRecord(s->staged, stream), "staging event");
+    s->staged_pending = true;
+  }
   CUDA_TRY(launch_cell_poses(s->ivs, s->cells, (int)n_cells, s->poses, stream), "cell poses");
   s->stats.launches += 1;
   return DVS_OK;
@@ -848,7 +865,7 @@ static int upload_staged(dvs_sensor *s, size_t count, size_t n_cells, cudaStream
 
 static int upload_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, size_t &n_cells_out) {
   int r = stage_batch(s, ivs, count, n_cells_out);
-  return r ? r : upload_staged(s, count, n_cells_out, s->stream);
+  return r ? r : upload_staged(s, count, n_cells_out, s->stream, true);
 }
 
 // Cells per optics launch and cells per warp packet for a batch.
@@ -1637,7 +1654,7 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
     cudaError_t e = cudaEventRecordWithFlags(b->ev_start, st, cudaEventRecordExternal);
     for (size_t m = 0; m < n && rc == DVS_OK && e == cudaSuccess; ++m) {
       if (!counts[m]) continue;
-      rc = upload_staged(b->members[m], counts[m], n_cells[m], st);
+      rc = upload_staged(b->members[m], counts[m], n_cells[m], st, false);
       if (rc == DVS_OK) rc = clear_batch_outputs(b->members[m], st);
     }
     for (int r = 0; r < rounds && rc == DVS_OK && e == cudaSuccess; ++r) {

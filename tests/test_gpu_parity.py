@@ -331,6 +331,39 @@ def test_seeded_shot_noise_repeatable():
         np.testing.assert_array_equal(ea[f], eb[f])
 
 
+def test_back_to_back_enqueues_equal_processing():
+    """Batches enqueued without collecting in between (the device-timed loop of
+    the benchmark) advance the pixel circuits exactly as processed batches:
+    each upload finishes reading the pinned staging before the next batch
+    overwrites it.  The last batch's events are those of processing."""
+    cam = dict(width=64, height=48, fx=60.0, fy=60.0, cx=32.0, cy=24.0)
+    V, N, I, camera, hap, scene = terrain_scene(n=80, seed=9, camera=cam, ss=2)
+    traj = trajectory.StraightPass((0.0, 0.0, 400.0), (50.0, 0.0, 0.0), trajectory.sun_direction(30), 1000.0)
+    phys = davis_physic(threshold_std=0.02, photon_shot_noise=1, max_events_per_step=64, readout_bandwidth=0,
+                        readout_latency=0, threshold_pos=0.05, threshold_neg=0.05, random_seed=3)
+    batches, t = [], 0.0
+    for k in range(6):
+        ivs = trajectory.horizons(traj, t, 1e-4, 8)
+        t = ivs[-1][3]
+        batches.append(ivs)
+    a, b = EventSensor(scene, phys), EventSensor(scene, phys)
+    a.initialize(traj.state(0.0), 0.0)
+    b.initialize(traj.state(0.0), 0.0)
+    for ivs in batches[:-1]:
+        a.enqueue(ivs)
+    a.enqueue(batches[-1])
+    last_a = a.collect()
+    for ivs in batches[:-1]:
+        b.process_many(ivs)
+    last_b = b.process_many(batches[-1])
+    sa, ra = a.read_state()
+    sb, rb = b.read_state()
+    assert np.array_equal(sa, sb) and np.array_equal(ra, rb)
+    assert len(last_a) == len(last_b) > 0
+    for f in ("timestamp", "x", "y", "polarity", "depth"):
+        np.testing.assert_array_equal(last_a[f], last_b[f])
+
+
 def test_capacity_error_and_rejections():
     scene, phys = plane_sensor(max_events_per_step=1, refractory_time=0, threshold_pos=0.01, threshold_neg=0.01,
                                threshold_min=0.001)
