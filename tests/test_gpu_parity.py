@@ -346,6 +346,9 @@ def test_back_to_back_enqueues_equal_processing():
         ivs = trajectory.horizons(traj, t, 1e-4, 8)
         t = ivs[-1][3]
         batches.append(ivs)
+    # a light pulse closes the last batch, so it carries events
+    p0, p1 = traj.state(t), traj.state(t + 2e-3)
+    batches[-1].append((dict(p0, intensity_rate=8e6), dict(p1, intensity_rate=-8e6), t, t + 2e-3))
     a, b = EventSensor(scene, phys), EventSensor(scene, phys)
     a.initialize(traj.state(0.0), 0.0)
     b.initialize(traj.state(0.0), 0.0)
