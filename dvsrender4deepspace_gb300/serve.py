@@ -69,6 +69,10 @@ class _Active:
         self.job, self.scene, self.sensor, self.reserved = job, scene, sensor, reserved
         self.cursor = 0.0
         self.chunks = []
+        # horizons of the job, counted once: float-rounded horizon ends (as the
+        # reference app's float time_resolution) must not add a horizon at the end
+        self.total_h = max(1, math.ceil(job.duration / job.time_resolution - 1e-9))
+        self.done_h = 0
 
 
 class Server:
@@ -105,12 +109,11 @@ class Server:
 
     def _remaining_samples(self, a):
         j = a.job
-        horizons = max(0, math.ceil((j.duration - a.cursor) / j.time_resolution - 1e-9))
-        return j.pixels * j.supersample ** 2 * horizons * self._cells_per_horizon(j)
+        return j.pixels * j.supersample ** 2 * (a.total_h - a.done_h) * self._cells_per_horizon(j)
 
     def _step_samples(self, a):
         j = a.job
-        horizons = min(self.horizons, max(1, math.ceil((j.duration - a.cursor) / j.time_resolution - 1e-9)))
+        horizons = min(self.horizons, a.total_h - a.done_h)
         return j.pixels * j.supersample ** 2 * horizons * self._cells_per_horizon(j)
 
     def _choose(self, active):
@@ -170,15 +173,16 @@ class Server:
             chosen = self._choose(active)
             for a in chosen:  # launch each chosen job's next batch; nothing waits here
                 j = a.job
-                count = min(self.horizons, max(1, math.ceil((j.duration - a.cursor) / j.time_resolution - 1e-9)))
+                count = min(self.horizons, a.total_h - a.done_h)
                 ivs = T.horizons(j.path, a.cursor, j.time_resolution, count)
                 a.sensor.enqueue(interval_array(ivs))
                 a.cursor = ivs[-1][3]
+                a.done_h += count
             self.steps += 1
             done = set()
             for a in chosen:
                 a.chunks.append(a.sensor.collect())
-                if a.cursor >= a.job.duration - 1e-12:
+                if a.done_h >= a.total_h:
                     self._release(a, now())
                     done.add(id(a))
             active = [a for a in active if id(a) not in done]
