@@ -243,6 +243,31 @@ def test_shadow_origins_above_tilted_plane(oracle32):
     assert failures == 0
 
 
+def test_watertight_known_answers(oracle32):
+    """Hit distance and barycentrics of the watertight test on a unit right
+    triangle: interior, on the hypotenuse, on a vertex, behind the origin,
+    and parallel to the plane."""
+    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    N = np.tile(np.float32([0, 0, 1]), (3, 1))
+    cam = dict(width=4, height=4, fx=1, fy=1, cx=2, cy=2)
+    hap = dict(b=0.24, c=0.305, hS=0.08, hC=1.0, thetap=0.45, w=0.324, B_S0=2.42, B_C0=0.0, phi=0.3)
+    sc = O.OracleScene(V, N, np.array([[0, 1, 2]]), cam, 1, hap, watertight=True)
+    tri, t, u, v = C.c_int(), C.c_float(), C.c_float(), C.c_float()
+
+    def hit(o, d):
+        o, d = np.float32(o), np.float32(d)
+        h = oracle32.oracle_trace_nearest(C.byref(sc.s), O.fptr(o), O.fptr(d), C.byref(tri), C.byref(t),
+                                          C.byref(u), C.byref(v))
+        return h, t.value, u.value, v.value
+    assert hit([0.25, 0.25, 2.0], [0, 0, -1]) == (1, 2.0, 0.25, 0.25)       # u on v1, v on v2
+    h, tt, uu, vv = hit([0.5, 0.5, 1.0], [0, 0, -1])                        # the hypotenuse
+    assert h == 1 and tt == 1.0 and uu + vv == 1.0
+    assert hit([0.0, 0.0, 3.0], [0, 0, -1])[:2] == (1, 3.0)                 # a vertex
+    assert hit([0.25, 0.25, -1.0], [0, 0, -1])[0] == 0                      # behind the origin
+    assert hit([0.25, 0.25, 1.0], [1, 0, 0])[0] == 0                        # parallel
+    assert hit([0.75, 0.75, 1.0], [0, 0, -1])[0] == 0                       # outside
+
+
 def test_watertight_test_closes_shared_edges(oracle32):
     """The precision geometry's watertight test (Woop et al. 2013): rays aimed at
     the shared diagonal of a two-triangle quad, at km coordinates, always hit
