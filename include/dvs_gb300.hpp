@@ -66,6 +66,8 @@ class DeviceScene {
   dvs_camera camera_{};
 };
 
+class SensorBatch;
+
 class DvsRayCaster {
  public:
   DvsRayCaster(std::shared_ptr<DeviceScene> scene, const dvs_physic &physic, const dvs_sensor_options *options = nullptr)
@@ -134,8 +136,10 @@ class DvsRayCaster {
   }
   std::size_t dropped_events() const { return stats().dropped; }
   std::size_t peak_queue() const { return stats().peak_queue; }
+  dvs_sensor *get() const { return sensor_.get(); }
 
  private:
+  friend class SensorBatch;
   void read(size_t n, std::vector<dvs_event> &events) {
     events.resize(n);
     size_t got = 0;
@@ -218,6 +222,52 @@ class CamRayCaster {
 
  private:
   std::shared_ptr<DeviceScene> scene_;
+};
+
+// Many DvsRayCasters over one scene geometry advanced together (dvs_batch_*):
+// one persistent trace launch and one circuit launch per step, captured into a
+// CUDA graph; each member's events are those it yields alone.  The members
+// must outlive the batch.  No counterpart in the reference.
+class SensorBatch {
+ public:
+  explicit SensorBatch(const std::vector<DvsRayCaster *> &members) : members_(members) {
+    std::vector<dvs_sensor *> handles;
+    for (DvsRayCaster *m : members) handles.push_back(m ? m->get() : nullptr);
+    dvs_batch *b = nullptr;
+    check(dvs_batch_create(handles.data(), handles.size(), &b));
+    batch_.reset(b);
+  }
+  // intervals[m]: member m's next contiguous intervals (empty: it idles this
+  // step); events[m] receives member m's ready events.
+  void advance_many(const std::vector<std::vector<dvs_optical_interval>> &intervals,
+                    std::vector<std::vector<dvs_event>> &events) {
+    const size_t n = members_.size();
+    if (intervals.size() != n) throw std::invalid_argument("one interval list per batch sensor");
+    std::vector<const dvs_optical_interval *> ptr(n);
+    std::vector<size_t> count(n), ready(n, 0);
+    for (size_t m = 0; m < n; ++m) {
+      ptr[m] = intervals[m].empty() ? nullptr : intervals[m].data();
+      count[m] = intervals[m].size();
+    }
+    check(dvs_batch_process(batch_.get(), ptr.data(), count.data(), ready.data()));
+    events.resize(n);
+    for (size_t m = 0; m < n; ++m) {
+      if (count[m]) members_[m]->read(ready[m], events[m]);
+      else events[m].clear();
+    }
+  }
+  dvs_batch_stats stats() const {
+    dvs_batch_stats st{};
+    check(dvs_batch_stats_get(batch_.get(), &st));
+    return st;
+  }
+
+ private:
+  struct Deleter {
+    void operator()(dvs_batch *b) const { dvs_batch_destroy(b); }
+  };
+  std::vector<DvsRayCaster *> members_;
+  std::unique_ptr<dvs_batch, Deleter> batch_;
 };
 
 }  // namespace dvs_gb300

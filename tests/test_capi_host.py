@@ -95,6 +95,14 @@ def test_cpp_facade_compiles_links_and_throws(lib, tmp_path):
     src.write_text(r'''
 #include "dvs_gb300.hpp"
 #include <cstdio>
+// compiled and linked, not called (it needs a GPU): the batch facade's API
+void batch_api(std::vector<dvs_gb300::DvsRayCaster *> members,
+               const std::vector<std::vector<dvs_optical_interval>> &ivs) {
+  dvs_gb300::SensorBatch batch(members);
+  std::vector<std::vector<dvs_event>> events;
+  batch.advance_many(ivs, events);
+  std::printf("%llu\n", (unsigned long long)batch.stats().graph_launches);
+}
 int main() {
   dvs_camera cam{4, 4, 1.f, 1.f, 2.f, 2.f};
   dvs_hapke hap{.24f, .3f, .08f, 1.f, .4f, .3f, 2.f, 0.f, .3f};
