@@ -191,11 +191,18 @@ def test_hapke_identity_form_against_the_fp64_reference_form(oracle32):
     k = 4000
     l, v = unit(k), unit(k)
     l[:, 2], v[:, 2] = np.abs(l[:, 2]), np.abs(v[:, 2])
+    l[:400, 2] *= 1e-3          # grazing light
+    v[400:800, 2] *= 1e-3       # grazing view
+    l /= np.linalg.norm(l, axis=1, keepdims=True)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
     geo = np.stack([l[:, 2], v[:, 2], (l * v).sum(1)], 1).astype(np.float32)
     mats = [dict(b=.3, c=.4, hS=.06, hC=1.0, thetap=0.349066, w=.25, B_S0=1.0, B_C0=0.0, phi=0.3),
             dict(b=0.24, c=0.305, hS=0.08, hC=1.0, thetap=26.0 * float(np.float32(math.pi)) / 180.0, w=0.324,
                  B_S0=2.42, B_C0=0.0, phi=0.3),
-            dict(b=.2, c=.5, hS=.05, hC=.05, thetap=0.0, w=.5, B_S0=1.5, B_C0=1.0, phi=0.0)]
+            dict(b=.2, c=.5, hS=.05, hC=.05, thetap=0.0, w=.5, B_S0=1.5, B_C0=1.0, phi=0.0),
+            # extremes: strong forward lobe, 40 degree roughness, w near 1, porous; near-smooth, dark
+            dict(b=.9, c=.1, hS=.01, hC=.02, thetap=0.7, w=0.99, B_S0=3.0, B_C0=1.0, phi=0.6),
+            dict(b=.05, c=.9, hS=.5, hC=.5, thetap=1e-9, w=0.01, B_S0=0.0, B_C0=0.5, phi=1e-9)]
     for m in mats:
         hs = O.hapke_struct(m)
 
@@ -214,7 +221,7 @@ def test_hapke_identity_form_against_the_fp64_reference_form(oracle32):
         assert np.mean(e_id > 1e-5) <= np.mean(e_ref > 1e-5) + 1e-3
         # cos psi clamped to -1: the FP32 reference's tan(pi_f / 2) < 0 overflows exp and
         # makes the sample NaN (dropped by the sampler); FP64 gives a finite value.
-        if m["thetap"] > 0:
+        if m["thetap"] > 1e-8:  # the rough branch (hapke.hpp:88 treats thetap <= 1e-8 as smooth)
             corner = np.float32([[0.5, 0.5, -0.51]])
             assert math.isnan(ev(oracle32, 0, corner)[0]) and math.isnan(ev(oracle32, 1, corner)[0])
             a, b = ev(o64, 0, corner)[0], ev(o64, 1, corner)[0]
