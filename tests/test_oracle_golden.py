@@ -221,7 +221,7 @@ def test_hapke_identity_form_against_the_fp64_reference_form(oracle32):
         assert np.mean(e_id > 1e-5) <= np.mean(e_ref > 1e-5) + 1e-3
         # cos psi clamped to -1: the FP32 reference's tan(pi_f / 2) < 0 overflows exp and
         # makes the sample NaN (dropped by the sampler); FP64 gives a finite value.
-        if m["thetap"] > 1e-8:  # the rough branch (hapke.hpp:88 treats thetap <= 1e-8 as smooth)
+        if m["thetap"] > 1e-8:  # the rough branch (hapke.hpp:89 treats thetap <= 1e-8 as smooth)
             corner = np.float32([[0.5, 0.5, -0.51]])
             assert math.isnan(ev(oracle32, 0, corner)[0]) and math.isnan(ev(oracle32, 1, corner)[0])
             a, b = ev(o64, 0, corner)[0], ev(o64, 1, corner)[0]
