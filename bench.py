@@ -64,10 +64,9 @@ PHYSIC = dict(threshold_pos=0.2, threshold_neg=0.2, refractory_time=200e-6, read
               readout_queue_capacity=1000000)
 METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency vs plain path"
 # DRAM bytes (read + write) per pixel-cell of one trace_cells_kernel launch, by
-# workload and BVH format, from the ncu captures summarised in
-# profiles/trace_cells_kernel_orbit_346x260_ss4.md and
-# profiles/launches_precision_1280x720_ss16.md (precision: a 16-cell launch of
-# the FP16-bounds tree, a 4-cell launch of the FP32 one, scaled by the cells traced).
+# workload and BVH format, measured with ncu's dram__bytes_read.sum and
+# dram__bytes_write.sum on one launch (precision: a 16-cell launch of the
+# FP16-bounds tree, a 4-cell launch of the FP32 one), scaled by the cells traced.
 TRACE_DRAM_BYTES_PER_PIXEL_CELL = {("precision", "half"): (33122816 + 75504384) / (16 * 921600),
                                    ("precision", "reference"): (32344832 + 1251328) / (4 * 921600),
                                    ("orbit", "reference"): (22470144 + 407428864) / (640 * 89960)}
@@ -144,14 +143,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(name, V, N, I, traj, w, budget_s=15.0, threads=0, osc=None, build_s=None):
-    """Oracle port (reference arithmetic, FP32 rays) on a bounded sample of the
-    workload's pixel-cells; returns Mrays/s and the sample description."""
+def cpu_baseline(name, V, N, I, traj, w, budget_s=15.0, threads=0, osc=None, build_s=None, fp64=False):
+    """Oracle port on a bounded sample of the workload's pixel-cells: the
+    optics only (primary + shadow rays with Hapke shading; the circuit, a
+    negligible share of the CPU time, is not in the sample), in the
+    reference's FP32 ray arithmetic or, with fp64, the FP64 oracle's.
+    Returns Mrays/s and the sample description."""
     from oracle import oracle as O
     cam = w["camera"]
     if osc is None:
         t_build = time.time()
-        osc = O.OracleScene(V, N, I, cam, w["ss"], HAPKE, max_leaf=64)
+        osc = O.OracleScene(V, N, I, cam, w["ss"], HAPKE, max_leaf=64, fp64=fp64)
         build_s = time.time() - t_build
     rng = np.random.default_rng(7)
     n_pix = cam["width"] * cam["height"]
@@ -167,11 +169,12 @@ def cpu_baseline(name, V, N, I, traj, w, budget_s=15.0, threads=0, osc=None, bui
         total_rays += prim + shad
         cells += 1
     return {"value": total_rays / total_t / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+            "scope": "optics only (rays + Hapke), %s oracle port" % ("FP64" if fp64 else "FP32"),
             "sample": "%d pixel-cells (%d random pixels x %d cell times, ss=%d), %.1f s of CPU work; oracle "
                       "binary BVH (leaf 64) built in %.1f s" % (batch * cells, batch, cells, w["ss"], total_t, build_s)}
 
 
-def precision_errors(V, N, I, traj, w, scene, geometry, circuit, budget_pixels=2048, threads=0):
+def precision_errors(V, N, I, traj, w, scene, geometry, circuit, budget_pixels=2048, threads=0, o64=None):
     """The precision config's accuracy statement, measured: the GPU path's
     radiance and depth on a seeded sample of the config's pixels (one pose,
     all sub-rays) against the FP64 oracle, and its events on a crop of the
@@ -182,34 +185,45 @@ def precision_errors(V, N, I, traj, w, scene, geometry, circuit, budget_pixels=2
     from oracle import oracle as O
     nthreads = threads or os.cpu_count()
     cam = w["camera"]
-    t_build = time.time()
-    o64 = O.OracleScene(V, N, I, cam, w["ss"], HAPKE, max_leaf=64, fp64=True,
-                        watertight=bool(GEOMETRY[geometry] & 2))
-    build_s = time.time() - t_build
-    out = {"oracle": "FP64 (geometry, rays, Hapke in double; binary BVH leaf 64, built in %.1f s)" % build_s,
+    if o64 is None:
+        o64 = O.OracleScene(V, N, I, cam, w["ss"], HAPKE, max_leaf=64, fp64=True,
+                            watertight=bool(GEOMETRY[geometry] & 2))
+    out = {"oracle": "FP64 (geometry, rays, Hapke in double; binary BVH leaf 64)",
            "geometry": geometry, "circuit_precision": circuit}
-    # radiance and depth: one pose, seeded pixel sample
+    # radiance and depth: one pose, seeded pixel sample, with the oracle's
+    # margin classes (optical margin, conditioning, crack) named per pixel
     pose = traj.state(0.0)
     img, dep = CamRayCaster(scene).render_state(pose)
     rng = np.random.default_rng(11)
     pix = rng.choice(cam["width"] * cam["height"], size=budget_pixels, replace=False).astype(np.int32)
-    orad, odep, _, _ = o64.render_pixels(pose, pix, nthreads)
+    t_cls = time.time()
+    orad, odep, margin = o64.render_margin(pose, pix, nthreads=nthreads)
+    out["classifier_seconds"] = time.time() - t_cls
     g_rad, g_dep = img.reshape(-1)[pix].astype(np.float64), dep.reshape(-1)[pix].astype(np.float64)
     lit = orad > 0
-    rel = np.abs(g_rad[lit] - orad[lit]) / orad[lit]
+    rel = np.where(lit, np.abs(g_rad - orad) / np.where(lit, orad, 1.0), 0.0)
     hit = odep > 0
-    drel = np.abs(g_dep[hit] - odep[hit]) / odep[hit]
-    out["radiance"] = {"pixels": int(lit.sum()), "max_rel": float(rel.max()), "p99_rel": float(np.quantile(rel, .99)),
-                       "frac_above_1e-5": float(np.mean(rel > 1e-5))}
-    out["depth"] = {"pixels": int(hit.sum()), "max_rel": float(drel.max()), "p99_rel": float(np.quantile(drel, .99)),
-                    "frac_above_1e-5": float(np.mean(drel > 1e-5)), "misses_agree": bool(np.all((g_dep[~hit] < 0)))}
+    drel = np.where(hit, np.abs(g_dep - odep) / np.where(hit, odep, 1.0), 0.0)
+    plain = margin == 0
+    classes = {"optical": int(np.count_nonzero(margin & O.MARGIN_OPTICAL)),
+               "conditioning": int(np.count_nonzero(margin & O.MARGIN_CONDITIONING)),
+               "crack": int(np.count_nonzero(margin & O.MARGIN_CRACK))}
+    out["radiance"] = {"pixels": int(lit.sum()), "max_rel": float(rel[lit].max()),
+                       "p99_rel": float(np.quantile(rel[lit], .99)), "above_1e-5": int((rel > 1e-5).sum()),
+                       "margin_pixels": int((~plain).sum()), "margin_classes": classes,
+                       "non_margin_above_1e-5": int(((rel > 1e-5) & plain).sum()),
+                       "max_rel_non_margin": float(rel[lit & plain].max())}
+    out["depth"] = {"pixels": int(hit.sum()), "max_rel": float(drel[hit].max()),
+                    "p99_rel": float(np.quantile(drel[hit], .99)), "above_1e-5": int((drel > 1e-5).sum()),
+                    "non_margin_above_1e-5": int(((drel > 1e-5) & plain).sum()),
+                    "misses_agree_non_margin": bool(np.all((g_dep < 0) == (odep < 0) | ~plain))}
     # events: a 16x12 crop at the image centre, 0.5 ms light pulse (500 cells of 1 us)
     x0, y0 = cam["width"] // 2 - 8, cam["height"] // 2 - 6
     crop = dict(cam, width=16, height=12, cx=cam["cx"] - x0, cy=cam["cy"] - y0)
     phys = dict(PHYSIC, photon_shot_noise=0, threshold_std=0, readout_bandwidth=0, readout_latency=0,
                 max_events_per_step=64)
     sensor = EventSensor(scene.view(crop, w["ss"]), phys, circuit_precision=circuit)
-    ors = O.OracleSensor(o64.with_camera(crop), phys)
+    ors = O.OracleSensor(o64.with_camera(crop), phys, margin=True)
     sensor.initialize(pose, 0.0)
     ors.initialize(pose, 0.0, nthreads)
     a, b = dict(pose, intensity_rate=1.6e8), dict(traj.state(5e-4), intensity_rate=-1.6e8)
@@ -218,6 +232,7 @@ def precision_errors(V, N, I, traj, w, scene, geometry, circuit, budget_pixels=2
     gev = np.concatenate([sensor.process_many(ivs), sensor.drain()])
     oev = np.concatenate([ors.process(ivs, nthreads), ors.drain()])
     cpu_s = time.time() - t0
+    margins = ors.margins()
 
     def per_pixel(ev):
         d = {}
@@ -225,18 +240,22 @@ def precision_errors(V, N, I, traj, w, scene, geometry, circuit, budget_pixels=2
             d.setdefault((int(e["x"]), int(e["y"])), []).append((float(e["timestamp"]), int(e["polarity"])))
         return d
     pg, po = per_pixel(gev), per_pixel(oev)
-    same, worst = 0, 0.0
+    same, unclassified, worst = 0, 0, 0.0
     for key in set(pg) | set(po):
         x, y = pg.get(key, []), po.get(key, [])
+        flagged = margins[key[1] * crop["width"] + key[0]] != 0
         if [p for _, p in x] == [p for _, p in y]:
             same += 1
-            if x:
+            if x and not flagged:
                 worst = max(worst, max(abs(u - v) for (u, _), (v, _) in zip(x, y)))
+        elif not flagged:
+            unclassified += 1
     n_px = len(set(pg) | set(po))
     out["events"] = {"crop": "16x12 at (%d, %d)" % (x0, y0), "interval": "0.5 ms pulse, 500 cells",
                      "gpu_events": int(len(gev)), "oracle_events": int(len(oev)), "pixels_with_events": n_px,
-                     "pixels_same_polarity_sequence": same, "max_timestamp_error_s": worst,
-                     "oracle_seconds": cpu_s}
+                     "pixels_same_polarity_sequence": same, "margin_pixels": int((margins != 0).sum()),
+                     "non_margin_sequence_mismatches": unclassified,
+                     "max_timestamp_error_s_non_margin": worst, "oracle_seconds": cpu_s}
     return out
 
 
@@ -419,11 +438,21 @@ def run_gb300(args):
     circuit_ms = st["circuit_ms"] / max(1, st["circuit_launches"])
     circuit_bytes = n_pix * cells_per_launch * 8.0 + n_pix * (5 * 8 + 1 + 48) * 2 + n_pix * 4 * 2
     cb = None
+    o64 = None
     if not args.no_cpu_baseline:
         cb = cpu_baseline(args.workload, V, N, I, traj, w, budget_s=15.0)
+        # beside it, the FP64 oracle of the same optics (the precision report's oracle)
+        from oracle import oracle as O
+        t_build = time.time()
+        o64 = O.OracleScene(V, N, I, w["camera"], w["ss"], HAPKE, max_leaf=64, fp64=True,
+                            watertight=bool(GEOMETRY[args.geometry] & 2))
+        b64 = time.time() - t_build
+        cb64 = cpu_baseline(args.workload, V, N, I, traj, w, budget_s=8.0, osc=o64, build_s=b64, fp64=True)
+        cb["fp64_oracle"] = {"value": cb64["value"], "unit": cb64["unit"], "cores": cb64["cores"],
+                             "sample": cb64["sample"]}
     errors = None
     if args.workload == "precision" and not args.no_precision_report and rank == 0:
-        errors = precision_errors(V, N, I, traj, w, scene, args.geometry, args.circuit)
+        errors = precision_errors(V, N, I, traj, w, scene, args.geometry, args.circuit, o64=o64)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",

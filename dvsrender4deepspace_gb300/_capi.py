@@ -105,7 +105,7 @@ EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_d
            "dvs_readout_counters", "dvs_config_load", "dvs_frames_load", "dvs_trajectory_create",
            "dvs_trajectory_destroy", "dvs_trajectory_range", "dvs_trajectory_evaluate", "dvs_cam_render_blur",
            "dvs_scene_view_create", "dvs_sensor_device_bytes", "dvs_sensor_set_tuning", "dvs_sensor_autotune",
-           "dvs_batch_create", "dvs_batch_destroy", "dvs_batch_process", "dvs_batch_stats_get")
+           "dvs_batch_create", "dvs_batch_destroy", "dvs_batch_process", "dvs_batch_stats_get", "dvs_noise_poisson")
 
 
 class Tuning(C.Structure):
@@ -151,6 +151,7 @@ def _declare(lib):
     lib.dvs_sensor_options_default.argtypes = [C.POINTER(SensorOptions)]
     lib.dvs_sensor_options_default.restype = None
     lib.dvs_derive_parameters.argtypes = [C.POINTER(Physic), C.c_int32, C.POINTER(C.c_double)]
+    lib.dvs_noise_poisson.argtypes = [C.c_int32, C.c_double, C.c_uint32, sz, C.POINTER(C.c_double)]
     lib.dvs_scene_create.argtypes = [f_p, f_p, C.POINTER(C.c_uint32), f_p, sz, sz, C.POINTER(Camera), C.c_int32,
                                      C.POINTER(Hapke), C.POINTER(BvhParams), C.POINTER(vp)]
     lib.dvs_scene_destroy.argtypes = [vp]

@@ -119,6 +119,9 @@ cudaError_t grow_pinned(T *&ptr, size_t &cap, size_t need) {
 
 }  // namespace
 
+// Per-device set-up of dvs_cam_render_noalloc (noalloc.cu).
+int dvsgb_noalloc_prepare(int device, int geometry);
+
 // ---- handles --------------------------------------------------------------------
 struct dvs_scene {
   int device = 0;
@@ -255,12 +258,22 @@ struct dvs_sensor {
   int pixels() const { return n_pix; }
   CellPose *probe_poses = nullptr;  // the five initial adaptive probe poses
   int rays_per_lane = 2;  // traversal tuning: 1, 2 or 4 sub-rays per lane (dvs_sensor_set_tuning / autotune)
+  // The view the hot path traces with: its radiance chunk is float when the
+  // circuit is FP32 (photo.chunk_f32).  view64: the same with a double chunk,
+  // for the initialization and the adaptive solver's knots and probes.
   SceneView view() const {
+    SceneView v = view64();
+    v.radiance_f32 = photo.chunk_f32;
+    return v;
+  }
+  SceneView view64() const {
     SceneView v = scene->view();
     v.pixel_of_rank = order;
     v.rays = rays_per_lane;
+    v.radiance_f32 = 0;
     return v;
   }
+  size_t chunk_bytes_per_cell() const { return photo.chunk_f32 ? sizeof(float) : sizeof(double); }
 };
 
 // Accessors for the no-allocation entry point (noalloc.cu).
@@ -278,6 +291,23 @@ void dvs_sensor_options_default(dvs_sensor_options *out) {
   std::memset(out, 0, sizeof(*out));
   out->physic_effects = 1;
   out->aer_delay = 1;
+}
+
+int dvs_noise_poisson(int32_t generator, double lambda, uint32_t seed, size_t n, double *out) {
+  if (!out || n == 0 || n > (size_t(1) << 28) || (generator != 0 && generator != 1) || !std::isfinite(lambda))
+    return fail(DVS_ERR_INVALID, "invalid photon-count draw request");
+  double *d = nullptr;
+  cudaStream_t st = nullptr;
+  CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "draw stream");
+  cudaError_t e = cudaMallocAsync(&d, sizeof(double) * n, st);
+  if (e == cudaSuccess) e = launch_poisson_draws(generator, lambda, seed, (int)n, 0.0, d, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+  if (d) cudaFreeAsync(d, st);
+  const cudaError_t es = cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  if (e == cudaSuccess) e = es;
+  if (e != cudaSuccess) return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in photon-count draws : ") + cudaGetErrorString(e));
+  return DVS_OK;
 }
 
 int dvs_derive_parameters(const dvs_physic *physic, int32_t physic_effects, double *out9) {
@@ -329,27 +359,34 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   std::vector<BvhQNode> qnodes;
   if (half_bounds && !quantize_bvh(bvh.nodes, qnodes, err)) return fail(DVS_ERR_INVALID, err);
 
-  // leaf-order records
-  std::vector<TriRecord> tris(n_triangles);
+  // leaf-order records; a watertight scene keeps three copies of each
+  // triangle's vertices, copy k in the cyclic axis order ((k+1)%3, (k+2)%3, k)
+  // that the watertight test of a ray with dominant axis k reads
+  const size_t copies = watertight ? 3 : 1;
+  std::vector<TriRecord> tris(n_triangles * copies);
   std::vector<ShadeRecord> shade(n_triangles);
   const long long nt = (long long)n_triangles;
 #pragma omp parallel for schedule(static)
   for (long long i = 0; i < nt; ++i) {
     const uint32_t src = bvh.order[i];
     const uint32_t a = indices[3 * (size_t)src], b = indices[3 * (size_t)src + 1], c = indices[3 * (size_t)src + 2];
-    TriRecord &t = tris[i];
-    std::memset(&t, 0, sizeof(t));
-    for (int d = 0; d < 3; ++d) {
-      t.v0[d] = vertices[3 * (size_t)a + d];
-      if (watertight) {  // the vertices themselves, for the watertight test
-        t.e1[d] = vertices[3 * (size_t)b + d];
-        t.e2[d] = vertices[3 * (size_t)c + d];
-      } else {
-        t.e1[d] = vertices[3 * (size_t)b + d] - vertices[3 * (size_t)a + d];
-        t.e2[d] = vertices[3 * (size_t)c + d] - vertices[3 * (size_t)a + d];
+    for (size_t k = 0; k < copies; ++k) {
+      TriRecord &t = tris[i * copies + k];
+      std::memset(&t, 0, sizeof(t));
+      const int axis[3] = {(int)(k + 1) % 3, (int)(k + 2) % 3, (int)k};
+      for (int d = 0; d < 3; ++d) {
+        if (watertight) {  // the vertices themselves, for the watertight test
+          t.v0[d] = vertices[3 * (size_t)a + axis[d]];
+          t.e1[d] = vertices[3 * (size_t)b + axis[d]];
+          t.e2[d] = vertices[3 * (size_t)c + axis[d]];
+        } else {
+          t.v0[d] = vertices[3 * (size_t)a + d];
+          t.e1[d] = vertices[3 * (size_t)b + d] - vertices[3 * (size_t)a + d];
+          t.e2[d] = vertices[3 * (size_t)c + d] - vertices[3 * (size_t)a + d];
+        }
       }
+      t.original = src;
     }
-    t.original = src;
     ShadeRecord &s = shade[i];
     std::memset(&s, 0, sizeof(s));
     for (int d = 0; d < 3; ++d) {
@@ -390,7 +427,7 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   const size_t off_nodes = 0;
   const size_t node_bytes = half_bounds ? sizeof(BvhQNode) : sizeof(BvhNode);
   const size_t off_tris = align_up(off_nodes + node_bytes * s->n_nodes, 256);
-  const size_t off_shade = align_up(off_tris + sizeof(TriRecord) * n_triangles, 256);
+  const size_t off_shade = align_up(off_tris + sizeof(TriRecord) * tris.size(), 256);
   const size_t total = align_up(off_shade + sizeof(ShadeRecord) * n_triangles, 256);
   void *arena = nullptr;
   cudaError_t e = cudaMalloc(&arena, total);
@@ -416,7 +453,7 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
     e = cudaMemcpy(s->qnodes, qnodes.data(), sizeof(BvhQNode) * s->n_nodes, cudaMemcpyHostToDevice);
   else
     e = cudaMemcpy(s->nodes, bvh.nodes.data(), sizeof(BvhNode) * s->n_nodes, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(s->tris, tris.data(), sizeof(TriRecord) * n_triangles, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(s->tris, tris.data(), sizeof(TriRecord) * tris.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(s->shade, shade.data(), sizeof(ShadeRecord) * n_triangles, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -425,6 +462,10 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   if (e != cudaSuccess) {
     dvs_scene_destroy(s);
     return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in upload scene array : ") + cudaGetErrorString(e));
+  }
+  if (int r = dvsgb_noalloc_prepare(s->device, s->geometry_kind)) {
+    dvs_scene_destroy(s);
+    return r;
   }
   *out = s;
   return DVS_OK;
@@ -498,6 +539,10 @@ int dvs_scene_view_create(const dvs_scene *base, const dvs_camera *camera, int32
     return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in upload scene array : ") + cudaGetErrorString(e));
   }
   s->arena_bytes = sizeof(int32_t) * order.size();  // its own allocations; the geometry is the base's
+  if (int r = dvsgb_noalloc_prepare(s->device, s->geometry_kind)) {
+    dvs_scene_destroy(s);
+    return r;
+  }
   *out = s;
   return DVS_OK;
 }
@@ -635,6 +680,7 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
   s->order = scene->pixel_of_rank;
   derive(*physic, s->opt.physic_effects != 0, s->p, s->photo);
   s->photo.fp32_circuit = s->opt.circuit_precision >= 1;
+  s->photo.chunk_f32 = s->photo.fp32_circuit;
   s->photo.philox = s->opt.circuit_precision == 2;
   s->photo.seed = (uint32_t)physic->random_seed;
   s->threshold_std = s->opt.physic_effects ? physic->threshold_std : 0;
@@ -756,7 +802,13 @@ static int map_error(int32_t word) {
   return DVS_OK;
 }
 
+// A radiance chunk of `cells` cells in the hot path's format (the buffer is
+// sized in doubles; a float chunk takes half as many).
 static cudaError_t ensure_radiance(dvs_sensor *s, size_t cells) {
+  const size_t bytes = cells * (size_t)s->pixels() * s->chunk_bytes_per_cell();
+  return grow_device(s->radiance, s->radiance_cap, (bytes + sizeof(double) - 1) / sizeof(double));
+}
+static cudaError_t ensure_radiance64(dvs_sensor *s, size_t cells) {
   return grow_device(s->radiance, s->radiance_cap, cells * (size_t)s->pixels());
 }
 
@@ -766,14 +818,14 @@ int dvs_sensor_initialize(dvs_sensor *s, const dvs_optical_state *pose, double t
     return fail(DVS_ERR_INVALID, "invalid sensor initialization");
   CUDA_TRY(cudaSetDevice(s->device), "select device");
   const int n = s->pixels();
-  CUDA_TRY(ensure_radiance(s, 1), "initial radiance");
+  CUDA_TRY(ensure_radiance64(s, 1), "initial radiance");
   CUDA_TRY(grow_device(s->poses, s->poses_cap, 1), "pose buffer");
   *s->h_state = *pose;
   CUDA_TRY(cudaMemcpyAsync(s->d_state, s->h_state, sizeof(dvs_optical_state), cudaMemcpyHostToDevice, s->stream),
            "upload pose");
   CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream), "clear initialization error");
   CUDA_TRY(launch_pose_from_state(s->d_state, s->poses, s->stream), "pose");
-  CUDA_TRY(launch_trace_cells(s->view(), n, s->poses, 0, 1, 0, s->radiance, nullptr, s->counters, s->stream),
+  CUDA_TRY(launch_trace_cells(s->view64(), n, s->poses, 0, 1, 0, s->radiance, nullptr, s->counters, s->stream),
            "initial optics");
   CUDA_TRY(launch_init_pixels(n, s->order, s->radiance, s->p, s->photo, s->threshold_std,
                               s->threshold_min, s->seed, s->st, s->error_word, s->stream),
@@ -871,7 +923,8 @@ static int upload_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t c
 // Cells per optics launch and cells per warp packet for a batch.
 static void chunk_shape(const dvs_sensor *s, size_t n_cells, size_t rows, size_t &chunk, int &cw_log2) {
   chunk = s->opt.cells_per_chunk > 0 ? (size_t)s->opt.cells_per_chunk
-                                     : std::max<size_t>(1, std::min<size_t>(2048, (size_t(512) << 20) / (8 * rows)));
+                                     : std::max<size_t>(1, std::min<size_t>(2048, (size_t(512) << 20) /
+                                                                                   (s->chunk_bytes_per_cell() * rows)));
   chunk = std::min(chunk, n_cells);
   cw_log2 = 0;
   if (s->opt.cells_per_warp > 0) {
@@ -1049,7 +1102,7 @@ static int ensure_exact(dvs_sensor *s) {
 // verify_receptor (event_sensor.cu:357-374): the probe pixels' receptors
 // driven by exactly traced and by interpolated light over every cell.
 static int verify_receptor(dvs_sensor *s, size_t n_cells, double start, double end) {
-  const SceneView view = s->view();
+  const SceneView view = s->view64();
   const int np = s->n_probes;
   size_t chunk;
   int cw_log2;
@@ -1106,12 +1159,12 @@ int dvs_sensor_process_adaptive(dvs_sensor *s, const dvs_optical_interval *ivs, 
   if (r) return r;
   if ((r = ensure_adaptive(s))) return r;
   const int n = s->pixels(), cap = s->knot_capacity;
-  const SceneView view = s->view();
+  const SceneView view = s->view64();  // knots, probes and exact cells are FP64
   // all refinement completes and is checked before pixel/RNG state changes
   CUDA_TRY(cudaMemsetAsync(s->ref_stats, 0, sizeof(unsigned long long) * kRefSlots, s->stream), "clear statistics");
   CUDA_TRY(cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream), "clear refinement errors");
   record_timer(s, 0);
-  CUDA_TRY(ensure_radiance(s, 5), "initial probe radiance");
+  CUDA_TRY(ensure_radiance64(s, 5), "initial probe radiance");
   if (!s->probe_poses) CUDA_TRY(cudaMalloc(&s->probe_poses, sizeof(CellPose) * 5), "probe poses");
   CUDA_TRY(launch_refine(view, n, s->ivs, (int)count, start, end, s->photo, tolerance, s->st, s->p.charge_scale, cap,
                          s->probe_poses, s->radiance, s->knots, s->knot_counts, s->ref_stats, s->error_word,
@@ -1181,8 +1234,9 @@ int dvs_sensor_process_adaptive(dvs_sensor *s, const dvs_optical_interval *ivs, 
     CUDA_TRY(grow_device(s->radiance, s->radiance_cap, chunk * (size_t)nf), "fallback optical tile");
     for (size_t c0 = 0; c0 < n_cells; c0 += chunk) {
       const int nc = (int)std::min(chunk, n_cells - c0);
-      CUDA_TRY(launch_trace_list(view, nf, s->fallback_list, s->poses, (int)c0, nc, cw_log2, s->radiance, nullptr,
-                                 s->counters, s->stream),
+      // the fallback tile feeds the circuit: the hot path's chunk format
+      CUDA_TRY(launch_trace_list(s->view(), nf, s->fallback_list, s->poses, (int)c0, nc, cw_log2, s->radiance,
+                                 nullptr, s->counters, s->stream),
                "parallel exact cell optics launch");
       CUDA_TRY(launch_circuit_list(nf, s->fallback_list, s->cells, (int)c0, nc, s->radiance, s->p, s->photo,
                                    s->max_events, s->st, s->ev_count, s->slab_t, s->slab_p, s->error_word,
@@ -1547,6 +1601,11 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
   std::vector<int> cw(n, 0);
   bool any = false;
   int rounds = 0;
+  // a member's enqueued batch must be collected first: the step would clear
+  // and overwrite the events that batch left on the device
+  for (size_t m = 0; m < n; ++m)
+    if (counts[m] && b->members[m]->pending)
+      return fail(DVS_ERR_INVALID, "a batch member has an uncollected dvs_sensor_enqueue; collect it first");
   // stage every active member's intervals and cells; allocations happen here,
   // before any capture
   for (size_t m = 0; m < n; ++m) {

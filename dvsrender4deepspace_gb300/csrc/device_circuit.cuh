@@ -216,22 +216,57 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, float rate
   return count;
 }
 
+// Poisson draw for means of 10 and more by the transformed rejection method
+// with squeeze of W. Hormann, "The transformed rejection method for
+// generating Poisson random variables", Insurance: Mathematics and Economics
+// 12 (1993) 39-45 (algorithm PTRS).  A candidate k comes from a transformed
+// uniform U, a second uniform V accepts it at once inside the squeeze (about
+// 90 % of candidates at these means), and the rest are decided by the exact
+// test log(V * alpha / (a / us^2 + b)) <= k log(mu) - mu - log(k!), evaluated
+// in FP64 because it cancels large terms.  The constants are the paper's.
+// Every candidate takes two uniforms; after 64 rejected candidates (a
+// probability far below 1e-60) the draw falls back to the rounded normal.
+__device__ __forceinline__ float poisson_ptrs(curandStatePhilox4_32_10_t &st, float mu) {
+  const float smu = sqrtf(mu);
+  const float b = 0.931f + 2.53f * smu;
+  const float a = -0.059f + 0.02483f * b;
+  const float inv_alpha = 1.1239f + 1.1328f / (b - 3.4f);
+  const float v_r = 0.9277f - 3.6224f / (b - 2.0f);
+  for (int attempt = 0; attempt < 64; ++attempt) {
+    const float U = curand_uniform(&st) - 0.5f;  // (-1/2, 1/2]
+    const float V = curand_uniform(&st);         // (0, 1]
+    const float us = 0.5f - fabsf(U);
+    if (us < 0.013f && V > us) continue;  // outside the hat's usable part (also guards us == 0)
+    const float k = floorf((2.0f * a / us + b) * U + mu + 0.43f);
+    if (us >= 0.07f && V <= v_r) return k;
+    if (k < 0.0f) continue;
+    const double lhs = log((double)V) + log((double)inv_alpha) - log((double)a / ((double)us * us) + (double)b);
+    const double rhs = -(double)mu + (double)k * log((double)mu) - lgamma((double)k + 1.0);
+    if (lhs <= rhs) return k;
+  }
+  return fmaxf(0.0f, floorf(mu + smu * curand_normal(&st) + 0.5f));
+}
+
 // Photon count of one cell from a counter-based Philox stream (precision
-// mode): inversion of the Poisson CDF by sequential search for small means
-// (the photon-starved regime of the sensor), a rounded normal approximation
-// above 64 electrons.  The stream is keyed by (seed, pixel) and placed at the
-// cell's absolute index, so the draws do not depend on how cells are batched.
+// mode): inversion of the Poisson CDF by sequential search below a mean of 10
+// (the photon-starved regime of the sensor), PTRS from 10 to 1e6, and above
+// 1e6 the rounded normal approximation the reference's poisson_electrons
+// uses there (include/dvs/photon_noise.cuh:7).  The stream is keyed by
+// (seed, pixel) and placed at the cell's absolute index, so the draws do not
+// depend on how cells are batched.
 __device__ __forceinline__ float poisson_electrons_philox(curandStatePhilox4_32_10_t &st, float lambda) {
   if (!(lambda > 0)) return 0;
-  if (lambda > 64) return fmaxf(0.0f, floorf(lambda + sqrtf(lambda) * curand_normal(&st) + 0.5f));
+  if (lambda > 1e6f) return fmaxf(0.0f, floorf(lambda + sqrtf(lambda) * curand_normal(&st) + 0.5f));
+  if (lambda >= 10.0f) return poisson_ptrs(st, lambda);
   const float u = curand_uniform(&st);  // (0, 1]
   float p = expf(-lambda), F = p;
   int k = 0;
   while (u > F && k < 512) {
     ++k;
     p *= lambda / (float)k;
-    if (!(p > 0.0f)) break;  // the CDF stopped growing in float
-    F += p;
+    const float next = F + p;
+    if (!(next > F)) break;  // the CDF stopped growing in float (tail mass below its last ulp)
+    F = next;
   }
   return (float)k;
 }

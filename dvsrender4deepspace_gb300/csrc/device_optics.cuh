@@ -251,35 +251,42 @@ __device__ __forceinline__ bool intersect_tri(float3 ray, float3 o, float3 v0, f
 // function that rounds to exactly zero is recomputed in FP64 (the products of
 // two floats are exact there), as the paper prescribes.  U, V, W weight v0,
 // v1, v2, so the reference's barycentrics (u on v1, v on v2) are V/det, W/det.
+//
+// GB300 layout: a watertight scene stores each triangle three times, its
+// vertices in the cyclic axis orders (y,z,x), (z,x,y) and (x,y,z) -- copy kz
+// lists axis kz last -- and a ray reads the copy of its dominant axis, so the
+// test runs on vertices already in the ray's (kx, ky, kz) order without a
+// select per component.  The paper's swap of kx and ky for a negative
+// direction only preserves the winding: it negates U, V, W, det and T
+// exactly, so t, u and v are the same bits with or without it, and the
+// kernels leave it out.
 struct WtRay {
-  int kx, ky, kz;
+  int kz;
   float sx, sy, sz;
 };
 __device__ __forceinline__ float comp3(float3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+// A vector in the cyclic order whose last axis is kz.
+__device__ __forceinline__ float3 wt_perm(float3 v, int kz) {
+  return kz == 2 ? v : (kz == 0 ? f3(v.y, v.z, v.x) : f3(v.z, v.x, v.y));
+}
 __device__ __forceinline__ WtRay wt_setup(float3 d) {
   const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
   WtRay w;
   w.kz = ax > ay ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
-  w.kx = w.kz == 2 ? 0 : w.kz + 1;
-  w.ky = w.kx == 2 ? 0 : w.kx + 1;
-  const float dz = comp3(d, w.kz);
-  if (dz < 0.0f) {
-    const int k = w.kx;
-    w.kx = w.ky;
-    w.ky = k;
-  }
-  w.sx = comp3(d, w.kx) / dz;
-  w.sy = comp3(d, w.ky) / dz;
-  w.sz = 1.0f / dz;
+  const float3 p = wt_perm(d, w.kz);
+  w.sx = p.x / p.z;
+  w.sy = p.y / p.z;
+  w.sz = 1.0f / p.z;
   return w;
 }
+// o, v0, v1, v2 in the ray's cyclic order (wt_perm).
 __device__ __forceinline__ bool intersect_wt(const WtRay &w, float3 o, float3 v0, float3 v1, float3 v2, float &t,
                                              float &u, float &v) {
   const float3 A = v0 - o, B = v1 - o, C = v2 - o;
-  const float az = comp3(A, w.kz), bz = comp3(B, w.kz), cz = comp3(C, w.kz);
-  const float ax = comp3(A, w.kx) - w.sx * az, ay = comp3(A, w.ky) - w.sy * az;
-  const float bx = comp3(B, w.kx) - w.sx * bz, by = comp3(B, w.ky) - w.sy * bz;
-  const float cx = comp3(C, w.kx) - w.sx * cz, cy = comp3(C, w.ky) - w.sy * cz;
+  const float az = A.z, bz = B.z, cz = C.z;
+  const float ax = A.x - w.sx * az, ay = A.y - w.sy * az;
+  const float bx = B.x - w.sx * bz, by = B.y - w.sy * bz;
+  const float cx = C.x - w.sx * cz, cy = C.y - w.sy * cz;
   float U = cx * by - cy * bx, V = ax * cy - ay * cx, W = bx * ay - by * ax;
   if (U == 0.0f || V == 0.0f || W == 0.0f) {
     U = (float)((double)cx * (double)by - (double)cy * (double)bx);
@@ -298,19 +305,33 @@ __device__ __forceinline__ bool intersect_wt(const WtRay &w, float3 o, float3 v0
   return true;
 }
 // One leaf-order triangle record against one ray.  Records hold (v0, e1, e2),
-// or (v0, v1, v2) in watertight scenes.
+// or in watertight scenes (v0, v1, v2) in the ray's cyclic order; o is the
+// ray origin, op the origin in that order (watertight scenes).
 template <int kGeo>
-__device__ __forceinline__ bool tri_hit(const WtRay &w, float3 d, float3 o, float4 a, float4 b, float4 q, float &t,
-                                        float &u, float &v) {
+__device__ __forceinline__ bool tri_hit(const WtRay &w, float3 d, float3 o, float3 op, float4 a, float4 b, float4 q,
+                                        float &t, float &u, float &v) {
   if constexpr (!(kGeo & kGeoWatertight))
     return intersect_tri(d, o, f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, q.x), t, u, v);
   else
-    return intersect_wt(w, o, f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, q.x), t, u, v);
+    return intersect_wt(w, op, f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, q.x), t, u, v);
 }
 template <int kGeo>
 __device__ __forceinline__ WtRay wt_ray(float3 d) {
-  if constexpr (!(kGeo & kGeoWatertight)) return WtRay{0, 0, 0, 0.f, 0.f, 0.f};
+  if constexpr (!(kGeo & kGeoWatertight)) return WtRay{2, 0.f, 0.f, 0.f};
   else return wt_setup(d);
+}
+template <int kGeo>
+__device__ __forceinline__ float3 wt_origin(const WtRay &w, float3 o) {
+  if constexpr (!(kGeo & kGeoWatertight)) return o;
+  else return wt_perm(o, w.kz);
+}
+// The record of leaf-order triangle `tri` a ray with dominant axis kz reads:
+// the single record, or in watertight scenes its copy kz (copy 2 holds the
+// vertices in world order).
+template <int kGeo>
+__device__ __forceinline__ const float4 *tri_record(const SceneView &S, int tri, int kz) {
+  if constexpr (!(kGeo & kGeoWatertight)) return reinterpret_cast<const float4 *>(S.tris + tri);
+  else return reinterpret_cast<const float4 *>(S.tris + 3 * (size_t)tri + kz);
 }
 
 // ---- 8-wide packet traversal ------------------------------------------------------
@@ -552,6 +573,7 @@ __device__ HitRecord trace_nearest_packet(const SceneView &S, float3 o, float3 d
                                           float *stack_t) {
   const float3 idir = inverse_direction(d);
   const WtRay wr = wt_ray<kGeo>(d);
+  const float3 op = wt_origin<kGeo>(wr, o);
   float closest = active ? 1e30f : -1.0f;
   HitRecord h{0, -1, 0.f, 0.f, 0.f};
   const Packet P = make_packet(S, o, d, idir, active);
@@ -578,10 +600,10 @@ __device__ HitRecord trace_nearest_packet(const SceneView &S, float3 o, float3 d
         float tn;
         const bool need = active && slab(c.lo, c.hi, o, idir, kRayEps, closest, tn);
         for (int i = 0; i < c.count; ++i) {
-          const float4 *r = reinterpret_cast<const float4 *>(S.tris + c.child + i);
+          const float4 *r = tri_record<kGeo>(S, c.child + i, wr.kz);
           const float4 a = __ldg(r), b = __ldg(r + 1), q = __ldg(r + 2);
           float t, u, v;
-          if (need && tri_hit<kGeo>(wr, d, o, a, b, q, t, u, v) && t < closest) {
+          if (need && tri_hit<kGeo>(wr, d, o, op, a, b, q, t, u, v) && t < closest) {
             closest = t;
             h.hit = 1; h.tri = c.child + i; h.t = t; h.u = u; h.v = v;
           }
@@ -606,6 +628,7 @@ DVS_SHADE_INLINE __device__ bool trace_shadow_packet(const SceneView &S, float3 
                                                      int *stack_code, float *stack_t) {
   const float3 idir = inverse_direction(d);
   const WtRay wr = wt_ray<kGeo>(d);
+  const float3 op = wt_origin<kGeo>(wr, o);
   bool alive = active;
   bool occluded = false;
   const float t_max = 1e30f;
@@ -635,11 +658,11 @@ DVS_SHADE_INLINE __device__ bool trace_shadow_packet(const SceneView &S, float3 
       const bool need = alive && slab(c.lo, c.hi, o, idir, kRayEps, t_max, tn);
       for (int i = 0; i < c.count; ++i) {
         const int id = c.child + i;
-        const float4 *r = reinterpret_cast<const float4 *>(S.tris + id);
+        const float4 *r = tri_record<kGeo>(S, id, wr.kz);
         const float4 a = __ldg(r), b = __ldg(r + 1), q = __ldg(r + 2);
         float t, u, v;
         if (need && alive && id != self &&
-            tri_hit<kGeo>(wr, d, o, a, b, q, t, u, v) && t > kRayEps &&
+            tri_hit<kGeo>(wr, d, o, op, a, b, q, t, u, v) && t > kRayEps &&
             t < t_max) {
           occluded = true;
           alive = false;
@@ -746,7 +769,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
           normal = normalize(f3(s0.x, s0.y, s0.z) * w + f3(s1.x, s1.y, s1.z) * hit.u + f3(s2.x, s2.y, s2.z) * hit.v);
           lit = !(dot(normal, light) <= 0 || dot(normal, -ray) <= 0);
           if (lit) {
-            const float4 *r = reinterpret_cast<const float4 *>(S.tris + hit.tri);
+            const float4 *r = tri_record<kGeo>(S, hit.tri, 2);
             const float4 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2);
             sorigin = shadow_origin_rec<kGeo>(a, b, c, hit.u, hit.v, light);
             if (S.has_albedo) {
@@ -913,13 +936,14 @@ __device__ __forceinline__ float lane_reach(const bool (&active)[R], const float
 template <int R, int kGeo>
 __device__ void trace_nearest_packet_r(const SceneView &S, const float3 (&o)[R], const float3 (&d)[R],
                                        const bool (&active)[R], int *stack_code, float *stack_t, HitRecord (&h)[R]) {
-  float3 idir[R];
+  float3 idir[R], op[R];
   float closest[R];
   WtRay wr[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     idir[r] = inverse_direction(d[r]);
     wr[r] = wt_ray<kGeo>(d[r]);
+    op[r] = wt_origin<kGeo>(wr[r], o[r]);
     closest[r] = active[r] ? 1e30f : -1.0f;
     h[r] = HitRecord{0, -1, 0.f, 0.f, 0.f};
   }
@@ -951,12 +975,24 @@ __device__ void trace_nearest_packet_r(const SceneView &S, const float3 (&o)[R],
           need[r] = active[r] && slab(c.lo, c.hi, o[r], idir[r], kRayEps, closest[r], tn);
         }
         for (int i = 0; i < c.count; ++i) {
-          const float4 *q4 = reinterpret_cast<const float4 *>(S.tris + c.child + i);
-          const float4 a = __ldg(q4), b = __ldg(q4 + 1), q = __ldg(q4 + 2);
+          // one record per lane for all its rays; a ray of another dominant
+          // axis (watertight scenes, rare inside a lane) reads its own copy
+          const float4 *q4 = tri_record<kGeo>(S, c.child + i, wr[0].kz);
+          float4 a = __ldg(q4), b = __ldg(q4 + 1), q = __ldg(q4 + 2);
+          int loaded = wr[0].kz;
 #pragma unroll
           for (int r = 0; r < R; ++r) {
+            if constexpr ((kGeo & kGeoWatertight) != 0) {
+              if (wr[r].kz != loaded) {
+                const float4 *p4 = tri_record<kGeo>(S, c.child + i, wr[r].kz);
+                a = __ldg(p4);
+                b = __ldg(p4 + 1);
+                q = __ldg(p4 + 2);
+                loaded = wr[r].kz;
+              }
+            }
             float t, u, v;
-            if (need[r] && tri_hit<kGeo>(wr[r], d[r], o[r], a, b, q, t, u, v) && t < closest[r]) {
+            if (need[r] && tri_hit<kGeo>(wr[r], d[r], o[r], op[r], a, b, q, t, u, v) && t < closest[r]) {
               closest[r] = t;
               h[r].hit = 1; h[r].tri = c.child + i; h[r].t = t; h[r].u = u; h[r].v = v;
             }
@@ -981,7 +1017,7 @@ __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], 
                                       const int (&self)[R], int *stack_code, float *stack_t, bool (&occluded)[R]) {
   const float3 idir1 = inverse_direction(light);
   const WtRay wr = wt_ray<kGeo>(light);
-  float3 d[R], idir[R];
+  float3 d[R], idir[R], op[R];
   bool alive[R];
   float reach[R];
   const float t_max = 1e30f;
@@ -989,6 +1025,7 @@ __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], 
   for (int r = 0; r < R; ++r) {
     d[r] = light;
     idir[r] = idir1;
+    op[r] = wt_origin<kGeo>(wr, o[r]);
     alive[r] = active[r];
     occluded[r] = false;
   }
@@ -1026,12 +1063,12 @@ __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], 
       }
       for (int i = 0; i < c.count; ++i) {
         const int id = c.child + i;
-        const float4 *q4 = reinterpret_cast<const float4 *>(S.tris + id);
+        const float4 *q4 = tri_record<kGeo>(S, id, wr.kz);
         const float4 a = __ldg(q4), b = __ldg(q4 + 1), q = __ldg(q4 + 2);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           float t, u, v;
-          if (need[r] && alive[r] && id != self[r] && tri_hit<kGeo>(wr, light, o[r], a, b, q, t, u, v) &&
+          if (need[r] && alive[r] && id != self[r] && tri_hit<kGeo>(wr, light, o[r], op[r], a, b, q, t, u, v) &&
               t > kRayEps && t < t_max) {
             occluded[r] = true;
             alive[r] = false;
@@ -1106,7 +1143,7 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
                                 f3(s2.x, s2.y, s2.z) * hit[r].v);
           lit[r] = !(dot(normal[r], light) <= 0 || dot(normal[r], -ray[r]) <= 0);
           if (lit[r]) {
-            const float4 *t4 = reinterpret_cast<const float4 *>(S.tris + hit[r].tri);
+            const float4 *t4 = tri_record<kGeo>(S, hit[r].tri, 2);
             const float4 a = __ldg(t4), b = __ldg(t4 + 1), c = __ldg(t4 + 2);
             sorigin[r] = shadow_origin_rec<kGeo>(a, b, c, hit[r].u, hit[r].v, light);
             if (S.has_albedo) {
@@ -1202,7 +1239,7 @@ __device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const
                               f3(s2.x, s2.y, s2.z) * hit[r].v);
         lit[r] = !(dot(normal[r], light) <= 0 || dot(normal[r], -ray[r]) <= 0);
         if (lit[r]) {
-          const float4 *t4 = reinterpret_cast<const float4 *>(S.tris + hit[r].tri);
+          const float4 *t4 = tri_record<kGeo>(S, hit[r].tri, 2);
           const float4 a = __ldg(t4), b = __ldg(t4 + 1), c = __ldg(t4 + 2);
           sorigin[r] = shadow_origin_rec<kGeo>(a, b, c, hit[r].u, hit[r].v, light);
           if (S.has_albedo) {

@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(128, DVS_TRACE_PAIR_MIN_BLOCKS)
   const PixelSample s = sample_pixel_subrays<kMode, kGeo>(S, pixel, pose, s_code[wib], s_t[wib]);
   if (lane == 0) {
     const size_t o = (size_t)cell * n_pix + rank;
-    radiance[o] = s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll);
+    store_radiance(S, radiance, o, s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll));
     if (depth_out) depth_out[o] = s.depth;
     if (counters) {
       atomicAdd(counters + kCntPrimary, (unsigned long long)s.primary);
@@ -234,9 +234,34 @@ __global__ void blur_accumulate_kernel(int n, int n_poses, const int32_t *pixel_
   image[pixel_of_rank[k]] = acc;
 }
 
+// Photon counts as the circuit kernels draw them, one per thread: generator 0
+// is the reference's stream -- curand_init(seed, i, 0) and poisson_electrons,
+// as the counts kernel of tests/test_sensor.cu:17-20 -- and generator 1 the
+// precision mode's Philox stream of pixel i at the cell starting at cell_t0.
+__global__ void poisson_draws_kernel(int generator, double lambda, unsigned seed, int n, double cell_t0,
+                                     double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (generator == 0) {
+    curandStateXORWOW_t rng;
+    curand_init(seed, i, 0, &rng);
+    out[i] = poisson_electrons(rng, lambda);
+  } else {
+    curandStatePhilox4_32_10_t ph = philox_at(seed, i, cell_t0);
+    out[i] = poisson_electrons_philox(ph, (float)lambda);
+  }
+}
+
 inline int blocks(long long threads, int per_block) { return (int)((threads + per_block - 1) / per_block); }
 
 }  // namespace
+
+cudaError_t launch_poisson_draws(int generator, double lambda, unsigned seed, int n, double cell_t0, double *out,
+                                 cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  poisson_draws_kernel<<<blocks(n, 128), 128, 0, s>>>(generator, lambda, seed, n, cell_t0, out);
+  return cudaGetLastError();
+}
 
 // ---- launchers ----------------------------------------------------------------------
 cudaError_t launch_pose_from_state(const dvs_optical_state *state, CellPose *out, cudaStream_t s) {
@@ -395,6 +420,38 @@ cudaError_t launch_event_depth(const SceneView &scene, const dvs_optical_interva
       event_depth_kernel<kGeoReference><<<sms * 4, 128, 0, s>>>(scene, ivs, n_ivs, events, count, error, counters);
   }
   return cudaGetLastError();
+}
+
+namespace {
+template <int kGeo>
+cudaError_t preload_camera_geo() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, trace_subray_kernel<kRadianceDepth, kGeo>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, trace_subray_kernel<kRadiance, kGeo>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, trace_cells_kernel<kRadianceDepth, 1, kGeo>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, trace_cells_kernel<kRadianceDepth, 2, kGeo>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, trace_cells_kernel<kRadiance, 1, kGeo>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, trace_cells_kernel<kRadiance, 2, kGeo>);
+  if constexpr (kGeo == kGeoReference) {
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, trace_cells_kernel<kRadianceDepth, 4, kGeo>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, trace_cells_kernel<kRadiance, 4, kGeo>);
+  }
+  return e;
+}
+}  // namespace
+
+cudaError_t preload_camera_kernels(int geometry) {
+  // cudaFuncGetAttributes loads a kernel that lazy module loading has not
+  // loaded yet, so a later launch of it allocates nothing
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, radiance_to_float_kernel);
+  if (e != cudaSuccess) return e;
+  switch (geometry) {
+    case kGeoHalfBounds: return preload_camera_geo<kGeoHalfBounds>();
+    case kGeoWatertight: return preload_camera_geo<kGeoWatertight>();
+    case kGeoHalfBounds | kGeoWatertight: return preload_camera_geo<kGeoHalfBounds | kGeoWatertight>();
+    default: return preload_camera_geo<kGeoReference>();
+  }
 }
 
 cudaError_t launch_radiance_to_float(int n, const int32_t *pixel_of_rank, const double *radiance, const float *depth,

@@ -20,6 +20,7 @@ struct SceneView {
   float coherent_span;  // largest origin spread a warp packet traverses as one interval bundle
   dvs_hapke hapke;
   int32_t rays;         // sub-rays a lane may carry: 1, 2 or 4 (used when samples^2 is a multiple)
+  int32_t radiance_f32; // 1: the radiance chunk is written as float (read by an FP32 circuit), 0: as double
 };
 
 // Camera state at one circuit-cell midpoint, already interpolated
@@ -46,6 +47,7 @@ struct PhotoParams {
   int32_t fp32_circuit;  // receptor/contrast arithmetic in FP32 (times and crossing solves stay FP64)
   int32_t philox;        // counter-based Philox noise keyed by (seed, pixel, cell index) instead of XORWOW
   uint32_t seed;
+  int32_t chunk_f32;     // the circuit reads a float radiance chunk (FP32 circuits: the values it uses are floats)
 };
 
 // Pixel-circuit state, structure of arrays indexed by Morton rank.
@@ -189,6 +191,14 @@ cudaError_t launch_advance_probes(int n_probes, const int32_t *probe_ranks, cons
                                   const double *light, const OpticalKnot *knots, const int32_t *knot_counts,
                                   int capacity, double start, double end, PhotoParams photo, double charge,
                                   double *probe_state, cudaStream_t s);
+// n photon counts of mean lambda: generator 0 = XORWOW (curand_init(seed, i, 0),
+// poisson_electrons), 1 = Philox of pixel i at cell start cell_t0.
+cudaError_t launch_poisson_draws(int generator, double lambda, unsigned seed, int n, double cell_t0, double *out,
+                                 cudaStream_t s);
+// Loads (without launching) every kernel a one-pose camera render of a scene
+// with this geometry may launch: the kernels of launch_trace_cells with one
+// cell and launch_radiance_to_float.
+cudaError_t preload_camera_kernels(int geometry);
 cudaError_t launch_radiance_to_float(int n_pix, const int32_t *pixel_of_rank, const double *radiance,
                                      const float *depth, float *image, float *depth_image, cudaStream_t s);
 

@@ -15,6 +15,9 @@
 // process exits.  It is shared by all calls, so calls that overlap on the
 // GPU (different streams or threads at the same time) race on it.  Each call
 // overwrites all of it that it reads, so nothing needs clearing between calls.
+// Creating the scene does the per-device set-up (dvsgb_noalloc_prepare):
+// it looks up the array's device address with cudaGetSymbolAddress and loads
+// the render's kernels, so the render itself loads and reserves nothing.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -35,12 +38,15 @@ namespace {
 constexpr size_t kNoAllocMaxPixels = 1280 * 720;
 constexpr size_t kPoseBytes = 256;
 constexpr size_t kScratchBytes = kPoseBytes + kNoAllocMaxPixels * (sizeof(double) + sizeof(float));
+// layout: the pose, then the FP64 radiance (8-byte aligned), then the depth
+static_assert(sizeof(CellPose) <= kPoseBytes && kPoseBytes % alignof(double) == 0, "no-allocation scratch layout");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 128;
 std::mutex g_setup_mutex;
 void *g_scratch_address[kMaxDevices] = {};  // device address of g_noalloc_scratch, per device
+bool g_kernels_loaded[kMaxDevices][4] = {};  // camera kernels loaded, per device and scene geometry
 
 __device__ __forceinline__ float3 normalize3(float3 v) {
   float len = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
@@ -76,6 +82,31 @@ int scratch_for_device(int device, unsigned char **out) {
 }
 
 }  // namespace
+
+// Set-up of the no-allocation render, called by dvs_scene_create and
+// dvs_scene_view_create with the scene's device current.  Under CUDA's lazy
+// module loading the first use of a module or kernel is what loads it, and
+// loading the module that holds the static array reserves the array's device
+// memory.  Doing that here, where the caller is creating a scene and may
+// allocate, leaves nothing to load or reserve in the render itself: the
+// array's address is looked up and every kernel the render launches for
+// this geometry is loaded.
+int dvsgb_noalloc_prepare(int device, int geometry) {
+  unsigned char *base = nullptr;
+  int status = scratch_for_device(device, &base);
+  if (status != DVS_OK) return status;
+  const int g = geometry & 3;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (g_kernels_loaded[device][g]) return DVS_OK;
+  cudaFuncAttributes attr;
+  cudaError_t e = cudaFuncGetAttributes(&attr, noalloc_pose_kernel);
+  if (e == cudaSuccess) e = preload_camera_kernels(g);
+  if (e != cudaSuccess)
+    return dvsgb_set_error(DVS_ERR_CUDA, (std::string("[CUDA Error] in no-allocation kernel set-up : ") +
+                                          cudaGetErrorString(e)).c_str());
+  g_kernels_loaded[device][g] = true;
+  return DVS_OK;
+}
 
 extern "C" int dvs_cam_render_noalloc(dvs_scene *scene, const dvs_optical_state *pose, float *radiance, float *depth,
                                       void *stream) {

@@ -16,6 +16,13 @@ constexpr int kWarpsPerBlock = 4;  // all ray kernels launch 128 threads
 #define DVS_TRACE_MIN_BLOCKS 5
 #endif
 constexpr int kCos4Table = 256;    // sub-rays per pixel with a shared cos^4 table (ss <= 16)
+
+// Element o of a radiance chunk: double, or float when the chunk feeds an
+// FP32 circuit (which uses the value as a float: the same bits, half the bytes).
+__device__ __forceinline__ void store_radiance(const SceneView &S, double *chunk, size_t o, double value) {
+  if (S.radiance_f32) reinterpret_cast<float *>(chunk)[o] = (float)value;
+  else chunk[o] = value;
+}
 // Several sub-rays per lane (SceneView::rays: 1, 2 or 4, when the pixel's
 // sub-ray count is a multiple): the kernels with more ray state per lane are
 // compiled for fewer resident blocks (more registers).
@@ -62,7 +69,7 @@ __device__ __forceinline__ void trace_cells_item(const SceneView &S, int n_pix, 
                                                    shared_cos4 ? cos4 : nullptr);
   if (active) {
     const size_t o = (size_t)cell * n_pix + rank;
-    radiance[o] = s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll);
+    store_radiance(S, radiance, o, s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll));
     if (depth_out) depth_out[o] = s.depth;
   }
   const unsigned prim = warp_sum(s.primary), shad = warp_sum(s.shadow);
@@ -117,11 +124,13 @@ __device__ __forceinline__ void circuit_rank(int r, int n, const int32_t *rank_l
                  (float)st.threshold_pos[k], (float)st.threshold_neg[k], st.reset_pending[k] != 0};
     const int pixel = kPhilox ? st.pixel[k] : 0;
     const float e_rad = (float)photo.electrons_per_radiance, dark = (float)photo.dark_electrons;
+    const float *chunk_f = photo.chunk_f32 ? reinterpret_cast<const float *>(radiance) : nullptr;
     for (int c = 0; c < nc; ++c) {
       const Cell cell = cells[c0 + c];
-      const double rad = radiance[(size_t)c * n + r];
+      const size_t o = (size_t)c * n + r;
+      const float rad = chunk_f ? chunk_f[o] : (float)radiance[o];
       if (!isfinite(rad)) { failed = kErrOptical; break; }
-      float rate = (float)rad * e_rad + dark;
+      float rate = rad * e_rad + dark;
       const float dt = (float)(cell.t1 - cell.t0);
       int emitted;
       if (kPhilox) {

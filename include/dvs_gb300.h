@@ -165,6 +165,14 @@ void dvs_sensor_options_default(dvs_sensor_options *out);
  * charge_scale, refractory_time, reference_leak, reset_noise_std;
  * out[6..8] = electrons_per_radiance, dark_electrons, integration_step. */
 int dvs_derive_parameters(const dvs_physic *physic, int32_t physic_effects, double *out9);
+/* n photon counts of mean `lambda` into the host array `out`, drawn on the
+ * device exactly as the circuit kernels draw them -- for distribution checks.
+ * generator 0: the reference's stream, draw i from curand_init(seed, i, 0) and
+ * poisson_electrons (include/dvs/photon_noise.cuh:4-9; the counts kernel of
+ * tests/test_sensor.cu:17-20); generator 1: the precision mode's Philox stream
+ * of pixel i for a cell starting at t = 0 (inversion below 10, Hormann's PTRS
+ * up to 1e6, rounded normal above).  n <= 2^28. */
+int dvs_noise_poisson(int32_t generator, double lambda, uint32_t seed, size_t n, double *out);
 
 /* ---- scene: replaces BVHBuilder::build + DeviceScene (src/bvh/build.cpp:27-76,
  *      src/cuda/device_scene.cu:15-37) ----------------------------------------- */
@@ -202,17 +210,19 @@ int dvs_cam_render(dvs_scene *scene, const dvs_optical_state *pose, float *radia
  * Intermediates live in one library-owned static device array sized for at
  * most 1280x720 pixels (about 11 MB, held on every GPU that loads the library
  * until the process exits); larger images are rejected with DVS_ERR_INVALID.
- * The first call on a device looks up that array's device address (once per
- * device), so make that first call before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race on it. */
+ * The per-device set-up -- looking up that array's device address and loading
+ * the render's kernels, which under lazy module loading is what reserves the
+ * array -- is done by dvs_scene_create / dvs_scene_view_create on the scene's
+ * device, so the render itself neither allocates nor loads anything.  All
+ * calls share the array: calls that overlap on the GPU race on it. */
+int dvs_cam_render_noalloc(dvs_scene *scene, const dvs_optical_state *pose, float *radiance, float *depth,
+                           void *stream);
 /* Motion-blur exposure (apps/main_cam_blur.cpp:64-77): the image
  * sum_j weights[j] * radiance(poses[j]), accumulated in float in pose order,
  * row-major, n_poses sub-exposure poses traced in one launch (the pose_count
  * form of OpticalSampler::evaluate, src/cuda/optical_sampler.cu:154-168). */
 int dvs_cam_render_blur(dvs_scene *scene, const dvs_optical_state *poses, const float *weights, size_t n_poses,
                         float *image);
-int dvs_cam_render_noalloc(dvs_scene *scene, const dvs_optical_state *pose, float *radiance, float *depth,
-                           void *stream);
 
 /* ---- event sensor: replaces EventSensor (src/cuda/event_sensor.cu:244-305) ---- */
 int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sensor_options *options,
@@ -274,7 +284,10 @@ int dvs_sensor_stats_reset(dvs_sensor *sensor);
  * must share one scene geometry (dvs_scene_view_create views of one scene), device
  * and circuit_precision, and must be initialized; their events are read with
  * dvs_sensor_read as after dvs_sensor_process, and are the same as when each member
- * is processed alone.  A member may not be used outside the batch during a step. */
+ * is processed alone.  A member may not be used outside the batch during a step, and
+ * a member with an uncollected dvs_sensor_enqueue is refused (DVS_ERR_INVALID) until
+ * it is collected.  The batch keeps the members' handles without owning them: every
+ * member (and its scene) must outlive the batch -- destroy the batch first. */
 typedef struct dvs_batch dvs_batch;
 typedef struct {
   uint64_t steps, graph_launches, graph_captures, persistent_launches;

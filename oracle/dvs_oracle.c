@@ -650,14 +650,15 @@ int oracle_trace_shadow(const oscene *s, const float *o, const float *d, int sel
   return trace_shadow_r(s, mk(o[0], o[1], o[2]), mk(d[0], d[1], d[2]), self, kRayEps, R(1e30));
 }
 
-/* shadow_origin (device_optics.cuh:37-51). */
-static rv3 shadow_origin_r(const oscene *s, int tri_id, real u, real v, rv3 light) {
+/* shadow_origin (device_optics.cuh:37-51); epsilon: the unit roundoff of its
+ * error bound (the arithmetic's own: 2^-24 in FP32, 2^-53 in FP64). */
+static rv3 shadow_origin_eps(const oscene *s, int tri_id, real u, real v, rv3 light, real epsilon) {
   const uint32_t *tri = &s->indices[3 * (size_t)tri_id];
   rv3 a = vtx(s, tri[0]), e1 = sub3(vtx(s, tri[1]), a), e2 = sub3(vtx(s, tri[2]), a);
   rv3 point = add3(add3(a, scale3(u, e1)), scale3(v, e2));
   rv3 normal = normalize3(cross3(e1, e2));
   if (dot3(normal, light) < 0) normal = neg3(normal);
-  const real epsilon = REAL_EPS_HALF, gamma = 8 * epsilon / (1 - 8 * epsilon);
+  const real gamma = 8 * epsilon / (1 - 8 * epsilon);
   rv3 error = mk(gamma * (fabs(a.x) + fabs(u * e1.x) + fabs(v * e2.x)),
                  gamma * (fabs(a.y) + fabs(u * e1.y) + fabs(v * e2.y)),
                  gamma * (fabs(a.z) + fabs(u * e1.z) + fabs(v * e2.z)));
@@ -670,6 +671,9 @@ static rv3 shadow_origin_r(const oscene *s, int tri_id, real u, real v, rv3 ligh
   if (offset.z != 0) point.z = nextafter(point.z, copysign(inf, offset.z));
   return point;
 }
+static rv3 shadow_origin_r(const oscene *s, int tri_id, real u, real v, rv3 light) {
+  return shadow_origin_eps(s, tri_id, u, v, light, REAL_EPS_HALF);
+}
 void oracle_shadow_origin(const oscene *s, int tri, float u, float v, const float *light, float *out) {
   rv3 p = shadow_origin_r(s, tri, u, v, mk(light[0], light[1], light[2]));
   out[0] = (float)p.x; out[1] = (float)p.y; out[2] = (float)p.z;
@@ -679,46 +683,203 @@ static real material_albedo(real value, real fallback) { /* device_optics.cuh:30
   return isfinite(value) && value >= 0 && value <= 1 ? value : fallback;
 }
 
-/* sample_pixel (device_optics.cuh:73-94).  Counts the rays it traces. */
-static void sample_pixel_r(const oscene *s, int pixel, const ostate *pose, double *radiance_out,
-                           float *depth_out, int *valid_out, uint64_t *n_primary, uint64_t *n_shadow) {
+/* Whether a lit sample can sit at Hapke's azimuth singularity in FP32: the
+ * clamped ratio cos psi of hapke.hpp:96,123, evaluated in float arithmetic
+ * from the sample's cosines moved by up to +-3e-7 (their FP32 error), reaches
+ * -1 at a corner of that box.  There the reference's FP32 formula yields NaN
+ * and the sample is dropped, while the FP64 value is finite; near-normal
+ * views (sin e -> 0) make the ratio ill-conditioned. */
+static int hapke_azimuth_singular(rv3 normal, rv3 light, rv3 view) {
+  const rv3 n = normalize3(normal), l = normalize3(light), v = normalize3(view);
+  const double ci = (double)dot3(n, l), ce = (double)dot3(n, v), cg = (double)dot3(l, v);
+  for (int k = 0; k < 8; ++k) {
+    float fi = (float)(ci + ((k & 1) ? 3e-7 : -3e-7)), fe = (float)(ce + ((k & 2) ? 3e-7 : -3e-7));
+    float fg = (float)(cg + ((k & 4) ? 3e-7 : -3e-7));
+    if (fi <= 0.0f || fe <= 0.0f) continue;
+    fi = fminf(fmaxf(fi, 0.0f), 1.0f);
+    fe = fminf(fmaxf(fe, 0.0f), 1.0f);
+    fg = fminf(fmaxf(fg, -1.0f), 1.0f);
+    const float si = sqrtf(fmaxf(0.0f, 1.0f - fi * fi)), se = sqrtf(fmaxf(0.0f, 1.0f - fe * fe));
+    const float c = fminf(fmaxf((fg - fi * fe) / (si * se + 1e-6f), -1.0f), 1.0f);
+    if (c <= -1.0f) return 1;
+  }
+  return 0;
+}
+
+/* One sub-ray of sample_pixel (device_optics.cuh:76-92): nearest hit,
+ * shading test, shadow ray and Hapke term.  status: 1 hit, 0 miss, -1 stack
+ * overflow; term: the sub-ray's radiance term (0 when unlit or shadowed);
+ * cos4 is the sub-ray's field falloff. */
+typedef struct { int status; real t; double term; int singular, crack; } osubray;
+
+/* Whether a Moller-Trumbore hit lies within the FP32 rounding of its
+ * barycentrics of an edge of the triangle: there an FP32 test of the same ray
+ * can pass between this triangle and its neighbour across the edge (the test
+ * is not watertight) and hit what lies behind.  The bound on each barycentric
+ * is 16 * 2^-24 times the magnitudes of the dot product that forms it
+ * (device_ray.hpp:62-75 operation order) over |det|. */
+static int mt_crack(const oscene *s, rv3 o, rv3 d, int tri_id) {
+  const uint32_t *tri = &s->indices[3 * (size_t)tri_id];
+  const double u32 = 16 * 5.960464477539063e-8;
+  const double v0[3] = {s->vertices[tri[0]].x, s->vertices[tri[0]].y, s->vertices[tri[0]].z};
+  const double v1[3] = {s->vertices[tri[1]].x, s->vertices[tri[1]].y, s->vertices[tri[1]].z};
+  const double v2[3] = {s->vertices[tri[2]].x, s->vertices[tri[2]].y, s->vertices[tri[2]].z};
+  const double dd[3] = {d.x, d.y, d.z}, oo[3] = {o.x, o.y, o.z};
+  double e1[3], e2[3], tv[3];
+  for (int k = 0; k < 3; ++k) { e1[k] = v1[k] - v0[k]; e2[k] = v2[k] - v0[k]; tv[k] = oo[k] - v0[k]; }
+  const double pv[3] = {dd[1] * e2[2] - dd[2] * e2[1], dd[2] * e2[0] - dd[0] * e2[2], dd[0] * e2[1] - dd[1] * e2[0]};
+  const double qv[3] = {tv[1] * e1[2] - tv[2] * e1[1], tv[2] * e1[0] - tv[0] * e1[2], tv[0] * e1[1] - tv[1] * e1[0]};
+  const double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
+  if (det == 0) return 1;
+  const double u = (tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2]) / det;
+  const double v = (dd[0] * qv[0] + dd[1] * qv[1] + dd[2] * qv[2]) / det;
+  const double bu = u32 * (fabs(tv[0] * pv[0]) + fabs(tv[1] * pv[1]) + fabs(tv[2] * pv[2])) / fabs(det);
+  const double bv = u32 * (fabs(dd[0] * qv[0]) + fabs(dd[1] * qv[1]) + fabs(dd[2] * qv[2])) / fabs(det);
+  return u < bu || v < bv || 1.0 - u - v < bu + bv;
+}
+static osubray subray_eps(const oscene *s, const ostate *pose, rv3 position, rv3 light, rv3 ray, double cos4,
+                          uint64_t *n_primary, uint64_t *n_shadow, real offset_eps) {
+  osubray o = {0, R(0.0), 0.0, 0, 0};
+  const real w_default = (real)s->hapke.w;
+  ++*n_primary;
+  rhit hit = trace_nearest_r(s, position, ray);
+  o.status = hit.hit;
+  if (hit.hit != 1) return o;
+  o.t = hit.t;
+  if (!s->watertight) o.crack = mt_crack(s, position, ray, hit.tri);
+  const uint32_t *tri = &s->indices[3 * (size_t)hit.tri];
+  real w = R(1.0) - hit.u - hit.v;
+  rv3 n0 = from_f3(s->normals[tri[0]]), n1 = from_f3(s->normals[tri[1]]), n2 = from_f3(s->normals[tri[2]]);
+  rv3 normal = normalize3(add3(add3(scale3(w, n0), scale3(hit.u, n1)), scale3(hit.v, n2)));
+  if (dot3(normal, light) <= 0 || dot3(normal, neg3(ray)) <= 0) return o;
+  rv3 origin = shadow_origin_eps(s, hit.tri, hit.u, hit.v, light, offset_eps);
+  ++*n_shadow;
+  if (trace_shadow_r(s, origin, light, hit.tri, kRayEps, R(1e30))) return o;
+  real albedo = s->albedos ? material_albedo(s->albedos[tri[0]], w_default) * w +
+                                 material_albedo(s->albedos[tri[1]], w_default) * hit.u +
+                                 material_albedo(s->albedos[tri[2]], w_default) * hit.v
+                           : w_default;
+  o.term = fmax(R(0.0), hapke_directional_r(normal, light, neg3(ray), albedo, &s->hapke) *
+                            (real)pose->intensity) * cos4;
+  o.singular = hapke_azimuth_singular(normal, light, neg3(ray));
+  return o;
+}
+static osubray subray_r(const oscene *s, const ostate *pose, rv3 position, rv3 light, rv3 ray, double cos4,
+                        uint64_t *n_primary, uint64_t *n_shadow) {
+  return subray_eps(s, pose, position, light, ray, cos4, n_primary, n_shadow, REAL_EPS_HALF);
+}
+
+/* ---- margin classification (test infrastructure; no reference counterpart) --
+ * A sub-ray is a margin sub-ray when its outcome is discontinuous within the
+ * rounding of an FP32 evaluation: re-traced with its image-plane direction
+ * moved by +-eta in x and in y (eta a few times the FP32 error of a ray
+ * direction), one of the four re-traces changes its hit status, its hit
+ * distance by more than 1e-3 (a silhouette), or its radiance term by more
+ * than 1e-3 of the larger term (a shadow or terminator boundary); or its
+ * shadow ray, started from the shadow origin that the FP32 form of
+ * shadow_origin's error bound gives (epsilon 2^-24: an offset off the surface
+ * hundreds of times the FP64 one), changes the term likewise.  Smooth
+ * changes -- crossing the shared edge of two triangles of one surface, the
+ * shading gradient -- stay far below those jumps.  A pixel with a margin
+ * sub-ray is a margin pixel.  g_margin_eta == 0 turns the test off. */
+static double g_margin_eta = 0.0, g_margin_eta_c = 2.384185791015625e-7; /* 4 * 2^-24 */
+static double g_margin_cond_tol = 1e-5;
+void oracle_set_margin_eta(double eta) { g_margin_eta = eta > 0 ? eta : 0.0; }
+void oracle_set_conditioning(double eta_c, double tolerance) {
+  g_margin_eta_c = eta_c > 0 ? eta_c : 0.0;
+  g_margin_cond_tol = tolerance > 0 ? tolerance : 1e-5;
+}
+static int subray_jumps(const osubray *a, const osubray *b) {
+  if (a->status != b->status) return 1;
+  if (a->status == 1 && fabs((double)b->t - (double)a->t) > 1e-3 * fabs((double)a->t)) return 1;
+  const double big = fmax(a->term, b->term);
+  return big > 0 && fabs(a->term - b->term) > 1e-3 * big;
+}
+
+/* sample_pixel (device_optics.cuh:73-94), every sub-ray moved by (dx, dy)
+ * in the image plane (0, 0: the pixel itself).  Counts the rays it traces.
+ * With margin != NULL and the margin test on, *margin |= 1 for a sub-ray
+ * that jumps (subray_jumps) or sits at Hapke's azimuth singularity. */
+static void sample_pixel_shifted(const oscene *s, int pixel, const ostate *pose, real dx, real dy,
+                                 double *radiance_out, float *depth_out, int *valid_out, uint64_t *n_primary,
+                                 uint64_t *n_shadow, uint8_t *margin) {
   double radiance = 0, depth = 0;
   int valid_depth = 0;
   const rv3 light = normalize3(from_f3(pose->light));
   const rv3 position = from_f3(pose->position);
   const int ss = s->samples;
-  const real w_default = (real)s->hapke.w;
+  const real eta = (real)g_margin_eta;
   for (int sy = 0; sy < ss; ++sy)
     for (int sx = 0; sx < ss; ++sx) {
       real px = ((real)(pixel % s->width) + (sx + R(.5)) / (real)ss - R(.5) - (real)s->cx) / (real)s->fx;
       real py = ((real)(pixel / s->width) + (sy + R(.5)) / (real)ss - R(.5) - (real)s->cy) / (real)s->fy;
+      px += dx;
+      py += dy;
       rv3 ray = normalize3(rotate_ray(pose->rotation, mk(px, -py, R(-1.0))));
-      ++*n_primary;
-      rhit hit = trace_nearest_r(s, position, ray);
-      if (hit.hit < 0) { *radiance_out = 0; *depth_out = -1; *valid_out = 0; return; }
-      if (hit.hit == 0) continue;
-      depth += hit.t;
+      const double cos4 = 1.0 / ((1.0 + px * px + py * py) * (1.0 + px * px + py * py));
+      const osubray o = subray_r(s, pose, position, light, ray, cos4, n_primary, n_shadow);
+      if (o.status < 0) { *radiance_out = 0; *depth_out = -1; *valid_out = 0; return; }
+      if (margin && eta > 0 && o.crack) *margin |= 16;
+      if (margin && eta > 0 && !(*margin & 1)) {
+        if (o.singular) *margin |= 1;
+        for (int k = 0; k < 4 && !(*margin & 1); ++k) {
+          const real qx = px + (k == 0 ? eta : (k == 1 ? -eta : R(0.0)));
+          const real qy = py + (k == 2 ? eta : (k == 3 ? -eta : R(0.0)));
+          const rv3 moved = normalize3(rotate_ray(pose->rotation, mk(qx, -qy, R(-1.0))));
+          uint64_t a = 0, b = 0;
+          const osubray p = subray_r(s, pose, position, light, moved, cos4, &a, &b);
+          if (subray_jumps(&o, &p)) *margin |= 1;
+        }
+        if (!(*margin & 1) && REAL_EPS_HALF != 5.960464477539063e-8) {
+          uint64_t a = 0, b = 0;
+          const osubray p = subray_eps(s, pose, position, light, ray, cos4, &a, &b, (real)5.960464477539063e-8);
+          if (subray_jumps(&o, &p)) *margin |= 1;
+        }
+      }
+      if (o.status == 0) continue;
+      depth += o.t;
       ++valid_depth;
-      const uint32_t *tri = &s->indices[3 * (size_t)hit.tri];
-      real w = R(1.0) - hit.u - hit.v;
-      rv3 n0 = from_f3(s->normals[tri[0]]), n1 = from_f3(s->normals[tri[1]]), n2 = from_f3(s->normals[tri[2]]);
-      rv3 normal = normalize3(add3(add3(scale3(w, n0), scale3(hit.u, n1)), scale3(hit.v, n2)));
-      if (dot3(normal, light) <= 0 || dot3(normal, neg3(ray)) <= 0) continue;
-      rv3 origin = shadow_origin_r(s, hit.tri, hit.u, hit.v, light);
-      ++*n_shadow;
-      if (trace_shadow_r(s, origin, light, hit.tri, kRayEps, R(1e30))) continue;
-      real albedo = s->albedos ? material_albedo(s->albedos[tri[0]], w_default) * w +
-                                     material_albedo(s->albedos[tri[1]], w_default) * hit.u +
-                                     material_albedo(s->albedos[tri[2]], w_default) * hit.v
-                               : w_default;
-      double cos4 = 1.0 / ((1.0 + px * px + py * py) * (1.0 + px * px + py * py));
-      radiance += fmax(R(0.0), hapke_directional_r(normal, light, neg3(ray), albedo, &s->hapke) *
-                                   (real)pose->intensity) * cos4;
+      radiance += o.term;
     }
   radiance /= ss * ss;
   *radiance_out = radiance;
   *depth_out = valid_depth ? (float)(depth / valid_depth) : -1.0f;
   *valid_out = 1;
+}
+static void sample_pixel_m(const oscene *s, int pixel, const ostate *pose, double *radiance_out,
+                           float *depth_out, int *valid_out, uint64_t *n_primary, uint64_t *n_shadow,
+                           uint8_t *margin) {
+  sample_pixel_shifted(s, pixel, pose, R(0.0), R(0.0), radiance_out, depth_out, valid_out, n_primary, n_shadow,
+                       margin);
+}
+static void sample_pixel_r(const oscene *s, int pixel, const ostate *pose, double *radiance_out,
+                           float *depth_out, int *valid_out, uint64_t *n_primary, uint64_t *n_shadow) {
+  sample_pixel_m(s, pixel, pose, radiance_out, depth_out, valid_out, n_primary, n_shadow, NULL);
+}
+
+/* Conditioning class of a pixel: its radiance or depth, as this oracle
+ * computes them, moves by more than `tolerance` (relative) when every
+ * sub-ray is moved by +-eta_c in x or in y, eta_c about the FP32 error of a
+ * ray direction.  Such a pixel's value is not fixed to the tolerance by a
+ * float ray at all (grazing incidence with varying vertex normals, a shadow
+ * edge or silhouette inside the pixel).  Returns 8 for a conditioning pixel. */
+static uint8_t pixel_conditioning(const oscene *s, int pixel, const ostate *pose, double radiance, float depth,
+                                  double eta_c, double tolerance) {
+  for (int k = 0; k < 4; ++k) {
+    const real dx = (real)(k == 0 ? eta_c : (k == 1 ? -eta_c : 0.0));
+    const real dy = (real)(k == 2 ? eta_c : (k == 3 ? -eta_c : 0.0));
+    double r;
+    float d;
+    int valid;
+    uint64_t a = 0, b = 0;
+    sample_pixel_shifted(s, pixel, pose, dx, dy, &r, &d, &valid, &a, &b, NULL);
+    if (!valid) return 8;
+    const double big = fmax(fabs(r), fabs(radiance));
+    if (big > 0 && fabs(r - radiance) > tolerance * big) return 8;
+    if ((d < 0) != (depth < 0)) return 8;
+    if (depth > 0 && fabs((double)d - (double)depth) > tolerance * (double)depth) return 8;
+  }
+  return 0;
 }
 
 void oracle_sample_pixel(const oscene *s, int pixel, const ostate *pose, double *radiance, float *depth,
@@ -764,6 +925,25 @@ void oracle_render_pixels(const oscene *s, const ostate *pose, const int32_t *pi
   }
   *primary_rays = prim;
   *shadow_rays = shad;
+}
+
+void oracle_render_pixels_margin(const oscene *s, const ostate *pose, const int32_t *pixels, int n,
+                                 double *radiance, float *depth, uint8_t *margin, int nthreads) {
+  const int nt = thread_count(nthreads);
+  (void)nt;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+  for (int i = 0; i < n; ++i) {
+    int valid;
+    uint64_t a = 0, b = 0;
+    margin[i] = 0;
+    sample_pixel_m(s, pixels[i], pose, &radiance[i], &depth[i], &valid, &a, &b, &margin[i]);
+    if (!valid) {
+      radiance[i] = NAN;
+      continue;
+    }
+    if (g_margin_eta > 0)
+      margin[i] |= pixel_conditioning(s, pixels[i], pose, radiance[i], depth[i], g_margin_eta_c, g_margin_cond_tol);
+  }
 }
 
 /* ---- BVH build (src/bvh/build.cpp, src/bvh/bining.cpp, include/bvh/common.h) */
@@ -1057,7 +1237,26 @@ struct osensor {
   opixel_state *states;
   oreadout *readout;
   uint64_t primary_rays, shadow_rays;
+  /* margin classification (oracle_sensor_set_margin): per pixel the flags
+   * (1 optical margin at a cell sample, 2 circuit margin, 4 optical margin of
+   * an event-time depth sample) and two shadow circuits with both thresholds
+   * moved by +shift and -shift, whose polarity sequences are compared with the
+   * circuit's own through a count and a running hash per circuit */
+  int classify;
+  double threshold_shift;
+  uint8_t *margin;
+  opixel_state *shifted;     /* 2 per pixel: +shift, -shift */
+  uint64_t *seq;             /* 3 per pixel: (count << 48) ^ hash of the polarity sequence */
 };
+
+static void seq_push(uint64_t *seq, const int32_t *pol, int n) {
+  uint64_t count = *seq >> 48, hash = *seq & 0xffffffffffffull;
+  for (int j = 0; j < n; ++j) {
+    hash = (hash * 3 + (uint64_t)(pol[j] + 1)) & 0xffffffffffffull;
+    ++count;
+  }
+  *seq = (count << 48) | hash;
+}
 
 osensor *oracle_sensor_create(const oscene *scene, const ophysic *c, int physic_effects, int aer_delay) {
   /* EventSensor::EventSensor (event_sensor.cu:244-260) */
@@ -1076,8 +1275,30 @@ osensor *oracle_sensor_create(const oscene *scene, const ophysic *c, int physic_
                                      (size_t)c->readout_queue_capacity);
   return s;
 }
+int oracle_sensor_set_margin(osensor *s, double threshold_shift) {
+  /* before initialize: the shadow circuits start from the same state */
+  if (s->initialized || !(threshold_shift > 0)) return 3;
+  const size_t n = (size_t)s->scene.width * s->scene.height;
+  s->classify = 1;
+  s->threshold_shift = threshold_shift;
+  s->margin = (uint8_t *)calloc(n, 1);
+  s->shifted = (opixel_state *)calloc(2 * n, sizeof(opixel_state));
+  s->seq = (uint64_t *)calloc(3 * n, sizeof(uint64_t));
+  return 0;
+}
+void oracle_sensor_margins(const osensor *s, uint8_t *out) {
+  const size_t n = (size_t)s->scene.width * s->scene.height;
+  for (size_t i = 0; i < n; ++i) {
+    uint8_t m = s->classify ? s->margin[i] : 0;
+    if (s->classify && (s->seq[3 * i] != s->seq[3 * i + 1] || s->seq[3 * i] != s->seq[3 * i + 2])) m |= 2;
+    out[i] = m;
+  }
+}
 void oracle_sensor_destroy(osensor *s) {
   if (!s) return;
+  free(s->margin);
+  free(s->shifted);
+  free(s->seq);
   free(s->states);
   oracle_readout_destroy(s->readout);
   free(s);
@@ -1098,7 +1319,7 @@ int oracle_sensor_initialize(osensor *s, const ostate *pose, double t, int nthre
     float depth;
     int valid;
     uint64_t a = 0, b = 0;
-    sample_pixel_r(&s->scene, i, pose, &rad, &depth, &valid, &a, &b);
+    sample_pixel_m(&s->scene, i, pose, &rad, &depth, &valid, &a, &b, s->classify ? &s->margin[i] : NULL);
     prim += a;
     shad += b;
     if (!valid || !isfinite(rad)) {
@@ -1115,6 +1336,15 @@ int oracle_sensor_initialize(osensor *s, const ostate *pose, double t, int nthre
     st.threshold_pos = fmax(s->threshold_min, s->params.threshold_pos + s->threshold_std * 0.0);
     st.threshold_neg = fmax(s->threshold_min, s->params.threshold_neg + s->threshold_std * 0.0);
     s->states[i] = st;
+    if (s->classify) {
+      opixel_state hi = st, lo = st;
+      hi.threshold_pos += s->threshold_shift;
+      hi.threshold_neg += s->threshold_shift;
+      lo.threshold_pos -= s->threshold_shift;
+      lo.threshold_neg -= s->threshold_shift;
+      s->shifted[2 * (size_t)i] = hi;
+      s->shifted[2 * (size_t)i + 1] = lo;
+    }
   }
   s->primary_rays += prim;
   s->shadow_rays += shad;
@@ -1155,6 +1385,7 @@ int oracle_sensor_process(osensor *s, const ointerval *ivs, int count, oevent *o
     int cnt = 0, failed = 0;
     uint64_t a = 0, b = 0;
     opixel_state st = s->states[i];
+    uint8_t *mark = s->classify ? &s->margin[i] : NULL;
     for (int k = 0; k < count && !failed; ++k) {
       const ointerval *iv = &ivs[k];
       int steps = (int)ceil((iv->t1 - iv->t0) / s->photo.integration_step);
@@ -1166,11 +1397,22 @@ int oracle_sensor_process(osensor *s, const ointerval *ivs, int count, oevent *o
         double rad;
         float depth;
         int valid;
-        sample_pixel_r(&s->scene, i, &pose, &rad, &depth, &valid, &a, &b);
+        sample_pixel_m(&s->scene, i, &pose, &rad, &depth, &valid, &a, &b, mark);
         if (!valid || !isfinite(rad)) { failed = 2; break; }
         double rate = rad * s->photo.electrons_per_radiance + s->photo.dark_electrons;
         int emitted = advance_pixel(&st, &s->params, rate, t0, t1, lt + cnt, lp + cnt, maxev - cnt);
         if (emitted < 0) { failed = 1; break; }
+        if (mark) {
+          /* the two shadow circuits see the same light */
+          seq_push(&s->seq[3 * (size_t)i], lp + cnt, emitted);
+          for (int v = 0; v < 2; ++v) {
+            double vt[64];
+            int32_t vp[64];
+            const int e = advance_pixel(&s->shifted[2 * (size_t)i + v], &s->params, rate, t0, t1, vt, vp, 64);
+            if (e < 0) *mark |= 2;
+            else seq_push(&s->seq[3 * (size_t)i + 1 + v], vp, e);
+          }
+        }
         cnt += emitted;
       }
     }
@@ -1184,8 +1426,10 @@ int oracle_sensor_process(osensor *s, const ointerval *ivs, int count, oevent *o
         double rad;
         float depth;
         int valid;
-        sample_pixel_r(&s->scene, i, &pose, &rad, &depth, &valid, &a, &b);
+        uint8_t depth_mark = 0;
+        sample_pixel_m(&s->scene, i, &pose, &rad, &depth, &valid, &a, &b, mark ? &depth_mark : NULL);
         if (!valid) { failed = 2; break; }
+        if (depth_mark) *mark |= 4;
         ev_d[(size_t)i * maxev + j] = depth;
       }
     }

@@ -187,6 +187,42 @@ void oracle_sensor_states(const osensor *s, opixel_state *out);
 size_t oracle_sensor_dropped(const osensor *s);
 uint64_t oracle_sensor_rays(const osensor *s, int shadow);
 
+/* ---- margin classification (no reference counterpart) -------------------
+ * The accuracy statement exempts two classes from exact agreement, and these
+ * calls name them instead of tolerating a fraction of differences:
+ *   optical margin: a sub-ray whose outcome jumps when its image-plane
+ *     direction moves by +-eta in x or y (eta several times the FP32 error of
+ *     a ray direction): hit status, hit distance beyond 1e-3 (silhouette) or
+ *     radiance term beyond 1e-3 (shadow / terminator boundary);
+ *   circuit margin: a pixel whose polarity sequence changes when both
+ *     thresholds move by +shift or by -shift (a log-intensity margin below
+ *     shift at some crossing or near-crossing).
+ *   conditioning (renders only): a pixel whose radiance or depth moves by
+ *     more than the tolerance (1e-5) when all its sub-rays move by
+ *     +-eta_c in x or y, eta_c (default 4 * 2^-24) about the FP32 error of a
+ *     ray direction: no float ray fixes its value to the tolerance;
+ *   crack (Moller-Trumbore scenes only): a primary hit within the FP32
+ *     rounding bound of its barycentrics of an edge, where an FP32 test is not
+ *     watertight and the ray can pass between two triangles;
+ *   also optical margin: a lit sample at Hapke's azimuth singularity (cos psi
+ *     evaluated in FP32 within the FP32 error of its cosines reaches -1), where
+ *     the reference's FP32 formula yields NaN and drops the sample.
+ * oracle_set_margin_eta sets eta for every later render and sensor call (0:
+ * off, the default). */
+void oracle_set_margin_eta(double eta);
+/* eta_c and the relative change that makes a conditioning pixel (default
+ * 4 * 2^-24 and 1e-5, the tolerance). */
+void oracle_set_conditioning(double eta_c, double tolerance);
+/* oracle_render_pixels with per-pixel flags (1: optical margin, 8:
+ * conditioning, 16: crack); NaN radiance marks a traversal overflow. */
+void oracle_render_pixels_margin(const oscene *s, const ostate *pose, const int32_t *pixels, int n,
+                                 double *radiance, float *depth, uint8_t *margin, int nthreads);
+/* Before initialize: track margins in this sensor (threshold_shift > 0). */
+int oracle_sensor_set_margin(osensor *s, double threshold_shift);
+/* Per pixel, row-major: 1 optical margin at a cell sample, 2 circuit margin,
+ * 4 optical margin of an event-time depth sample, 16 crack at a cell sample. */
+void oracle_sensor_margins(const osensor *s, uint8_t *out);
+
 #ifdef __cplusplus
 }
 #endif

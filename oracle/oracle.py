@@ -104,7 +104,9 @@ def build():
     """Compile the two oracle libraries (and the reference harness when the
     reference checkout is present)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref = os.environ.get("DVS_REFERENCE_DIR", "/root/reference")
+    # the reference checkout: DVS_REFERENCE_DIR, else the development
+    # container's read-only checkout (absent on the GPU machines)
+    ref = os.environ.get("DVS_REFERENCE_DIR") or "/root/reference"
     if os.path.isdir(os.path.join(ref, "include", "dvs")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref], check=True)
 
@@ -170,7 +172,23 @@ def _declare(lib):
     lib.oracle_sensor_dropped.argtypes = [C.c_void_p]
     lib.oracle_sensor_rays.restype = C.c_uint64
     lib.oracle_sensor_rays.argtypes = [C.c_void_p, C.c_int]
+    lib.oracle_set_margin_eta.argtypes = [C.c_double]
+    lib.oracle_set_conditioning.argtypes = [C.c_double, C.c_double]
+    lib.oracle_render_pixels_margin.argtypes = [C.POINTER(oscene), C.POINTER(ostate), C.POINTER(C.c_int32),
+                                                C.c_int, c_d_p, c_f_p, C.POINTER(C.c_uint8), C.c_int]
+    lib.oracle_sensor_set_margin.restype = C.c_int
+    lib.oracle_sensor_set_margin.argtypes = [C.c_void_p, C.c_double]
+    lib.oracle_sensor_margins.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
     return lib
+
+
+# Margin classification defaults (the accuracy statement's exception classes).
+# MARGIN_ETA: image-plane displacement of a sub-ray's direction, about ten
+# times the FP32 rounding error of a normalized ray direction (a few ulps of
+# 6e-8); MARGIN_SHIFT: the log-intensity margin to a threshold, 1e-4.
+MARGIN_ETA = 2e-6
+MARGIN_SHIFT = 1e-4
+MARGIN_OPTICAL, MARGIN_CIRCUIT, MARGIN_DEPTH, MARGIN_CONDITIONING, MARGIN_CRACK = 1, 2, 4, 8, 16
 
 
 def load(fp64=False):
@@ -345,11 +363,29 @@ class OracleScene:
                                       px.size, dptr(rad), fptr(dep), nthreads, C.byref(a), C.byref(b))
         return rad, dep, a.value, b.value
 
+    def render_margin(self, pose, pixels=None, eta=None, nthreads=0):
+        """Radiance, depth and margin flags (MARGIN_OPTICAL) of the given
+        pixels (all when None) at one pose."""
+        px = np.arange(self.pixels, dtype=np.int32) if pixels is None else np.ascontiguousarray(pixels, np.int32)
+        rad = np.zeros(px.size, np.float64)
+        dep = np.zeros(px.size, np.float32)
+        margin = np.zeros(px.size, np.uint8)
+        st = state_struct(pose)
+        self.lib.oracle_set_margin_eta(MARGIN_ETA if eta is None else eta)
+        try:
+            self.lib.oracle_render_pixels_margin(C.byref(self.s), C.byref(st),
+                                                 px.ctypes.data_as(C.POINTER(C.c_int32)), px.size, dptr(rad),
+                                                 fptr(dep), margin.ctypes.data_as(C.POINTER(C.c_uint8)), nthreads)
+        finally:
+            self.lib.oracle_set_margin_eta(0.0)
+        return rad, dep, margin
+
 
 class OracleSensor:
     """EventSensor restatement with deterministic physics."""
 
-    def __init__(self, scene, physic, physic_effects=True, aer_delay=True):
+    def __init__(self, scene, physic, physic_effects=True, aer_delay=True, margin=False, eta=None, shift=None):
+        """margin: also classify every pixel's margin class (margins())."""
         self.scene = scene
         self.lib = scene.lib
         self.phys = physic_struct(physic)
@@ -358,6 +394,22 @@ class OracleSensor:
         if not self.h:
             raise ValueError("invalid sensor capacity")
         self.max_events = int(physic["max_events_per_step"])
+        self.eta = (MARGIN_ETA if eta is None else eta) if margin else 0.0
+        if margin and self.lib.oracle_sensor_set_margin(self.h, MARGIN_SHIFT if shift is None else shift):
+            raise ValueError("invalid margin threshold shift")
+
+    def _classified(self, call, *args):
+        self.lib.oracle_set_margin_eta(self.eta)
+        try:
+            return call(*args)
+        finally:
+            self.lib.oracle_set_margin_eta(0.0)
+
+    def margins(self):
+        """Per pixel (row-major): MARGIN_OPTICAL | MARGIN_CIRCUIT | MARGIN_DEPTH flags."""
+        out = np.zeros(self.scene.pixels, np.uint8)
+        self.lib.oracle_sensor_margins(self.h, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return out
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -366,7 +418,7 @@ class OracleSensor:
 
     def initialize(self, pose, t, nthreads=0):
         st = state_struct(pose)
-        r = self.lib.oracle_sensor_initialize(self.h, C.byref(st), float(t), nthreads)
+        r = self._classified(self.lib.oracle_sensor_initialize, self.h, C.byref(st), float(t), nthreads)
         if r:
             raise RuntimeError("oracle initialize failed: %d" % r)
 
@@ -375,8 +427,8 @@ class OracleSensor:
         cap = capacity or (self.scene.pixels * self.max_events + 1_000_000)
         out = np.zeros(cap, dtype=EVENT_DTYPE)
         n = C.c_size_t(0)
-        r = self.lib.oracle_sensor_process(self.h, arr, len(intervals), out.ctypes.data, cap, C.byref(n),
-                                           nthreads)
+        r = self._classified(self.lib.oracle_sensor_process, self.h, arr, len(intervals), out.ctypes.data, cap,
+                             C.byref(n), nthreads)
         if r:
             raise RuntimeError({1: "pixel event capacity exceeded; reduce numerical window",
                                 2: "invalid optical sample or BVH traversal overflow",

@@ -86,22 +86,31 @@ def terrain_scene(n=96, seed=5, camera=None, ss=2, fp64_oracle=False, leaf=4):
     return (V, N, I, camera, hap, DeviceScene(V, N, I, camera, ss, hap, leaf_size=leaf))
 
 
-def test_cam_terrain_matches_oracle():
-    V, N, I, camera, hap, scene = terrain_scene()
+def outside_tolerance(img, dep, orad, odep):
+    """Pixels whose radiance or depth is outside RTOL of the oracle's, or whose hit/miss differs."""
+    img, dep = np.asarray(img, np.float64), np.asarray(dep, np.float64)
+    orad, odep = np.asarray(orad, np.float64), np.asarray(odep, np.float64)
+    rad = (orad > 0) & (np.abs(img - orad) > RTOL * orad)
+    dpt = (odep > 0) & (np.abs(dep - odep) > RTOL * odep)
+    return rad | dpt | ((odep < 0) != (dep < 0)) | ((orad == 0) != (img == 0))
+
+
+@pytest.mark.parametrize("ss", [2, 8])
+def test_cam_terrain_matches_oracle(ss):
+    """Radiance and depth within 1e-5 of both oracles at every pixel outside
+    the named margin classes of the FP64 oracle's classifier (optical margin,
+    conditioning, crack); the classes are counted and stay a small minority."""
+    V, N, I, camera, hap, scene = terrain_scene(ss=ss)
     pose = dict(position=(13.0, -7.0, 700.0), rotation=(0.02, -0.01, 0.3, math.sqrt(1 - 0.02**2 - 0.01**2 - 0.09)),
                 light=trajectory.sun_direction(30, 40), intensity=1000)
     img, dep = CamRayCaster(scene).render_state(pose)
-    for fp64 in (False, True):
-        osc = O.OracleScene(V, N, I, camera, 2, hap, fp64=fp64)
-        orad, odep, oval = osc.render(pose)
-        assert oval.all()
-        err = rel_err(img, orad.astype(np.float32))
-        lit = orad > 0
-        frac = float(np.mean(err[lit] > RTOL))
-        # sub-rays whose hit or shadow decision sits on an edge/silhouette may differ (margin class)
-        assert frac < (0.002 if not fp64 else 0.01), frac
-        derr = rel_err(dep, odep)
-        assert float(np.mean(derr > RTOL)) < (0.002 if not fp64 else 0.01)
+    r64, d64, margin = O.OracleScene(V, N, I, camera, ss, hap, fp64=True).render_margin(pose)
+    r32, d32, v32 = O.OracleScene(V, N, I, camera, ss, hap).render(pose)
+    assert v32.all() and np.all(np.isfinite(r64))
+    for orad, odep in ((r32, d32), (r64, d64)):
+        bad = outside_tolerance(img, dep, orad, odep)
+        assert not np.any(bad & (margin == 0)), np.flatnonzero(bad & (margin == 0))[:10]
+    assert (margin > 0).mean() < 0.06
     assert (img > 0).mean() > 0.5 and (dep > 0).mean() > 0.8
 
 
@@ -241,17 +250,15 @@ def test_fp32_circuit_precision_mode_against_the_fp64_oracle():
     ivs = [(POSE, POSE, 0, 0.001), (start, end, 0.001, 0.003)]
     s = EventSensor(scene, phys, circuit_precision="fp32")
     s.initialize(POSE, 0)
-    ev = pixel_sorted(s.process_many(ivs))
+    ev = s.process_many(ivs)
     V, N, I = plane_mesh()
-    ors = O.OracleSensor(O.OracleScene(V, N, I, DAVIS, 1, DAVIS_HAPKE), phys)
+    ors = O.OracleSensor(O.OracleScene(V, N, I, DAVIS, 1, DAVIS_HAPKE, fp64=True), phys, margin=True)
     ors.initialize(POSE, 0)
-    oev = pixel_sorted(ors.process(ivs))
-    assert abs(len(ev) - len(oev)) <= max(2, len(oev) // 1000) and len(oev) > 0
-    if len(ev) == len(oev):
-        for f in ("x", "y", "polarity"):
-            assert float(np.mean(ev[f] != oev[f])) < 1e-3
-        same = (ev["x"] == oev["x"]) & (ev["y"] == oev["y"]) & (ev["polarity"] == oev["polarity"])
-        assert np.max(np.abs(ev["timestamp"][same] - oev["timestamp"][same])) < 1e-6
+    oev = ors.process(ivs)
+    assert len(oev) > 1000
+    report = compare_event_streams(ev, oev, ors.margins(), DAVIS["width"])
+    assert report["unclassified_mismatches"] == 0, report
+    assert report["max_timestamp_error_s"] < 1e-6, report
     with pytest.raises(ValueError):
         EventSensor(scene, phys, circuit_precision="fp16")
 
@@ -409,7 +416,7 @@ def test_sensor_matches_oracle_on_moving_terrain():
     s = EventSensor(scene, phys)
     s.initialize(traj.state(0.0), 0.0)
     osc = O.OracleScene(V, N, I, camera, 1, hap)
-    ors = O.OracleSensor(osc, phys)
+    ors = O.OracleSensor(osc, phys, margin=True)
     ors.initialize(traj.state(0.0), 0.0)
     gpu, ora = [], []
     t = 0.0
@@ -425,24 +432,35 @@ def test_sensor_matches_oracle_on_moving_terrain():
     ora.append(ors.drain())
     g, o = np.concatenate(gpu), np.concatenate(ora)
     assert len(o) > 50
+    report = compare_event_streams(g, o, ors.margins(), cam["width"])
+    assert report["unclassified_mismatches"] == 0, report
+    assert report["max_timestamp_error_s"] < 1e-6, report
+    assert report["margin_pixels"] < 0.05 * cam["width"] * cam["height"], report
 
+
+def compare_event_streams(g, o, margins, width):
+    """Per-pixel polarity sequences of two event streams: pixels whose sequences
+    differ must be margin pixels of the oracle's classifier; timestamps of the
+    other pixels' events are compared in order."""
     def per_pixel(ev):
         d = {}
         for e in ev:
             d.setdefault((int(e["x"]), int(e["y"])), []).append((float(e["timestamp"]), int(e["polarity"])))
         return d
     pg, po = per_pixel(g), per_pixel(o)
-    mismatched = 0
-    worst = 0.0
+    mismatched, unclassified, worst = 0, 0, 0.0
     for key in set(pg) | set(po):
         a, b = pg.get(key, []), po.get(key, [])
+        flagged = margins[key[1] * width + key[0]] != 0
         if [p for _, p in a] != [p for _, p in b]:
             mismatched += 1
+            unclassified += 0 if flagged else 1
             continue
-        if a:
+        if a and not flagged:
             worst = max(worst, max(abs(x - y) for (x, _), (y, _) in zip(a, b)))
-    assert mismatched <= max(1, 0.002 * cam["width"] * cam["height"]), mismatched
-    assert worst < 1e-6
+    return {"pixels_with_events": len(set(pg) | set(po)), "mismatched_pixels": mismatched,
+            "unclassified_mismatches": unclassified, "margin_pixels": int((margins != 0).sum()),
+            "max_timestamp_error_s": worst}
 
 
 def test_packet_shape_and_autotuner_do_not_change_events():

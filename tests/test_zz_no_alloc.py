@@ -36,18 +36,46 @@ def test_noalloc_render_matches_allocating_render_twice():
     n = cam["width"] * cam["height"]
     st = state_array(pose)
     stream = torch.cuda.current_stream().cuda_stream
-    for call in range(2):
-        img = torch.full((n,), -7.0, dtype=torch.float32, device="cuda")
-        dep = torch.full((n,), -7.0, dtype=torch.float32, device="cuda")
+    # every output buffer exists before the first call, so the device's free
+    # memory may only change if the entry point itself allocated
+    outs = [(torch.full((n,), -7.0, dtype=torch.float32, device="cuda"),
+             torch.full((n,), -7.0, dtype=torch.float32, device="cuda")) for _ in range(2)]
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    for img, dep in outs:
         r = lib.dvs_cam_render_noalloc(scene.handle, st.ctypes.data, C.c_void_p(img.data_ptr()),
                                        C.c_void_p(dep.data_ptr()), C.c_void_p(stream))
         assert r == _capi.DVS_OK, lib.dvs_last_error()
         torch.cuda.synchronize()
+    free_after = torch.cuda.mem_get_info()[0]
+    assert free_after >= free_before, "the first calls reserved %d bytes" % (free_before - free_after)
+    for img, dep in outs:
         got_img, got_dep = img.cpu().numpy(), dep.cpu().numpy()
         assert np.all(np.isfinite(got_img))
         np.testing.assert_allclose(got_img, want_img, rtol=RTOL, atol=0)
         np.testing.assert_allclose(got_dep, want_dep, rtol=RTOL, atol=0)
     assert (want_img > 0).mean() > 0.5
+
+
+def test_noalloc_render_without_depth_on_its_own_stream():
+    torch = pytest.importorskip("torch")
+    lib = _capi.load()
+    V, N, I = terrain.terrain_mesh(64, seed=9)
+    cam = dict(width=96, height=72, fx=80.0, fy=80.0, cx=48.0, cy=36.0)
+    scene = DeviceScene(V, N, I, cam, 1, HAPKE)
+    pose = dict(position=(-20.0, 11.0, 500.0), rotation=(0.0, 0.0, 0.0, 1.0),
+                light=trajectory.sun_direction(40, 10), intensity=1000)
+    want_img, _ = CamRayCaster(scene).render_state(pose)
+    st = state_array(pose)
+    side = torch.cuda.Stream()
+    for call in range(2):
+        img = torch.full((cam["width"] * cam["height"],), -7.0, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        r = lib.dvs_cam_render_noalloc(scene.handle, st.ctypes.data, C.c_void_p(img.data_ptr()), None,
+                                       C.c_void_p(side.cuda_stream))
+        assert r == _capi.DVS_OK, lib.dvs_last_error()
+        side.synchronize()
+        np.testing.assert_allclose(img.cpu().numpy(), want_img, rtol=RTOL, atol=0)
 
 
 def test_noalloc_render_rejects_images_above_the_limit():
