@@ -766,7 +766,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision-report", action="store_true",
                     help="skip the precision workload's error report against the FP64 oracle")
-    ap.add_argument("--autotune", action="store_true", help="time the packet shapes on the first warm-up batch")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip the autotuner (packet shape, then circuit-step chunk) on the first warm-up batch")
     ap.add_argument("--rays", type=int, default=0, help="sub-rays per lane: 1, 2 or 4 (0 = default)")
     ap.add_argument("--adaptive-ms", type=float, default=2.0,
                     help="also run the adaptive optical solver over this many simulated milliseconds")

@@ -61,7 +61,7 @@ class Physic(C.Structure):
 class SensorOptions(C.Structure):
     _fields_ = [("physic_effects", C.c_int32), ("aer_delay", C.c_int32), ("cells_per_chunk", C.c_int32),
                 ("cells_per_warp", C.c_int32), ("timing", C.c_int32), ("row_begin", C.c_int32),
-                ("row_end", C.c_int32), ("circuit_precision", C.c_int32)]
+                ("row_end", C.c_int32), ("circuit_precision", C.c_int32), ("host_readout", C.c_int32)]
 
 
 class BvhParams(C.Structure):
@@ -105,12 +105,16 @@ EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_d
            "dvs_readout_counters", "dvs_config_load", "dvs_frames_load", "dvs_trajectory_create",
            "dvs_trajectory_destroy", "dvs_trajectory_range", "dvs_trajectory_evaluate", "dvs_cam_render_blur",
            "dvs_scene_view_create", "dvs_sensor_device_bytes", "dvs_sensor_set_tuning", "dvs_sensor_autotune",
-           "dvs_batch_create", "dvs_batch_destroy", "dvs_batch_process", "dvs_batch_stats_get", "dvs_noise_poisson")
+           "dvs_batch_create", "dvs_batch_destroy", "dvs_batch_process", "dvs_batch_stats_get", "dvs_noise_poisson",
+           "dvs_device_readout_create", "dvs_device_readout_destroy", "dvs_device_readout_submit",
+           "dvs_device_readout_drain", "dvs_device_readout_read", "dvs_device_readout_counters")
 
 
 class Tuning(C.Structure):
     _fields_ = [("cells_per_warp", C.c_int32), ("rays_per_lane", C.c_int32), ("candidates", C.c_int32),
-                ("cells_timed", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double)]
+                ("cells_timed", C.c_int32), ("best_ms", C.c_double), ("default_ms", C.c_double),
+                ("cells_per_chunk", C.c_int32), ("chunk_candidates", C.c_int32), ("chunk_cells", C.c_int32),
+                ("chunk_best_ms", C.c_double), ("chunk_default_ms", C.c_double)]
 
 
 class SceneConfig(C.Structure):
@@ -188,6 +192,12 @@ def _declare(lib):
     lib.dvs_readout_drain.argtypes = [vp, C.POINTER(sz)]
     lib.dvs_readout_read.argtypes = [vp, vp, sz, C.POINTER(sz)]
     lib.dvs_readout_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    lib.dvs_device_readout_create.argtypes = [C.c_double, C.c_double, sz, sz, C.POINTER(vp)]
+    lib.dvs_device_readout_destroy.argtypes = [vp]
+    lib.dvs_device_readout_submit.argtypes = [vp, vp, sz, C.c_double, C.POINTER(sz)]
+    lib.dvs_device_readout_drain.argtypes = [vp, C.POINTER(sz)]
+    lib.dvs_device_readout_read.argtypes = [vp, vp, sz, C.POINTER(sz)]
+    lib.dvs_device_readout_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.dvs_config_load.argtypes = [C.c_char_p, C.POINTER(Camera), C.POINTER(Physic), C.POINTER(Hapke),
                                     C.POINTER(SceneConfig)]
     lib.dvs_frames_load.argtypes = [C.c_char_p, vp, sz, C.POINTER(sz)]

@@ -33,7 +33,7 @@ def nvcc():
 
 def _sources():
     cuda_and_core = [os.path.join(CSRC, f) for f in ("kernels.cu", "batch.cu", "adaptive.cu", "capi.cu", "noalloc.cu",
-                                                     "bvh_build.cpp", "readout.cpp")]
+                                                     "readout.cu", "bvh_build.cpp", "readout.cpp")]
     host_inputs = [os.path.join(APPS, f) for f in ("app_config.cpp", "app_scene.cpp", "app_trajectory.cpp",
                                                    "app_writers.cpp", "app_capi.cpp")]
     return cuda_and_core + host_inputs

@@ -122,6 +122,113 @@ cudaError_t grow_pinned(T *&ptr, size_t &cap, size_t need) {
 // Per-device set-up of dvs_cam_render_noalloc (noalloc.cu).
 int dvsgb_noalloc_prepare(int device, int geometry);
 
+// The device readout FIFO (readout.cu): its buffers in one allocation, the
+// pinned status words, and the released events of the last submit or drain.
+struct DeviceReadout {
+  ReadoutSort sort{};
+  ReadoutFifo fifo{};
+  size_t max_batch = 0;
+  int grid = 1;  // sort/scan blocks, sized from the previous batch
+  void *arena = nullptr;
+  int32_t *h_status = nullptr;  // [out_count, status]
+  unsigned long long *h_counters = nullptr;  // [dropped, peak]
+
+  cudaError_t create(double bandwidth, double latency, size_t capacity, size_t batch, cudaStream_t st) {
+    max_batch = std::max<size_t>(batch, 1);
+    const size_t ring = bandwidth > 0 ? next_pow2(std::min<size_t>(std::max<size_t>(capacity, 1), size_t(1) << 24))
+                                      : 1;
+    const int max_grid = 608;  // 4 blocks per SM of a GB300
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+      const size_t at = off;
+      off = align_up(off + bytes, 256);
+      return at;
+    };
+    const size_t o_kt0 = take(8 * max_batch), o_kt1 = take(8 * max_batch), o_yx0 = take(4 * max_batch),
+                 o_yx1 = take(4 * max_batch), o_i0 = take(4 * max_batch), o_i1 = take(4 * max_batch),
+                 o_hist = take(4 * 256 * (size_t)max_grid), o_ring = take(sizeof(DevEvent) * ring),
+                 o_bmax = take(8 * (size_t)max_grid), o_comp = take(8 * max_batch), o_del = take(8 * max_batch),
+                 o_out = take(sizeof(DevEvent) * (ring + max_batch)), o_u64 = take(8 * 5), o_avail = take(8),
+                 o_i32 = take(4 * 5), o_plan = take(8 * 3);
+    cudaError_t e = cudaMalloc(&arena, off);
+    if (e != cudaSuccess) return e;
+    bytes = off;
+    char *b = static_cast<char *>(arena);
+    sort.kt[0] = reinterpret_cast<unsigned long long *>(b + o_kt0);
+    sort.kt[1] = reinterpret_cast<unsigned long long *>(b + o_kt1);
+    sort.kyx[0] = reinterpret_cast<unsigned *>(b + o_yx0);
+    sort.kyx[1] = reinterpret_cast<unsigned *>(b + o_yx1);
+    sort.idx[0] = reinterpret_cast<unsigned *>(b + o_i0);
+    sort.idx[1] = reinterpret_cast<unsigned *>(b + o_i1);
+    sort.hist = reinterpret_cast<unsigned *>(b + o_hist);
+    int32_t *i32 = reinterpret_cast<int32_t *>(b + o_i32);
+    sort.cur = i32;
+    sort.skip = i32 + 1;
+    fifo.overflow = i32 + 2;
+    fifo.status = i32 + 3;
+    fifo.out_count = i32 + 4;
+    unsigned long long *u64 = reinterpret_cast<unsigned long long *>(b + o_u64);
+    fifo.head = u64;
+    fifo.tail = u64 + 1;
+    fifo.peak = u64 + 2;
+    fifo.peak_batch = u64 + 3;
+    fifo.dropped = u64 + 4;
+    fifo.available = reinterpret_cast<double *>(b + o_avail);
+    fifo.ring = reinterpret_cast<DevEvent *>(b + o_ring);
+    fifo.ring_size = ring;
+    fifo.capacity = capacity;
+    fifo.step = bandwidth > 0 ? 1.0 / bandwidth : 0.0;
+    fifo.latency = latency;
+    fifo.block_max = reinterpret_cast<double *>(b + o_bmax);
+    fifo.completion = reinterpret_cast<double *>(b + o_comp);
+    fifo.delivery = reinterpret_cast<double *>(b + o_del);
+    fifo.plan = reinterpret_cast<long long *>(b + o_plan);
+    fifo.out = reinterpret_cast<DevEvent *>(b + o_out);
+    e = cudaMemsetAsync(b + o_u64, 0, o_plan + 8 * 3 - o_u64, st);  // positions, counters, availability, words
+    if (e == cudaSuccess) e = cudaMallocHost(&h_status, sizeof(int32_t) * 2);
+    if (e == cudaSuccess) e = cudaMallocHost(&h_counters, sizeof(unsigned long long) * 2);
+    return e;
+  }
+  ~DeviceReadout() {
+    cudaFree(arena);
+    if (h_status) cudaFreeHost(h_status);
+    if (h_counters) cudaFreeHost(h_counters);
+  }
+  static size_t next_pow2(size_t v) {
+    size_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+  }
+  // Enqueues the FIFO over *count device events (none when *gate != 0) and
+  // the copies of its status and counters to pinned memory.
+  cudaError_t submit(const DevEvent *events, const int32_t *count, const int32_t *gate, const double *now,
+                     cudaStream_t st) {
+    ReadoutFifo f = fifo;
+    f.gate = gate;
+    cudaError_t e = launch_readout_submit(events, count, sort, f, now, grid, st);
+    return e == cudaSuccess ? copy_status(st) : e;
+  }
+  cudaError_t drain(cudaStream_t st) {
+    cudaError_t e = launch_readout_drain(fifo, grid, st);
+    return e == cudaSuccess ? copy_status(st) : e;
+  }
+  cudaError_t copy_status(cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(h_status, fifo.out_count, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_status + 1, fifo.status, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_counters, fifo.dropped, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h_counters + 1, fifo.peak, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    return e;
+  }
+  // After the stream reached the copies: the next batches' sort grid.
+  void observed(size_t events) {
+    grid = (int)std::min<size_t>(608, std::max<size_t>(1, (events + 4095) / 4096));
+  }
+  size_t bytes = 0;  // device memory held
+  // kernels of one submit: keys, 12 radix passes of 4, the scan's 3, commit, release, advance
+  int launches() const { return 1 + 12 * 4 + (fifo.step > 0 ? 3 : 0) + 3; }
+};
+
 // ---- handles --------------------------------------------------------------------
 struct dvs_scene {
   int device = 0;
@@ -192,7 +299,8 @@ struct dvs_sensor {
   double threshold_std = 0, threshold_min = 0;
   int max_events = 16;
   unsigned seed = 0;
-  Readout *readout = nullptr;
+  Readout *readout = nullptr;        // host FIFO (options.host_readout)
+  DeviceReadout *dro = nullptr;      // device FIFO (the default)
   bool initialized = false;
   double last_time = 0;
   bool pending = false;  // an enqueued batch awaits collect
@@ -738,6 +846,14 @@ int dvs_sensor_create(dvs_scene *scene, const dvs_physic *physic, const dvs_sens
   if ((e = cudaEventCreateWithFlags(&s->staged, cudaEventDisableTiming)) != cudaSuccess) return bail(e, "event");
   if ((e = cudaMemsetAsync(s->counters, 0, sizeof(unsigned long long) * kCntSlots, s->stream)) != cudaSuccess)
     return bail(e, "clear counters");
+  if (!s->opt.host_readout) {
+    s->dro = new DeviceReadout;
+    if ((e = s->dro->create(s->opt.aer_delay ? (double)physic->readout_bandwidth : 0,
+                            s->opt.aer_delay ? (double)physic->readout_latency : 0,
+                            (size_t)std::max(1, physic->readout_queue_capacity), (size_t)n * s->max_events,
+                            s->stream)) != cudaSuccess)
+      return bail(e, "device readout");
+  }
   *out = s;
   return DVS_OK;
 }
@@ -789,6 +905,7 @@ int dvs_sensor_destroy(dvs_sensor *s) {
   if (s->h_ref) cudaFreeHost(s->h_ref);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s->readout;
+  delete s->dro;
   delete s;
   return DVS_OK;
 }
@@ -975,6 +1092,11 @@ static int enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count)
   CUDA_TRY(launch_event_depth(view, s->ivs, (int)count, s->events, s->event_total, s->error_word, s->counters,
                               s->stream),
            "event depth");
+  if (s->dro) {  // the readout FIFO on the device, after the event depths
+    CUDA_TRY(s->dro->submit(s->events, s->event_total, s->error_word, &s->ivs[count - 1].t1, s->stream),
+             "device readout");
+    s->stats.launches += s->dro->launches();
+  }
   record_timer(s, 3);
   s->stats.launches += 2;
   s->last_time = ivs[count - 1].t1;
@@ -996,6 +1118,28 @@ static void collect_timers(dvs_sensor *s) {
   s->timers_used = 0;
 }
 
+// The device FIFO's released events (its status words already copied and
+// the stream synchronized), appended to the ready list; counters updated.
+static int fetch_released(dvs_sensor *s) {
+  DeviceReadout &d = *s->dro;
+  if (d.h_status[1]) return fail(DVS_ERR_CAPACITY, "readout queue capacity exceeds the device ring buffer");
+  const int32_t released = d.h_status[0];
+  if (released > 0) {
+    CUDA_TRY(grow_pinned(s->h_events, s->h_events_cap, (size_t)released), "event staging");
+    CUDA_TRY(cudaMemcpyAsync(s->h_events, d.fifo.out, sizeof(DevEvent) * released, cudaMemcpyDeviceToHost,
+                             s->stream),
+             "copy released events");
+    CUDA_TRY(cudaStreamSynchronize(s->stream), "copy released events");
+  }
+  for (int32_t i = 0; i < released; ++i) {
+    const DevEvent &e = s->h_events[i];
+    s->ready.push_back(HostEvent{e.t, e.x, e.y, e.polarity, e.depth});
+  }
+  s->stats.dropped = d.h_counters[0];
+  s->stats.peak_queue = d.h_counters[1];
+  return DVS_OK;
+}
+
 // collect_events (event_sensor.cu:296-305): status, events, readout.
 static int collect(dvs_sensor *s, double end, size_t *n_ready) {
   CUDA_TRY(cudaMemcpyAsync(s->h_status, s->event_total, sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream), "copy count");
@@ -1006,6 +1150,21 @@ static int collect(dvs_sensor *s, double end, size_t *n_ready) {
   const int32_t count = s->h_status[0], word = s->h_status[1];
   if (word) return map_error(word);
   auto t0 = std::chrono::steady_clock::now();
+  if (s->ready_head > 0 && s->ready_head == s->ready.size()) {
+    s->ready.clear();
+    s->ready_head = 0;
+  }
+  if (s->dro) {  // the device FIFO already ran: fetch what it released
+    const size_t before = s->ready.size();
+    int r = fetch_released(s);
+    if (r) return r;
+    s->dro->observed((size_t)count);
+    s->stats.events_generated += (uint64_t)count;
+    s->stats.events_delivered += s->ready.size() - before;
+    s->stats.readout_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (n_ready) *n_ready = s->ready.size() - s->ready_head;
+    return DVS_OK;
+  }
   if (count > 0) {
     CUDA_TRY(grow_pinned(s->h_events, s->h_events_cap, (size_t)count), "event staging");
     CUDA_TRY(cudaMemcpyAsync(s->h_events, s->events, sizeof(DevEvent) * count, cudaMemcpyDeviceToHost, s->stream),
@@ -1016,10 +1175,6 @@ static int collect(dvs_sensor *s, double end, size_t *n_ready) {
   for (int32_t i = 0; i < count; ++i) {
     const DevEvent &d = s->h_events[i];
     batch[i] = HostEvent{d.t, d.x, d.y, d.polarity, d.depth};
-  }
-  if (s->ready_head > 0 && s->ready_head == s->ready.size()) {
-    s->ready.clear();
-    s->ready_head = 0;
   }
   const size_t before = s->ready.size();
   s->readout->submit(batch, end, s->ready);
@@ -1249,6 +1404,11 @@ int dvs_sensor_process_adaptive(dvs_sensor *s, const dvs_optical_interval *ivs, 
   CUDA_TRY(launch_emit_events(n, s->order, s->scene->camera.width, s->max_events, s->ev_count,
                               s->slab_t, s->slab_p, s->events, s->event_total, s->stream),
            "compact events");
+  if (s->dro) {
+    CUDA_TRY(s->dro->submit(s->events, s->event_total, s->error_word, &s->ivs[count - 1].t1, s->stream),
+             "device readout");
+    s->stats.launches += s->dro->launches();
+  }
   record_timer(s, 3);
   s->stats.launches += 2;
   s->last_time = end;
@@ -1323,7 +1483,19 @@ int dvs_sensor_process_events(dvs_sensor *s, const dvs_optical_interval *ivs, si
 
 int dvs_sensor_drain(dvs_sensor *s, dvs_event *out, size_t capacity, size_t *n_out) {
   if (!s || !n_out) return fail(DVS_ERR_INVALID, "null argument");
-  s->readout->drain(s->ready);
+  if (s->dro) {
+    CUDA_TRY(cudaSetDevice(s->device), "select device");
+    CUDA_TRY(s->dro->drain(s->stream), "device readout drain");
+    CUDA_TRY(cudaStreamSynchronize(s->stream), "device readout drain");
+    if (s->ready_head > 0 && s->ready_head == s->ready.size()) {
+      s->ready.clear();
+      s->ready_head = 0;
+    }
+    int r = fetch_released(s);
+    if (r) return r;
+  } else {
+    s->readout->drain(s->ready);
+  }
   return dvs_sensor_read(s, out, capacity, n_out);
 }
 
@@ -1338,6 +1510,7 @@ int dvs_sensor_device_bytes(const dvs_sensor *s, uint64_t *bytes) {
   if (s->knots) b += n * (uint64_t)s->knot_capacity * sizeof(OpticalKnot) + 3 * n * sizeof(int32_t);
   if (s->exact_cells) b += n * (uint64_t)s->knot_capacity * (2 * sizeof(int32_t) + sizeof(double));
   if (s->probe_state) b += (uint64_t)s->n_probes * (sizeof(int32_t) + 2 * sizeof(double));
+  if (s->dro) b += s->dro->bytes;
   *bytes = b;
   return DVS_OK;
 }
@@ -1365,12 +1538,104 @@ int dvs_sensor_set_tuning(dvs_sensor *s, int32_t cells_per_warp, int32_t rays_pe
   return DVS_OK;
 }
 
+}  // extern "C"
+
+// Second stage of the autotuner: the circuit-step chunk.  The optics ->
+// circuit pipeline of every pixel over the first (up to 64) cells of the
+// staged batch, with the chosen packet shape, for chunks of 1, 1/2, 1/4 and
+// 1/8 of them (at least 4 cells), each run from the same shadow copy of the
+// circuit state; the real state, RNG and time are untouched.  Keeps the
+// current chunk unless another is >= 3 % faster.
+static int autotune_chunk(dvs_sensor *s, size_t n_cells, dvs_tuning *out) {
+  const int n = s->pixels();
+  const int ncs = (int)std::min<size_t>(n_cells, 64);
+  size_t def_chunk;
+  int cw_log2;
+  chunk_shape(s, (size_t)ncs, (size_t)n, def_chunk, cw_log2);
+  std::vector<int> cands;
+  for (int c = ncs; c >= 4 && cands.size() < 4; c /= 2) cands.push_back(c);
+  if (std::find(cands.begin(), cands.end(), (int)def_chunk) == cands.end()) cands.push_back((int)def_chunk);
+  out->cells_per_chunk = (int32_t)def_chunk;
+  out->chunk_candidates = 0;
+  out->chunk_cells = ncs;
+  out->chunk_best_ms = out->chunk_default_ms = -1;
+  if (cands.size() < 2) return DVS_OK;
+  // shadow state: the five FP64 fields, the reset flags and (when drawn) the XORWOW states
+  const bool rng = !s->photo.philox && (s->photo.shot_noise || s->p.reset_noise_std > 0);
+  const size_t fbytes = sizeof(double) * (size_t)n, rbytes = rng ? sizeof(curandStateXORWOW_t) * (size_t)n : 0;
+  char *shadow = nullptr;
+  CUDA_TRY(cudaMalloc(&shadow, 5 * fbytes + (size_t)n + rbytes), "autotune shadow state");
+  CircuitState st = s->st;
+  double **fields[5] = {&st.receptor_log, &st.reference_log, &st.refractory_until, &st.threshold_pos,
+                        &st.threshold_neg};
+  double *src[5] = {s->st.receptor_log, s->st.reference_log, s->st.refractory_until, s->st.threshold_pos,
+                    s->st.threshold_neg};
+  for (int f = 0; f < 5; ++f) *fields[f] = reinterpret_cast<double *>(shadow + f * fbytes);
+  st.reset_pending = reinterpret_cast<int8_t *>(shadow + 5 * fbytes);
+  if (rng) st.rng = reinterpret_cast<curandStateXORWOW_t *>(shadow + 5 * fbytes + (size_t)n);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t err = cudaEventCreate(&e0);
+  if (err == cudaSuccess) err = cudaEventCreate(&e1);
+  if (err == cudaSuccess) err = ensure_radiance(s, (size_t)ncs);
+  const SceneView view = s->view();
+  float best = -1, def_ms = -1;
+  int best_c = (int)def_chunk;
+  for (int c : cands) {
+    if (err != cudaSuccess) break;
+    for (int f = 0; f < 5 && err == cudaSuccess; ++f)
+      err = cudaMemcpyAsync(*fields[f], src[f], fbytes, cudaMemcpyDeviceToDevice, s->stream);
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(st.reset_pending, s->st.reset_pending, (size_t)n, cudaMemcpyDeviceToDevice, s->stream);
+    if (err == cudaSuccess && rng) err = cudaMemcpyAsync(st.rng, s->st.rng, rbytes, cudaMemcpyDeviceToDevice, s->stream);
+    if (err == cudaSuccess) err = cudaMemsetAsync(s->ev_count, 0, sizeof(int32_t) * n, s->stream);
+    if (err == cudaSuccess) err = cudaEventRecord(e0, s->stream);
+    for (int c0 = 0; c0 < ncs && err == cudaSuccess; c0 += c) {
+      const int nc = std::min(c, ncs - c0);
+      err = launch_trace_cells(view, n, s->poses, c0, nc, cw_log2, s->radiance, nullptr, nullptr, s->stream);
+      if (err == cudaSuccess)
+        err = launch_circuit(n, s->cells, c0, nc, s->radiance, s->p, s->photo, s->max_events, st, s->ev_count,
+                             s->slab_t, s->slab_p, s->error_word, nullptr, s->stream);
+    }
+    float ms = 0;
+    if (err == cudaSuccess) err = cudaEventRecord(e1, s->stream);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (err != cudaSuccess) break;
+    ++out->chunk_candidates;
+    if (c == (int)def_chunk) def_ms = ms;
+    if (best < 0 || ms < best) {
+      best = ms;
+      best_c = c;
+    }
+  }
+  // the tuning runs leave no events or errors behind for the next batch
+  if (err == cudaSuccess) err = cudaMemsetAsync(s->ev_count, 0, sizeof(int32_t) * n, s->stream);
+  if (err == cudaSuccess) err = cudaMemsetAsync(s->error_word, 0, sizeof(int32_t), s->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s->stream);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(shadow);
+  if (err != cudaSuccess) return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in chunk autotune : ") + cudaGetErrorString(err));
+  if (def_ms > 0 && best > 0.97f * def_ms) {
+    best = def_ms;
+    best_c = (int)def_chunk;
+  }
+  s->opt.cells_per_chunk = best_c;
+  out->cells_per_chunk = best_c;
+  out->chunk_best_ms = best;
+  out->chunk_default_ms = def_ms;
+  return DVS_OK;
+}
+
+extern "C" {
+
 int dvs_sensor_autotune(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count, dvs_tuning *out) {
   // Times the optics of (a prefix of) the next batch for every packet shape
   // -- cells per warp 4..32, one or two sub-rays per lane -- and keeps the
-  // fastest.  Only the trace kernel runs: no circuit state, RNG or time
-  // changes, so the same batch is then processed as usual.
+  // fastest, then the circuit-step chunk (autotune_chunk).  No circuit
+  // state, RNG or time changes, so the same batch is then processed as usual.
   if (!out) return fail(DVS_ERR_INVALID, "null argument");
+  if (s && s->pending) return fail(DVS_ERR_INVALID, "collect the enqueued batch before autotuning");
   size_t n_cells = 0;
   int r = upload_batch(s, ivs, count, n_cells);
   if (r) return r;
@@ -1449,7 +1714,7 @@ int dvs_sensor_autotune(dvs_sensor *s, const dvs_optical_interval *ivs, size_t c
   out->cells_timed = nc;
   out->best_ms = best;
   out->default_ms = def_ms;
-  return DVS_OK;
+  return autotune_chunk(s, n_cells, out);
 }
 
 int dvs_sensor_stats_reset(dvs_sensor *s) {
@@ -1732,6 +1997,8 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
       if (e == cudaSuccess)
         e = launch_event_depth(s->view(), s->ivs, (int)counts[m], s->events, s->event_total, s->error_word,
                                s->counters, st);
+      if (e == cudaSuccess && s->dro)
+        e = s->dro->submit(s->events, s->event_total, s->error_word, &s->ivs[counts[m] - 1].t1, st);
     }
     if (e == cudaSuccess) e = cudaEventRecordWithFlags(b->ev_end, st, cudaEventRecordExternal);
     cudaGraph_t graph = nullptr;
@@ -1769,7 +2036,7 @@ int dvs_batch_process(dvs_batch *b, const dvs_optical_interval *const *intervals
   for (size_t m = 0; m < n; ++m) {
     if (!counts[m]) continue;
     dvs_sensor *s = b->members[m];
-    s->stats.launches += 4;
+    s->stats.launches += 4 + (s->dro ? s->dro->launches() : 0);
     s->stats.optics_launches += 1;
     s->stats.circuit_launches += 1;
     s->last_time = intervals[m][counts[m] - 1].t1;
@@ -1859,6 +2126,149 @@ int dvs_readout_counters(const dvs_readout *r, uint64_t *dropped, uint64_t *peak
   if (!r) return fail(DVS_ERR_INVALID, "null argument");
   if (dropped) *dropped = r->fifo.dropped();
   if (peak_queue) *peak_queue = r->fifo.peak();
+  return DVS_OK;
+}
+
+}  // extern "C"
+
+// ---- standalone device readout FIFO ---------------------------------------------------
+struct dvs_device_readout {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DeviceReadout dro;
+  DevEvent *d_in = nullptr, *h_in = nullptr, *h_out = nullptr;
+  int32_t *d_count = nullptr, *h_count = nullptr;
+  double *d_now = nullptr, *h_now = nullptr;
+  std::vector<HostEvent> ready;
+  size_t head = 0;
+};
+
+namespace {
+int device_readout_fetch(dvs_device_readout *r) {
+  CUDA_TRY(cudaStreamSynchronize(r->stream), "device readout");
+  if (r->dro.h_status[1]) return fail(DVS_ERR_CAPACITY, "readout queue capacity exceeds the device ring buffer");
+  const int32_t released = r->dro.h_status[0];
+  if (released > 0) {
+    CUDA_TRY(cudaMemcpyAsync(r->h_out, r->dro.fifo.out, sizeof(DevEvent) * released, cudaMemcpyDeviceToHost,
+                             r->stream),
+             "copy released events");
+    CUDA_TRY(cudaStreamSynchronize(r->stream), "copy released events");
+  }
+  if (r->head && r->head == r->ready.size()) {
+    r->ready.clear();
+    r->head = 0;
+  }
+  for (int32_t i = 0; i < released; ++i) {
+    const DevEvent &e = r->h_out[i];
+    r->ready.push_back(HostEvent{e.t, e.x, e.y, e.polarity, e.depth});
+  }
+  return DVS_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int dvs_device_readout_create(double bandwidth, double latency, size_t capacity, size_t max_batch,
+                              dvs_device_readout **out) {
+  if (!out) return fail(DVS_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (!std::isfinite(bandwidth) || !std::isfinite(latency) || capacity < 1 || max_batch < 1 ||
+      max_batch > (size_t(1) << 28))
+    return fail(DVS_ERR_INVALID, "invalid readout bandwidth, latency, capacity or batch size");
+  dvs_device_readout *r = new dvs_device_readout;
+  cudaGetDevice(&r->device);
+  const size_t out_cap = r->dro.next_pow2(std::min<size_t>(capacity, size_t(1) << 24)) + max_batch;
+  cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = r->dro.create(bandwidth, latency, capacity, max_batch, r->stream);
+  if (e == cudaSuccess) e = cudaMalloc(&r->d_in, sizeof(DevEvent) * max_batch + 64);
+  if (e == cudaSuccess) e = cudaMallocHost(&r->h_in, sizeof(DevEvent) * max_batch + 64);
+  if (e == cudaSuccess) e = cudaMallocHost(&r->h_out, sizeof(DevEvent) * out_cap);
+  if (e == cudaSuccess) {
+    r->d_count = reinterpret_cast<int32_t *>(r->d_in + max_batch);
+    r->d_now = reinterpret_cast<double *>(r->d_in + max_batch) + 1;
+    r->h_count = reinterpret_cast<int32_t *>(r->h_in + max_batch);
+    r->h_now = reinterpret_cast<double *>(r->h_in + max_batch) + 1;
+  }
+  if (e != cudaSuccess) {
+    dvs_device_readout_destroy(r);
+    return fail(DVS_ERR_CUDA, std::string("[CUDA Error] in create device readout : ") + cudaGetErrorString(e));
+  }
+  *out = r;
+  return DVS_OK;
+}
+
+int dvs_device_readout_destroy(dvs_device_readout *r) {
+  if (!r) return DVS_OK;
+  cudaSetDevice(r->device);
+  if (r->stream) cudaStreamSynchronize(r->stream);
+  cudaFree(r->d_in);
+  if (r->h_in) cudaFreeHost(r->h_in);
+  if (r->h_out) cudaFreeHost(r->h_out);
+  if (r->stream) cudaStreamDestroy(r->stream);
+  delete r;
+  return DVS_OK;
+}
+
+int dvs_device_readout_submit(dvs_device_readout *r, const dvs_event *events, size_t n, double now,
+                              size_t *n_ready) {
+  if (!r || !n_ready || (n && !events)) return fail(DVS_ERR_INVALID, "null argument");
+  if (n > r->dro.max_batch) return fail(DVS_ERR_INVALID, "more events than the readout's batch size");
+  if (!std::isfinite(now)) return fail(DVS_ERR_INVALID, "invalid readout time");
+  CUDA_TRY(cudaSetDevice(r->device), "select device");
+  for (size_t i = 0; i < n; ++i) {
+    DevEvent d{};
+    d.t = events[i].timestamp;
+    d.depth = events[i].depth;
+    d.rank = (int32_t)i;
+    d.x = events[i].x;
+    d.y = events[i].y;
+    d.polarity = events[i].polarity;
+    r->h_in[i] = d;
+  }
+  *r->h_count = (int32_t)n;
+  *r->h_now = now;
+  if (n) CUDA_TRY(cudaMemcpyAsync(r->d_in, r->h_in, sizeof(DevEvent) * n, cudaMemcpyHostToDevice, r->stream),
+                  "upload events");
+  CUDA_TRY(cudaMemcpyAsync(r->d_count, r->h_count, 16, cudaMemcpyHostToDevice, r->stream), "upload count and time");
+  CUDA_TRY(r->dro.submit(r->d_in, r->d_count, nullptr, r->d_now, r->stream), "device readout");
+  int rc = device_readout_fetch(r);
+  if (rc) return rc;
+  r->dro.observed(n);
+  *n_ready = r->ready.size() - r->head;
+  return DVS_OK;
+}
+
+int dvs_device_readout_drain(dvs_device_readout *r, size_t *n_ready) {
+  if (!r || !n_ready) return fail(DVS_ERR_INVALID, "null argument");
+  CUDA_TRY(cudaSetDevice(r->device), "select device");
+  CUDA_TRY(r->dro.drain(r->stream), "device readout drain");
+  int rc = device_readout_fetch(r);
+  if (rc) return rc;
+  *n_ready = r->ready.size() - r->head;
+  return DVS_OK;
+}
+
+int dvs_device_readout_read(dvs_device_readout *r, dvs_event *out, size_t capacity, size_t *n_out) {
+  if (!r || !n_out) return fail(DVS_ERR_INVALID, "null argument");
+  const size_t m = std::min(capacity, r->ready.size() - r->head);
+  if (m && !out) return fail(DVS_ERR_INVALID, "null output buffer");
+  for (size_t i = 0; i < m; ++i) {
+    const HostEvent &e = r->ready[r->head + i];
+    out[i].timestamp = e.t;
+    out[i].x = e.x;
+    out[i].y = e.y;
+    out[i].polarity = e.p;
+    out[i].depth = e.depth;
+  }
+  r->head += m;
+  *n_out = m;
+  return DVS_OK;
+}
+
+int dvs_device_readout_counters(const dvs_device_readout *r, uint64_t *dropped, uint64_t *peak_queue) {
+  if (!r) return fail(DVS_ERR_INVALID, "null argument");
+  if (dropped) *dropped = r->dro.h_counters[0];
+  if (peak_queue) *peak_queue = r->dro.h_counters[1];
   return DVS_OK;
 }
 

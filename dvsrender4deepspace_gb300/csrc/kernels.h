@@ -68,6 +68,40 @@ struct alignas(8) DevEvent {
   int8_t pad[3];
 };
 
+// Device readout (readout.cu).  Sort buffers for up to max_batch events:
+// keys (order-preserving bits of t, then y<<16|x) and source indices, double
+// buffered; cur selects the buffer that holds the current order, skip marks
+// a radix pass that moves nothing; hist: 256 x grid per-block digit counts.
+struct ReadoutSort {
+  unsigned long long *kt[2];
+  unsigned *kyx[2];
+  unsigned *idx[2];
+  int32_t *cur, *skip;
+  unsigned *hist;
+};
+// FIFO state and scratch.  ring: pending delivered events, ring_size a power
+// of two; head/tail: monotone positions of the pending entries; plan: the
+// release counts of the parallel path (-1: the serial path finished the batch).
+struct ReadoutFifo {
+  DevEvent *ring;
+  unsigned long long ring_size, capacity;
+  unsigned long long *head, *tail, *peak, *peak_batch, *dropped;
+  double *available;
+  double step, latency;  // 1 / bandwidth (0: no FIFO delay), latency
+  double *block_max, *completion, *delivery;
+  int32_t *overflow, *status, *out_count;
+  long long *plan;
+  DevEvent *out;         // released events of the last submit or drain
+  const int32_t *gate;   // optional: a nonzero word (the batch's error word) leaves the FIFO untouched
+};
+// Orders a batch of *count events by (t, y, x) and passes it through the
+// FIFO at time *now (device memory, so a captured graph reads each step's);
+// the released events land in f.out (*f.out_count of them).  grid: blocks
+// of the sort and scan kernels (the sort's hist holds 256 x grid).
+cudaError_t launch_readout_submit(const DevEvent *events, const int32_t *count, ReadoutSort s, ReadoutFifo f,
+                                  const double *now, int grid, cudaStream_t st);
+cudaError_t launch_readout_drain(ReadoutFifo f, int grid, cudaStream_t st);
+
 // Error word bits (host maps them to DVS_ERR_* with capacity first, as
 // event_sensor.cu:300-301 tests code 1 before any other code).
 enum : int32_t { kErrCapacity = 1, kErrOptical = 2, kErrStalled = 4 };

@@ -154,7 +154,7 @@ class EventSensor:
     """EventSensor (include/dvs/event_sensor.hpp:40-79) on the GB300 path."""
 
     def __init__(self, scene, physic, physic_effects=True, aer_delay=True, cells_per_chunk=0, cells_per_warp=0,
-                 timing=False, row_begin=0, row_end=0, circuit_precision="fp64"):
+                 timing=False, row_begin=0, row_end=0, circuit_precision="fp64", host_readout=False):
         lib = _capi.load()
         self.scene = scene
         self.physic = dict(physic)
@@ -171,6 +171,7 @@ class EventSensor:
         if circuit_precision not in modes:
             raise ValueError("circuit_precision must be fp64, fp32 or fp32-philox")
         opt.circuit_precision = modes[circuit_precision]
+        opt.host_readout = int(host_readout)
         h = C.c_void_p()
         check(lib.dvs_sensor_create(scene.handle, C.byref(physic_struct(physic)), C.byref(opt), C.byref(h)))
         self.handle = h
@@ -299,46 +300,56 @@ class EventSensor:
 
 
 class EventReadout:
-    """EventReadout (include/dvs/event_sensor.hpp:24-37): the finite FIFO bus,
-    host side, for event runs merged from several sensors."""
+    """EventReadout (include/dvs/event_sensor.hpp:24-37): the finite FIFO bus
+    for event runs merged from several sensors -- on the host (serial, the
+    reference's structure) or, with device=True, on the GPU (dvs_device_readout_*:
+    radix sort, max-plus scan, device ring buffer; up to max_batch events per submit)."""
 
-    def __init__(self, bandwidth, latency, capacity):
+    def __init__(self, bandwidth, latency, capacity, device=False, max_batch=1 << 20):
         h = C.c_void_p()
-        check(_capi.load().dvs_readout_create(float(bandwidth), float(latency), int(capacity), C.byref(h)))
+        self.fn = "dvs_device_readout_" if device else "dvs_readout_"
+        lib = _capi.load()
+        if device:
+            check(lib.dvs_device_readout_create(float(bandwidth), float(latency), int(capacity), int(max_batch),
+                                                C.byref(h)))
+        else:
+            check(lib.dvs_readout_create(float(bandwidth), float(latency), int(capacity), C.byref(h)))
         self.handle = h
+
+    def _call(self, name, *args):
+        return getattr(_capi.load(), self.fn + name)(self.handle, *args)
 
     def _read(self, n):
         out = np.zeros(max(n, 1), EVENT_DTYPE)
         got = C.c_size_t()
-        check(_capi.load().dvs_readout_read(self.handle, out.ctypes.data, len(out), C.byref(got)))
+        check(self._call("read", out.ctypes.data, len(out), C.byref(got)))
         return out[: got.value].copy()
 
     def submit(self, events, now):
         ev = np.ascontiguousarray(events, EVENT_DTYPE) if len(events) else np.zeros(0, EVENT_DTYPE)
         n = C.c_size_t()
-        check(_capi.load().dvs_readout_submit(self.handle, ev.ctypes.data if len(ev) else None, len(ev), float(now),
-                                              C.byref(n)))
+        check(self._call("submit", ev.ctypes.data if len(ev) else None, len(ev), float(now), C.byref(n)))
         return self._read(n.value)
 
     def drain(self):
         n = C.c_size_t()
-        check(_capi.load().dvs_readout_drain(self.handle, C.byref(n)))
+        check(self._call("drain", C.byref(n)))
         return self._read(n.value)
 
     def dropped(self):
         d, p = C.c_uint64(), C.c_uint64()
-        check(_capi.load().dvs_readout_counters(self.handle, C.byref(d), C.byref(p)))
+        check(self._call("counters", C.byref(d), C.byref(p)))
         return d.value
 
     def peak_queue(self):
         d, p = C.c_uint64(), C.c_uint64()
-        check(_capi.load().dvs_readout_counters(self.handle, C.byref(d), C.byref(p)))
+        check(self._call("counters", C.byref(d), C.byref(p)))
         return p.value
 
     def __del__(self):
         try:
             if getattr(self, "handle", None):
-                _capi.load().dvs_readout_destroy(self.handle)
+                self._call("destroy")
                 self.handle = None
         except Exception:
             pass

@@ -34,6 +34,7 @@ from . import trajectory as T
 from .raycast import EventSensor, interval_array
 
 EVENT_SLAB_BYTES = 8 + 1 + 24   # per pixel and event slot: time, polarity, compacted event
+READOUT_EVENT_BYTES = 2 * 16 + 16 + 24  # per event slot of the device readout: sort keys x2, completions, output
 STATE_BYTES = 5 * 8 + 1 + 48 + 4  # per pixel: FP64 circuit state, reset flag, XORWOW, event count
 RADIANCE_CHUNK_CAP = 512 << 20    # the sensor's largest radiance chunk
 
@@ -80,9 +81,16 @@ class Server:
     resident); hbm_budget: device bytes the admitted jobs may hold."""
 
     def __init__(self, scenes, hbm_budget, horizons_per_step=64, max_active=64, policy="srpt",
-                 fill_samples=1 << 26):
+                 fill_samples=1 << 26, circuit="fp32"):
+        """circuit: the jobs' pixel circuit -- "fp32" (precision mode: FP32
+        receptor arithmetic, FP64 times and root solves; the default, the
+        circuit being what bounds supersample-1 jobs), "fp32-philox" or the
+        reference's "fp64"."""
         if policy not in ("srpt", "fair"):
             raise ValueError("policy must be srpt or fair")
+        if circuit not in ("fp64", "fp32", "fp32-philox"):
+            raise ValueError("circuit must be fp64, fp32 or fp32-philox")
+        self.circuit = circuit
         self.scenes = list(scenes)
         self.budget = int(hbm_budget)
         self.horizons = int(horizons_per_step)
@@ -99,9 +107,13 @@ class Server:
         chunk and batch buffers, and its view's pixel order."""
         n = job.pixels
         cells = self.horizons * max(1, math.ceil(job.time_resolution / job.physic.get("circuit_step", 1e-6) - 1e-9))
-        chunk = min(RADIANCE_CHUNK_CAP, 8 * n * min(2048, cells))
-        return (n * (STATE_BYTES + EVENT_SLAB_BYTES * int(job.physic.get("max_events_per_step", 16)) + 4) + chunk
-                + cells * 256 + (1 << 20))
+        chunk = min(RADIANCE_CHUNK_CAP, (4 if self.circuit != "fp64" else 8) * n * min(2048, cells))
+        slots = int(job.physic.get("max_events_per_step", 16))
+        ring = 0
+        if job.physic.get("readout_bandwidth", 0) > 0:  # the device readout's pending ring (a power of two)
+            ring = 24 * (1 << max(0, int(min(job.physic.get("readout_queue_capacity", 1), 1 << 24)) - 1).bit_length())
+        return (n * (STATE_BYTES + (EVENT_SLAB_BYTES + READOUT_EVENT_BYTES) * slots + 4) + chunk + ring
+                + cells * 256 + (4 << 20))
 
     @staticmethod
     def _cells_per_horizon(job):
@@ -129,7 +141,7 @@ class Server:
 
     def _admit(self, job, now):
         scene = self.scenes[job.terrain].view(job.camera, job.supersample)
-        sensor = EventSensor(scene, job.physic)
+        sensor = EventSensor(scene, job.physic, circuit_precision=self.circuit)
         sensor.initialize(job.path.state(0.0), 0.0)
         reserved = self.estimate_bytes(job)
         a = _Active(job, scene, sensor, reserved)

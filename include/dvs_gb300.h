@@ -105,6 +105,9 @@ typedef struct {
                                  solves (precision mode; no counterpart in the reference); 2: as 1 with
                                  counter-based Philox noise keyed by (seed, pixel, cell index) instead of
                                  the reference's XORWOW stream (native solver only) */
+  int32_t host_readout;       /* 0: the readout FIFO runs on the device (radix sort, max-plus scan of
+                                 completions, pending ring buffer in device memory); 1: on the host,
+                                 serially, as the reference's EventReadout */
 } dvs_sensor_options;
 
 #define DVS_BVH_HALF_BOUNDS 1
@@ -319,6 +322,24 @@ int dvs_readout_drain(dvs_readout *readout, size_t *n_ready);
 int dvs_readout_read(dvs_readout *readout, dvs_event *out, size_t capacity, size_t *n_out);
 int dvs_readout_counters(const dvs_readout *readout, uint64_t *dropped, uint64_t *peak_queue);
 
+/* ---- the same FIFO on the device: EventReadout::submit/drain
+ *      (src/event_readout.cpp:6-34) as a stable radix sort by (t, y, x), a
+ *      max-plus scan of the completions, per-arrival occupancy by binary search
+ *      (a bounded serial pass on the device when the queue fills) and a pending
+ *      ring buffer in device memory.  Sensors use it unless
+ *      dvs_sensor_options.host_readout is set; this handle reads out a host
+ *      array of up to max_batch events per submit.  Order, drops and peak are
+ *      the serial FIFO's; delivery times equal them up to FP64 rounding. ---- */
+typedef struct dvs_device_readout dvs_device_readout;
+int dvs_device_readout_create(double bandwidth, double latency, size_t capacity, size_t max_batch,
+                              dvs_device_readout **out);
+int dvs_device_readout_destroy(dvs_device_readout *readout);
+int dvs_device_readout_submit(dvs_device_readout *readout, const dvs_event *events, size_t n_events, double now,
+                              size_t *n_ready);
+int dvs_device_readout_drain(dvs_device_readout *readout, size_t *n_ready);
+int dvs_device_readout_read(dvs_device_readout *readout, dvs_event *out, size_t capacity, size_t *n_out);
+int dvs_device_readout_counters(const dvs_device_readout *readout, uint64_t *dropped, uint64_t *peak_queue);
+
 /* Traversal packet shape: cells_per_warp 1..32 (power of two; 0 = automatic)
  * and rays_per_lane 1, 2 (the default) or 4 neighbouring sub-rays per lane,
  * used when the pixel's sub-ray count is a multiple of it. */
@@ -327,12 +348,23 @@ typedef struct {
   int32_t cells_per_warp, rays_per_lane;  /* the shape chosen and now set */
   int32_t candidates, cells_timed;        /* shapes timed, circuit cells in the timed launch */
   double best_ms, default_ms;             /* trace time of the chosen shape and of the previous one */
+  int32_t cells_per_chunk;                /* circuit-step chunk chosen and now set (cells per optics launch) */
+  int32_t chunk_candidates, chunk_cells;  /* chunk sizes timed, cells of the timed pipeline */
+  double chunk_best_ms, chunk_default_ms; /* optics + circuit time of the chosen and of the previous chunk */
 } dvs_tuning;
-/* Autotuner: times the trace of a prefix (up to 64 circuit cells) of the next
- * batch (the intervals dvs_sensor_process/enqueue will be given next) over a
- * patch of up to 32768 pixels from the middle of the image, for each packet
- * shape, and sets the fastest.  Runs optics only: no circuit state, RNG or
- * time changes. */
+/* Autotuner, two stages, both on a prefix (up to 64 circuit cells) of the next
+ * batch (the intervals dvs_sensor_process/enqueue will be given next):
+ *  1. packet shape: the trace over a patch of up to 32768 pixels from the
+ *     middle of the image, for each shape (cells per warp 4..32 x 1, 2 or 4
+ *     sub-rays per lane);
+ *  2. circuit-step chunking: the whole optics -> circuit pipeline of every
+ *     pixel with the chosen shape, for chunks of 1, 1/2, 1/4 and 1/8 of the
+ *     prefix (at least 4 cells), on a shadow copy of the circuit state --
+ *     smaller chunks keep the radiance of a launch in L2 for the circuit,
+ *     larger ones launch less.
+ * Each stage keeps the current setting unless another is >= 3 % faster.  No
+ * circuit state, RNG or time changes; not allowed while an enqueued batch
+ * awaits collect. */
 int dvs_sensor_autotune(dvs_sensor *sensor, const dvs_optical_interval *intervals, size_t n_intervals,
                         dvs_tuning *out);
 /* Device memory the sensor holds now (state, RNG, event slabs, radiance

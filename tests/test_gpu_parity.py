@@ -501,6 +501,9 @@ def test_packet_shape_and_autotuner_do_not_change_events():
         if tuned:
             assert tuned["rays_per_lane"] in (1, 2, 4) and tuned["cells_per_warp"] in (4, 8, 16, 32)
             assert tuned["candidates"] >= 4 and tuned["best_ms"] > 0
+            # second stage: the circuit-step chunk over the first 64 cells (64, 32, 16, 8)
+            assert tuned["chunk_cells"] == 64 and tuned["chunk_candidates"] == 4
+            assert tuned["cells_per_chunk"] in (8, 16, 32, 64) and tuned["chunk_best_ms"] > 0
     s = EventSensor(scene, phys)
     with pytest.raises(ValueError):
         s.set_tuning(3, 2)

@@ -29,9 +29,10 @@ class FakeSensor:
     """Advances a clock over the enqueued intervals; one event per batch."""
     instances = []
 
-    def __init__(self, scene, physic):
+    def __init__(self, scene, physic, circuit_precision="fp64"):
         self.scene, self.t, self.batches, self.closed = scene, None, [], False
         self.rays = 0
+        self.circuit = circuit_precision
         FakeSensor.instances.append(self)
 
     def initialize(self, state, t):
