@@ -53,6 +53,14 @@ WORKLOADS = {
     "small": dict(grid=256, seed=20260001, camera=dict(width=346, height=260, fx=300.0, fy=300.0, cx=173.0, cy=130.0),
                   ss=1, z0=1000.0, z1=1000.0, duration=0.49, ground_speed=50.0, sun_elevation=30.0, intensity=1.0,
                   time_resolution=1e-5, batch=64, geometry="reference", circuit="fp64"),
+    # the large config: 8192^2 terrain (134M triangles), 1280x720, 4^2 sub-rays, a 10 s level traverse
+    # 300 m above the highest terrain of its corridor at 80 m/s, sun 5 deg above the horizon (long
+    # shadows, dense events), physic effects and the AER readout on; FP32 receptor arithmetic with
+    # FP64 timestamps and crossing solves
+    "large": dict(grid=8192, seed=20260005, camera=dict(width=1280, height=720, fx=1000.0, fy=1000.0, cx=640.0,
+                                                        cy=360.0),
+                  ss=4, altitude_agl=300.0, duration=10.0, ground_speed=80.0, sun_elevation=5.0, intensity=1000.0,
+                  time_resolution=1e-6, batch=64, geometry="half+watertight", circuit="fp32"),
 }
 HAPKE = dict(b=0.3, c=0.4, hS=0.06, hC=1.0, thetap=0.349066, w=0.25, B_S0=1.0, B_C0=0.0, phi=0.3)
 PHYSIC = dict(threshold_pos=0.2, threshold_neg=0.2, refractory_time=200e-6, readout_bandwidth=5e6,
@@ -67,9 +75,43 @@ METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency v
 # workload and BVH format, measured with ncu's dram__bytes_read.sum and
 # dram__bytes_write.sum on one launch (precision: a 16-cell launch of the
 # FP16-bounds tree, a 4-cell launch of the FP32 one), scaled by the cells traced.
-TRACE_DRAM_BYTES_PER_PIXEL_CELL = {("precision", "half"): (33122816 + 75504384) / (16 * 921600),
-                                   ("precision", "reference"): (32344832 + 1251328) / (4 * 921600),
-                                   ("orbit", "reference"): (22470144 + 407428864) / (640 * 89960)}
+TRACE_DRAM_BYTES_PER_PIXEL_CELL = {}
+# Warp instructions per traced ray (primary + shadow) of trace_cells_kernel, by
+# workload and BVH format: ncu smsp__inst_executed.sum of one launch divided
+# by the rays the sensor counted for it.
+TRACE_WARP_INSTRUCTIONS_PER_RAY = {}
+GB300_SMS = 152
+
+
+def readout_roofline(peak, n_events=1 << 22, batches=4):
+    """The device readout FIFO on a large synthetic batch: n_events events of
+    a 1280x720 sensor within one 64 us batch.  The configs' 5e6 s^-1 bus would
+    saturate and drop at that density (the serial path); an unbounded bus
+    (1e12 s^-1) keeps the parallel path -- radix sort, max-plus scan,
+    occupancy, release.  Device time from CUDA events around the kernels.
+    Algorithmic bytes per event: the event read once and delivered once."""
+    from dvsrender4deepspace_gb300._capi import EVENT_DTYPE
+    from dvsrender4deepspace_gb300.raycast import EventReadout
+    rng = np.random.default_rng(5)
+    r = EventReadout(1e12, 0.0, 1 << 24, device=True, max_batch=n_events)
+    times, t = [], 1.0
+    for b in range(batches + 1):
+        ev = np.zeros(n_events, EVENT_DTYPE)
+        ev["timestamp"] = t + rng.uniform(0.0, 64e-6, n_events)
+        ev["x"] = rng.integers(0, 1280, n_events)
+        ev["y"] = rng.integers(0, 720, n_events)
+        ev["polarity"] = rng.integers(0, 2, n_events)
+        t += 64e-6
+        out = r.submit(ev, t)
+        assert len(out) == n_events
+        if b:  # the first batch warms the kernels and sizes the sort grid
+            times.append(r.last_ms())
+    ms = statistics.median(times)
+    alg = n_events * 2 * 24.0
+    return {"bound": "hbm", "kernel": "device readout (radix sort, max-plus scan, release)",
+            "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / peak,
+            "ms_per_batch": ms, "events_per_batch": n_events, "events_per_s": n_events / (ms / 1e3),
+            "algorithmic_bytes": alg}
 
 
 def dist_env():
@@ -86,7 +128,12 @@ def make_workload(name, rank=0):
     light = trajectory.sun_direction(w["sun_elevation"], 35.0)
     # each rank flies its own job over the same terrain (offset start)
     x0 = -2000.0 + 1000.0 * rank if w["grid"] >= 1024 else 0.0
-    traj = trajectory.Descent((x0, 0.0), w["z0"], w["z1"], w["duration"], w["ground_speed"], light, w["intensity"])
+    z0, z1 = w.get("z0"), w.get("z1")
+    if w.get("altitude_agl"):  # level flight above the highest terrain of the flight corridor (+-300 m)
+        x1 = x0 + w["ground_speed"] * w["duration"]
+        corridor = (V[:, 0] > x0 - 300) & (V[:, 0] < x1 + 300) & (np.abs(V[:, 1]) < 300)
+        z0 = z1 = float(V[corridor, 2].max()) + w["altitude_agl"]
+    traj = trajectory.Descent((x0, 0.0), z0, z1, w["duration"], w["ground_speed"], light, w["intensity"])
     return w, V, N, I, traj
 
 
@@ -216,7 +263,7 @@ def precision_errors(V, N, I, traj, w, scene, geometry, circuit, budget_pixels=2
     out["depth"] = {"pixels": int(hit.sum()), "max_rel": float(drel[hit].max()),
                     "p99_rel": float(np.quantile(drel[hit], .99)), "above_1e-5": int((drel > 1e-5).sum()),
                     "non_margin_above_1e-5": int(((drel > 1e-5) & plain).sum()),
-                    "misses_agree_non_margin": bool(np.all((g_dep < 0) == (odep < 0) | ~plain))}
+                    "misses_agree_non_margin": bool(np.all(((g_dep < 0) == (odep < 0)) | ~plain))}
     # events: a 16x12 crop at the image centre, 0.5 ms light pulse (500 cells of 1 us)
     x0, y0 = cam["width"] // 2 - 8, cam["height"] // 2 - 6
     crop = dict(cam, width=16, height=12, cx=cam["cx"] - x0, cy=cam["cy"] - y0)
@@ -268,7 +315,7 @@ def bench_config(args, w, n_triangles, world):
             "shot_noise": "philox" if args.circuit == "fp32-philox" else "curand_xorwow",
             "sun_elevation_deg": w["sun_elevation"], "intensity": w["intensity"],
             "l2": "inputs larger than L2 (129 MB): the triangle and shading records alone are %.2f GB"
-                  % (n_triangles * 112 / 1e9),
+                  % (n_triangles * (48 * (3 if GEOMETRY[args.geometry] & 2 else 1) + 64) / 1e9),
             "parallelism": "dp%d (independent jobs)" % world, "geometry": args.geometry,
             "circuit_precision": args.circuit}
 
@@ -424,10 +471,12 @@ def run_gb300(args):
     n_pix = w["camera"]["width"] * w["camera"]["height"]
     optics_ms = st["optics_ms"] / max(1, st["optics_launches"])
     # dominant kernel: trace_cells (optics).  Algorithmic bytes per launch: the
-    # per-pixel-cell radiance it must write (8 B) -- the HBM-minimal traffic of
-    # a latency/ALU-bound traversal (the scene is read from L1/L2).
+    # per-pixel-cell radiance it must write (4 B float for the FP32 circuits,
+    # 8 B double for the FP64 one) -- the HBM-minimal traffic of an
+    # issue-bound traversal (the scene is read from L1/L2).
     cells_per_launch = st["circuit_cells"] / max(1, st["circuit_launches"]) / max(1, n_pix)
-    alg_bytes = n_pix * cells_per_launch * 8.0
+    chunk_bytes = 8.0 if args.circuit == "fp64" else 4.0
+    alg_bytes = n_pix * cells_per_launch * chunk_bytes
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -436,7 +485,27 @@ def run_gb300(args):
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / (optics_ms / 1e3) / 1e9 if optics_ms > 0 else None
     circuit_ms = st["circuit_ms"] / max(1, st["circuit_launches"])
-    circuit_bytes = n_pix * cells_per_launch * 8.0 + n_pix * (5 * 8 + 1 + 48) * 2 + n_pix * 4 * 2
+    # circuit bytes per launch, as each mode moves them: the radiance chunk, the
+    # state round trip (five FP64 fields and the reset flag; the XORWOW states
+    # only when a stream is drawn: Philox keeps none), the per-pixel event count
+    xorwow = args.circuit != "fp32-philox" and (PHYSIC["photon_shot_noise"] or PHYSIC["reset_thermal_noise"])
+    state_bytes = 5 * 8 + 1 + (48 if xorwow else 0)
+    circuit_bytes = n_pix * cells_per_launch * chunk_bytes + n_pix * state_bytes * 2 + n_pix * 4 * 2
+    # the trace kernel is issue-bound: its roofline is the SMs' instruction issue
+    # rate (4 warp instructions per clock per SM), from the warp instructions
+    # per ray that ncu counted for this kernel and format, at the sampled clock
+    rays_per_launch = rays / max(1, st["optics_launches"])
+    issue = None
+    ipr = TRACE_WARP_INSTRUCTIONS_PER_RAY.get((args.workload, args.geometry))
+    sm_mhz = clocks.summary()["sm_mhz"]
+    if ipr and optics_ms > 0 and sm_mhz:
+        issue_peak = GB300_SMS * 4 * sm_mhz * 1e6
+        issue_achieved = ipr * rays_per_launch / (optics_ms / 1e3)
+        issue = {"bound": "issue", "kernel": "trace_cells_kernel", "achieved": issue_achieved / 1e12,
+                 "peak": issue_peak / 1e12, "unit": "T warp-instructions/s", "frac": issue_achieved / issue_peak,
+                 "warp_instructions_per_ray": ipr, "sm_mhz": sm_mhz,
+                 "note": "issue rate of %d SMs x 4 schedulers at the sampled clock; instructions per ray from "
+                         "ncu smsp__inst_executed.sum of this kernel and format" % GB300_SMS}
     cb = None
     o64 = None
     if not args.no_cpu_baseline:
@@ -451,7 +520,7 @@ def run_gb300(args):
         cb["fp64_oracle"] = {"value": cb64["value"], "unit": cb64["unit"], "cores": cb64["cores"],
                              "sample": cb64["sample"]}
     errors = None
-    if args.workload == "precision" and not args.no_precision_report and rank == 0:
+    if args.workload in ("precision", "large") and not args.no_precision_report and rank == 0:
         errors = precision_errors(V, N, I, traj, w, scene, args.geometry, args.circuit, o64=o64)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
@@ -478,10 +547,13 @@ def run_gb300(args):
                                  if (args.workload, args.geometry) in TRACE_DRAM_BYTES_PER_PIXEL_CELL else None),
                      "algorithmic_bytes": alg_bytes,
                      "peak_source": "measured" if peaks else "fallback",
-                     "note": "traversal is L1-broadcast/ALU bound; bytes = radiance written per launch"},
+                     "note": "traversal is instruction-issue bound (roofline_issue); bytes = radiance written "
+                             "per launch"},
+        "roofline_issue": issue,
         "roofline_circuit": {"bound": "hbm", "kernel": "circuit_kernel",
                              "achieved": circuit_bytes / (circuit_ms / 1e3) / 1e9 if circuit_ms > 0 else None,
-                             "peak": peak, "unit": "GB/s"},
+                             "peak": peak, "unit": "GB/s", "algorithmic_bytes": circuit_bytes},
+        "roofline_readout": readout_roofline(peak) if not args.no_readout_leg else None,
         "clocks": clocks.summary(), "setup_s": setup_s, "bvh_build_s": info["build_seconds"], "tuning": tuning,
         "adaptive": adaptive,
         "cpu_baseline": cb,
@@ -611,17 +683,17 @@ def run_batching(args):
     K, Wm = args.steps, args.warmup
     active_steps = [int(math.ceil(frames / 400.0 * K)) for _, frames in members]
 
-    def make(view):
+    def make(view, count):
         sensors = []
-        for traj, _ in members:
+        for traj, _ in members[:count]:
             s = EventSensor(view, PHYSIC, cells_per_warp=args.cw, circuit_precision=args.circuit)
             s.initialize(traj.state(0.0), 0.0)
             sensors.append(s)
         return sensors
 
-    def plan(step, cursors, timed, horizons):
+    def plan(step, cursors, timed, horizons, count):
         rows = []
-        for m, (traj, _) in enumerate(members):
+        for m, (traj, _) in enumerate(members[:count]):
             if timed and step >= active_steps[m]:
                 rows.append([])
                 continue
@@ -636,14 +708,15 @@ def run_batching(args):
     def events_of(sensors):
         return sum(s.stats()["events_delivered"] for s in sensors)
 
-    def measure(view, horizons):
+    def measure(view, horizons, count=None):
+        count = count or len(members)
         results = {}
         for mode in ("batch", "loop"):
-            sensors = make(view)
+            sensors = make(view, count)
             batch = SensorBatch(sensors) if mode == "batch" else None
-            cursors = [0.0] * len(members)
+            cursors = [0.0] * count
             for k in range(Wm):
-                rows = plan(k, cursors, False, horizons)
+                rows = plan(k, cursors, False, horizons, count)
                 if batch:
                     batch.process(rows)
                 else:
@@ -652,7 +725,7 @@ def run_batching(args):
             rays0, ev0 = rays_of(sensors), events_of(sensors)
             st0 = batch.stats() if batch else None
             # the timed steps' intervals, generated beforehand (host Python, not the path)
-            timed_rows = [plan(k, cursors, True, horizons) for k in range(K)]
+            timed_rows = [plan(k, cursors, True, horizons, count) for k in range(K)]
             if world > 1:
                 torch.distributed.barrier()
             with ClockSampler(local) as clocks:  # started before and stopped after the timed region
@@ -695,6 +768,11 @@ def run_batching(args):
     # one graph per step replace per-member launches and synchronisations
     small_cam = dict(width=64, height=48, fx=60.0, fy=60.0, cx=32.0, cy=24.0)
     small = measure(base.view(small_cam, 1), 64) if args.batch_small else None
+    # members at the 1280x720 config's camera and 16^2 sub-rays (4 trajectories, 4 horizons a step):
+    # each member's step already fills the GPU, so this is where batching has nothing to add
+    prec_cam = WORKLOADS["precision"]["camera"]
+    prec = (measure(base.view(prec_cam, WORKLOADS["precision"]["ss"]), 4, count=args.batch_precision_members)
+            if args.batch_precision_members > 0 else None)
     b, l = results["batch"], results["loop"]
     vals = torch.tensor([b["device_ms"], b["wall_s"], b["rays"], l["wall_s"], l["rays"], b["events"]],
                         dtype=torch.float64, device="cuda")
@@ -738,6 +816,12 @@ def run_batching(args):
                 "per_sensor_loop": small["loop"],
                 "batch_vs_loop_wall": small["batch"]["mrays_per_s_wall"] / max(1e-9, small["loop"]["mrays_per_s_wall"]),
                 "events_batch_vs_loop": small["batch"]["events_per_s"] / max(1e-9, small["loop"]["events_per_s"])},
+            "precision_members": None if prec is None else {
+                "camera": "1280x720", "supersample": WORKLOADS["precision"]["ss"], "members": args.batch_precision_members,
+                "horizons_per_step": 4, "batch": prec["batch"], "per_sensor_loop": prec["loop"],
+                "batch_vs_loop_wall": prec["batch"]["mrays_per_s_wall"] / max(1e-9, prec["loop"]["mrays_per_s_wall"]),
+                "events_batch_vs_loop": prec["batch"]["events_per_s"] / max(1e-9, prec["loop"]["events_per_s"]),
+                "target_events_vs_plain": 5.0},
             "batch_vs_loop_wall": (b_rays / b_wall) / max(1e-9, l_rays / l_wall),
             "gpu_launches": int(2 * K + 3 * n_launch),
             "clocks": results["batch"]["clocks"], "setup_s": setup_s, "cpu_baseline": cb}
@@ -754,6 +838,8 @@ def main():
     ap.add_argument("--workload", default="precision", choices=sorted(WORKLOADS) + ["serving", "batching"])
     ap.add_argument("--batch-members", type=int, default=64)
     ap.add_argument("--batch-horizons", type=int, default=16, help="horizons per member per batching step")
+    ap.add_argument("--batch-precision-members", type=int, default=4,
+                    help="members at the 1280x720 config's camera and sub-rays (0: skip that leg)")
     ap.add_argument("--no-batch-small", dest="batch_small", action="store_false",
                     help="skip the batching workload's small-member leg (64x48, one sub-ray)")
     ap.add_argument("--serving-jobs", type=int, default=48)
@@ -764,6 +850,7 @@ def main():
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--cw", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-readout-leg", action="store_true", help="skip the device readout's large-batch leg")
     ap.add_argument("--no-precision-report", action="store_true",
                     help="skip the precision workload's error report against the FP64 oracle")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",

@@ -107,7 +107,8 @@ EXPORTS = ("dvs_last_error", "dvs_version", "dvs_sensor_options_default", "dvs_d
            "dvs_scene_view_create", "dvs_sensor_device_bytes", "dvs_sensor_set_tuning", "dvs_sensor_autotune",
            "dvs_batch_create", "dvs_batch_destroy", "dvs_batch_process", "dvs_batch_stats_get", "dvs_noise_poisson",
            "dvs_device_readout_create", "dvs_device_readout_destroy", "dvs_device_readout_submit",
-           "dvs_device_readout_drain", "dvs_device_readout_read", "dvs_device_readout_counters")
+           "dvs_device_readout_drain", "dvs_device_readout_read", "dvs_device_readout_counters",
+           "dvs_device_readout_last_ms")
 
 
 class Tuning(C.Structure):
@@ -198,6 +199,7 @@ def _declare(lib):
     lib.dvs_device_readout_drain.argtypes = [vp, C.POINTER(sz)]
     lib.dvs_device_readout_read.argtypes = [vp, vp, sz, C.POINTER(sz)]
     lib.dvs_device_readout_counters.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    lib.dvs_device_readout_last_ms.argtypes = [vp, C.POINTER(C.c_double)]
     lib.dvs_config_load.argtypes = [C.c_char_p, C.POINTER(Camera), C.POINTER(Physic), C.POINTER(Hapke),
                                     C.POINTER(SceneConfig)]
     lib.dvs_frames_load.argtypes = [C.c_char_p, vp, sz, C.POINTER(sz)]

@@ -1093,11 +1093,12 @@ static int enqueue(dvs_sensor *s, const dvs_optical_interval *ivs, size_t count)
                               s->stream),
            "event depth");
   if (s->dro) {  // the readout FIFO on the device, after the event depths
+    record_timer(s, 3);
     CUDA_TRY(s->dro->submit(s->events, s->event_total, s->error_word, &s->ivs[count - 1].t1, s->stream),
              "device readout");
     s->stats.launches += s->dro->launches();
   }
-  record_timer(s, 3);
+  record_timer(s, 4);
   s->stats.launches += 2;
   s->last_time = ivs[count - 1].t1;
   return DVS_OK;
@@ -1112,6 +1113,7 @@ static void collect_timers(dvs_sensor *s) {
       case 0: s->stats.optics_ms += ms; break;
       case 1: s->stats.circuit_ms += ms; break;
       case 2: s->stats.events_ms += ms; break;
+      case 3: s->stats.readout_ms += ms; break;  // the device readout
       default: break;
     }
   }
@@ -1161,7 +1163,6 @@ static int collect(dvs_sensor *s, double end, size_t *n_ready) {
     s->dro->observed((size_t)count);
     s->stats.events_generated += (uint64_t)count;
     s->stats.events_delivered += s->ready.size() - before;
-    s->stats.readout_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (n_ready) *n_ready = s->ready.size() - s->ready_head;
     return DVS_OK;
   }
@@ -1405,11 +1406,12 @@ int dvs_sensor_process_adaptive(dvs_sensor *s, const dvs_optical_interval *ivs, 
                               s->slab_t, s->slab_p, s->events, s->event_total, s->stream),
            "compact events");
   if (s->dro) {
+    record_timer(s, 3);
     CUDA_TRY(s->dro->submit(s->events, s->event_total, s->error_word, &s->ivs[count - 1].t1, s->stream),
              "device readout");
     s->stats.launches += s->dro->launches();
   }
-  record_timer(s, 3);
+  record_timer(s, 4);
   s->stats.launches += 2;
   s->last_time = end;
   if (accepted) *accepted = 1;
@@ -2141,6 +2143,8 @@ struct dvs_device_readout {
   double *d_now = nullptr, *h_now = nullptr;
   std::vector<HostEvent> ready;
   size_t head = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;  // around the kernels of the last submit
+  float last_ms = 0;
 };
 
 namespace {
@@ -2179,6 +2183,8 @@ int dvs_device_readout_create(double bandwidth, double latency, size_t capacity,
   cudaGetDevice(&r->device);
   const size_t out_cap = r->dro.next_pow2(std::min<size_t>(capacity, size_t(1) << 24)) + max_batch;
   cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&r->e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&r->e1);
   if (e == cudaSuccess) e = r->dro.create(bandwidth, latency, capacity, max_batch, r->stream);
   if (e == cudaSuccess) e = cudaMalloc(&r->d_in, sizeof(DevEvent) * max_batch + 64);
   if (e == cudaSuccess) e = cudaMallocHost(&r->h_in, sizeof(DevEvent) * max_batch + 64);
@@ -2204,6 +2210,8 @@ int dvs_device_readout_destroy(dvs_device_readout *r) {
   cudaFree(r->d_in);
   if (r->h_in) cudaFreeHost(r->h_in);
   if (r->h_out) cudaFreeHost(r->h_out);
+  if (r->e0) cudaEventDestroy(r->e0);
+  if (r->e1) cudaEventDestroy(r->e1);
   if (r->stream) cudaStreamDestroy(r->stream);
   delete r;
   return DVS_OK;
@@ -2230,9 +2238,12 @@ int dvs_device_readout_submit(dvs_device_readout *r, const dvs_event *events, si
   if (n) CUDA_TRY(cudaMemcpyAsync(r->d_in, r->h_in, sizeof(DevEvent) * n, cudaMemcpyHostToDevice, r->stream),
                   "upload events");
   CUDA_TRY(cudaMemcpyAsync(r->d_count, r->h_count, 16, cudaMemcpyHostToDevice, r->stream), "upload count and time");
+  CUDA_TRY(cudaEventRecord(r->e0, r->stream), "device readout timer");
   CUDA_TRY(r->dro.submit(r->d_in, r->d_count, nullptr, r->d_now, r->stream), "device readout");
+  CUDA_TRY(cudaEventRecord(r->e1, r->stream), "device readout timer");
   int rc = device_readout_fetch(r);
   if (rc) return rc;
+  CUDA_TRY(cudaEventElapsedTime(&r->last_ms, r->e0, r->e1), "device readout timer");
   r->dro.observed(n);
   *n_ready = r->ready.size() - r->head;
   return DVS_OK;
@@ -2269,6 +2280,12 @@ int dvs_device_readout_counters(const dvs_device_readout *r, uint64_t *dropped, 
   if (!r) return fail(DVS_ERR_INVALID, "null argument");
   if (dropped) *dropped = r->dro.h_counters[0];
   if (peak_queue) *peak_queue = r->dro.h_counters[1];
+  return DVS_OK;
+}
+
+int dvs_device_readout_last_ms(const dvs_device_readout *r, double *ms) {
+  if (!r || !ms) return fail(DVS_ERR_INVALID, "null argument");
+  *ms = r->last_ms;
   return DVS_OK;
 }
 

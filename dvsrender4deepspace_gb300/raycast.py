@@ -346,6 +346,12 @@ class EventReadout:
         check(self._call("counters", C.byref(d), C.byref(p)))
         return p.value
 
+    def last_ms(self):
+        """Device time of the last submit's kernels (device readout only)."""
+        ms = C.c_double()
+        check(_capi.load().dvs_device_readout_last_ms(self.handle, C.byref(ms)))
+        return ms.value
+
     def __del__(self):
         try:
             if getattr(self, "handle", None):

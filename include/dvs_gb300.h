@@ -139,7 +139,9 @@ typedef struct {
   uint64_t dropped, peak_queue;            /* readout FIFO (EventReadout::dropped/peak_queue) */
   uint64_t circuit_cells;                  /* pixel x cell integrations */
   uint64_t launches;                       /* kernels launched by this handle */
-  double optics_ms, circuit_ms, events_ms, readout_ms; /* with options.timing */
+  double optics_ms, circuit_ms, events_ms;  /* device time of the kernels (options.timing) */
+  double readout_ms;                        /* device time of the device readout (options.timing), or host
+                                               time of the host readout */
   uint64_t optics_launches, circuit_launches;
 } dvs_sensor_stats;
 
@@ -339,6 +341,8 @@ int dvs_device_readout_submit(dvs_device_readout *readout, const dvs_event *even
 int dvs_device_readout_drain(dvs_device_readout *readout, size_t *n_ready);
 int dvs_device_readout_read(dvs_device_readout *readout, dvs_event *out, size_t capacity, size_t *n_out);
 int dvs_device_readout_counters(const dvs_device_readout *readout, uint64_t *dropped, uint64_t *peak_queue);
+/* Device time of the last submit's kernels (CUDA events on the handle's stream). */
+int dvs_device_readout_last_ms(const dvs_device_readout *readout, double *ms);
 
 /* Traversal packet shape: cells_per_warp 1..32 (power of two; 0 = automatic)
  * and rays_per_lane 1, 2 (the default) or 4 neighbouring sub-rays per lane,

