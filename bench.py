@@ -35,6 +35,9 @@ sys.path.insert(0, ROOT)
 
 # dvs_bvh_params.precision flags: 1 = FP16 child bounds, 2 = watertight triangle test
 GEOMETRY = {"reference": 0, "half": 1, "watertight": 2, "half+watertight": 3}
+# dvs_bvh_params.builder
+BUILDERS = {"morton": 0, "sah": 1}
+BUILDERS_TEXT = {0: "Morton radix splits", 1: "binned SAH splits"}
 
 WORKLOADS = {
     # configs: precision (1280x720), small (346x260 DAVIS, plain method)
@@ -42,8 +45,9 @@ WORKLOADS = {
                                                             cy=360.0),
                       ss=16, z0=3000.0, z1=500.0, duration=2.0, ground_speed=80.0, sun_elevation=30.0,
                       intensity=1000.0, time_resolution=1e-6, batch=64,
-                      # the config's BVH: quantised FP16 child bounds (FP32 triangle tests); Philox noise
-                      geometry="half", circuit="fp32-philox"),
+                      # precision traversal: quantised FP16 child bounds and the watertight FP32 triangle
+                      # test; FP32 receptor arithmetic with Philox noise
+                      geometry="half+watertight", circuit="fp32-philox"),
     # one trajectory of the batching config: 1024^2 terrain (2.09M triangles), ss 4, 10 us horizons
     "orbit": dict(grid=1024, seed=20260002, camera=dict(width=346, height=260, fx=300.0, fy=300.0, cx=173.0,
                                                         cy=130.0),
@@ -317,7 +321,7 @@ def bench_config(args, w, n_triangles, world):
             "l2": "inputs larger than L2 (129 MB): the triangle and shading records alone are %.2f GB"
                   % (n_triangles * (48 * (3 if GEOMETRY[args.geometry] & 2 else 1) + 64) / 1e9),
             "parallelism": "dp%d (independent jobs)" % world, "geometry": args.geometry,
-            "circuit_precision": args.circuit}
+            "bvh_builder": args.builder, "circuit_precision": args.circuit}
 
 
 def run_reference(args):
@@ -364,7 +368,7 @@ def run_gb300(args):
     w, V, N, I, traj = make_workload(args.workload, rank)
     t_setup = time.time()
     scene = DeviceScene(V, N, I, w["camera"], w["ss"], HAPKE, leaf_size=args.leaf,
-                        geometry=GEOMETRY[args.geometry])
+                        geometry=GEOMETRY[args.geometry], builder=BUILDERS[args.builder])
     info = scene.info()
     sensor = EventSensor(scene, PHYSIC, timing=True, cells_per_chunk=args.chunk, cells_per_warp=args.cw,
                          circuit_precision=args.circuit)
@@ -528,7 +532,9 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": bench_config(args, w, len(I), world),
         "scene": {"device_gb": info["device_bytes"] / 1e9,
-                  "bvh": "8-wide Morton radix, leaf %d, depth %d" % (info["leaf_size"], info["depth"])},
+                  "bvh": "8-wide, %s, leaf %d, depth %d" % (BUILDERS_TEXT[info["builder"]], info["leaf_size"],
+                                                            info["depth"]),
+                  "sah_node_visits": info["sah_node_visits"], "sah_triangle_tests": info["sah_triangle_tests"]},
         "rays_per_step": rays / args.steps,
         "rays": {"primary_per_step": st["primary_rays"] / args.steps, "shadow_per_step": st["shadow_rays"] / args.steps,
                  "primary_mrays_s": st["primary_rays"] / (dev_ms / 1e3) / 1e6 if world == 1 else None,
@@ -676,7 +682,8 @@ def run_batching(args):
     light = trajectory.sun_direction(w["sun_elevation"], 35.0)
     members = batching_members(args.batch_members, 20260005 + rank, light, w["intensity"])
     t_setup = time.time()
-    base = DeviceScene(V, N, I, w["camera"], w["ss"], HAPKE, leaf_size=args.leaf, geometry=GEOMETRY[args.geometry])
+    base = DeviceScene(V, N, I, w["camera"], w["ss"], HAPKE, leaf_size=args.leaf, geometry=GEOMETRY[args.geometry],
+                       builder=BUILDERS[args.builder])
     info = base.info()
     setup_s = time.time() - t_setup
     dt, H = w["time_resolution"], args.batch_horizons
@@ -845,6 +852,8 @@ def main():
     ap.add_argument("--serving-jobs", type=int, default=48)
     ap.add_argument("--serving-scale", type=float, default=0.01)
     ap.add_argument("--leaf", type=int, default=0)
+    ap.add_argument("--builder", default="morton", choices=sorted(BUILDERS),
+                    help="split rule of the BVH: Morton radix splits or binned SAH splits")
     ap.add_argument("--geometry", default=None, choices=sorted(GEOMETRY),
                     help="BVH format: FP32 or FP16 (half) child bounds; Moller-Trumbore or watertight triangles")
     ap.add_argument("--chunk", type=int, default=0)

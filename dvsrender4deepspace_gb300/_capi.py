@@ -65,13 +65,14 @@ class SensorOptions(C.Structure):
 
 
 class BvhParams(C.Structure):
-    _fields_ = [("leaf_size", C.c_int32), ("precision", C.c_int32), ("reserved", C.c_int32 * 2)]
+    _fields_ = [("leaf_size", C.c_int32), ("precision", C.c_int32), ("builder", C.c_int32), ("reserved", C.c_int32)]
 
 
 class SceneInfo(C.Structure):
     _fields_ = [("triangles", C.c_uint64), ("vertices", C.c_uint64), ("nodes", C.c_uint64), ("depth", C.c_int32),
                 ("root", C.c_int32), ("device_bytes", C.c_uint64), ("build_seconds", C.c_double),
-                ("leaf_size", C.c_int32), ("precision", C.c_int32)]
+                ("leaf_size", C.c_int32), ("precision", C.c_int32), ("builder", C.c_int32),
+                ("reserved", C.c_int32), ("sah_node_visits", C.c_double), ("sah_triangle_tests", C.c_double)]
 
 
 class BatchStats(C.Structure):

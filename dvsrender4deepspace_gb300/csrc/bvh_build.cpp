@@ -9,7 +9,10 @@
 //      binary tree over contiguous leaf ranges (<= leaf_size triangles);
 //   4. collapse to 8-wide nodes by repeatedly opening the largest-area inner
 //      child; nodes are numbered breadth-first so the top levels are first.
-// All passes are O(n) or O(n log n) and OpenMP-parallel.
+// All passes are O(n) or O(n log n) and OpenMP-parallel.  Builder 1 replaces
+// the Morton steps 2-3 by binned SAH splits with the reference's criterion
+// (SahBuilder) and shares step 4, so the two trees differ only in where they
+// split; both report the surface-area model of the wide tree.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -173,14 +176,193 @@ struct TreeBuilder {
   }
 };
 
+// ---- binned SAH splits (builder 1) -------------------------------------------------
+// The reference's split criterion (src/bvh/bining.cpp:9-103): over the
+// centroid bounds of a range, min(32, 4 + 0.05 n) bins per axis; each
+// triangle's box grows the bin of its centroid; at every bin boundary of the
+// three axes the cost area(left) * n_left + area(right) * n_right, the least
+// taken (first axis, then first boundary, on ties).  Unlike the reference a
+// range is always split down to leaf_size triangles: the leaves here have a
+// fixed maximum size and the 8-wide collapse sets the node layout.  A range
+// whose centroids share one bin on every axis is halved by index.  Large
+// ranges scan their references in parallel chunks; subtrees of more than
+// 32768 triangles are OpenMP tasks.
+struct SahRef {
+  Box box;
+  float c[3];
+  uint32_t id;
+};
+constexpr int kSahBins = 32;
+
+struct SahBuilder {
+  std::vector<SahRef> &refs;
+  std::vector<BinNode> &nodes;
+  std::atomic<int32_t> next{0};
+  int leaf_size;
+
+  static int chunks_for(int32_t n) { return n > (1 << 20) ? std::max(1, std::min(4 * thread_count(), n >> 18)) : 1; }
+  static int32_t chunk_begin(int32_t b, int32_t n, int k, int chunks) {
+    return b + (int32_t)((int64_t)n * k / chunks);
+  }
+  static int bin_of(float c, float lo, float scale, int nb) {
+    const int j = (int)((c - lo) * scale);
+    return std::min(std::max(j, 0), nb - 1);
+  }
+
+  // box of the range and bounds of its centroids
+  void bounds(int32_t b, int32_t e, Box &range, Box &cent) {
+    const int32_t n = e - b;
+    const int chunks = chunks_for(n);
+    std::vector<Box> pr(chunks), pc(chunks);
+    for (int k = 0; k < chunks; ++k) {
+#pragma omp task shared(pr, pc) firstprivate(k) if (chunks > 1)
+      {
+        Box r = empty_box(), c = empty_box();
+        for (int32_t i = chunk_begin(b, n, k, chunks), ie = chunk_begin(b, n, k + 1, chunks); i < ie; ++i) {
+          grow(r, refs[i].box);
+          for (int d = 0; d < 3; ++d) {
+            c.lo[d] = std::min(c.lo[d], refs[i].c[d]);
+            c.hi[d] = std::max(c.hi[d], refs[i].c[d]);
+          }
+        }
+        pr[k] = r;
+        pc[k] = c;
+      }
+    }
+#pragma omp taskwait
+    range = cent = empty_box();
+    for (int k = 0; k < chunks; ++k) {
+      grow(range, pr[k]);
+      grow(cent, pc[k]);
+    }
+  }
+
+  struct Bins {
+    Box box[3][kSahBins];
+    int32_t count[3][kSahBins];
+    void clear() {
+      for (int d = 0; d < 3; ++d)
+        for (int j = 0; j < kSahBins; ++j) {
+          box[d][j] = empty_box();
+          count[d][j] = 0;
+        }
+    }
+  };
+
+  int32_t build(int32_t b, int32_t e) {
+    const int32_t id = next.fetch_add(1);
+    const int32_t n = e - b;
+    Box range, cent;
+    bounds(b, e, range, cent);
+    if (n <= leaf_size) {
+      BinNode &leaf = nodes[id];
+      leaf.box = range;
+      leaf.left = leaf.right = -1;
+      leaf.start = b;
+      leaf.count = n;
+      leaf.area = half_area(range);
+      return id;
+    }
+    const int nb = std::min(kSahBins, (int)(4.0f + 0.05f * (float)n));
+    float scale[3];
+    for (int d = 0; d < 3; ++d) {
+      const float extent = cent.hi[d] - cent.lo[d];
+      scale[d] = extent > 0 ? (float)nb / extent : 0.0f;
+    }
+    // bin the range (chunks in parallel for large ranges)
+    const int chunks = chunks_for(n);
+    std::vector<Bins> part(chunks);
+    for (int k = 0; k < chunks; ++k) {
+#pragma omp task shared(part, scale, cent) firstprivate(k) if (chunks > 1)
+      {
+        Bins &p = part[k];
+        p.clear();
+        for (int32_t i = chunk_begin(b, n, k, chunks), ie = chunk_begin(b, n, k + 1, chunks); i < ie; ++i)
+          for (int d = 0; d < 3; ++d) {
+            const int j = bin_of(refs[i].c[d], cent.lo[d], scale[d], nb);
+            grow(p.box[d][j], refs[i].box);
+            ++p.count[d][j];
+          }
+      }
+    }
+#pragma omp taskwait
+    Bins &bins = part[0];
+    for (int k = 1; k < chunks; ++k)
+      for (int d = 0; d < 3; ++d)
+        for (int j = 0; j < nb; ++j) {
+          grow(bins.box[d][j], part[k].box[d][j]);
+          bins.count[d][j] += part[k].count[d][j];
+        }
+    // sweep every boundary of every axis
+    float best = std::numeric_limits<float>::infinity();
+    int best_d = -1, best_j = 0;
+    for (int d = 0; d < 3; ++d) {
+      Box right[kSahBins];
+      int32_t right_n[kSahBins];
+      Box acc = empty_box();
+      int32_t acc_n = 0;
+      for (int j = nb - 1; j >= 0; --j) {
+        grow(acc, bins.box[d][j]);
+        acc_n += bins.count[d][j];
+        right[j] = acc;
+        right_n[j] = acc_n;
+      }
+      Box left = empty_box();
+      int32_t left_n = 0;
+      for (int j = 1; j < nb; ++j) {
+        grow(left, bins.box[d][j - 1]);
+        left_n += bins.count[d][j - 1];
+        if (left_n == 0 || right_n[j] == 0) continue;
+        const float cost = half_area(left) * (float)left_n + half_area(right[j]) * (float)right_n[j];
+        if (cost < best) {
+          best = cost;
+          best_d = d;
+          best_j = j;
+        }
+      }
+    }
+    int32_t m;
+    if (best_d >= 0) {
+      // the same bin_of as the binning pass, so the split has the swept counts
+      const int d = best_d;
+      const float lo = cent.lo[d], sc = scale[d];
+      m = (int32_t)(std::partition(refs.begin() + b, refs.begin() + e,
+                                   [&](const SahRef &r) { return bin_of(r.c[d], lo, sc, nb) < best_j; }) -
+                    refs.begin());
+    } else {
+      m = b + n / 2;  // every centroid in one bin on every axis
+    }
+    int32_t l, r;
+    if (n > 32768) {
+#pragma omp task shared(l)
+      l = build(b, m);
+#pragma omp task shared(r)
+      r = build(m, e);
+#pragma omp taskwait
+    } else {
+      l = build(b, m);
+      r = build(m, e);
+    }
+    BinNode &nn = nodes[id];
+    nn.box = range;
+    nn.left = l;
+    nn.right = r;
+    nn.start = 0;
+    nn.count = 0;
+    nn.area = half_area(range);
+    return id;
+  }
+};
+
 }  // namespace
 
-bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf_size, BvhBuild &out,
-                std::string &error) {
+bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf_size, int builder, BvhBuild &out,
+               std::string &error) {
   const auto t_start = std::chrono::steady_clock::now();
   if (nt == 0 || nv == 0) { error = "empty mesh"; return false; }
   if (nt > (size_t(1) << 28)) { error = "mesh exceeds 2^28 triangles"; return false; }
   if (leaf_size < 1 || leaf_size > 8) { error = "leaf_size must be 1..8"; return false; }
+  if (builder != 0 && builder != 1) { error = "BVH builder must be 0 (Morton radix) or 1 (binned SAH)"; return false; }
   for (size_t i = 0; i < 3 * nt; ++i)
     if (I[i] >= nv) { error = "mesh triangle index outside vertex array"; return false; }
 
@@ -206,39 +388,58 @@ bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf
 #pragma omp critical
     grow(scene, local);
   }
-  float extent = std::max({scene.hi[0] - scene.lo[0], scene.hi[1] - scene.lo[1], scene.hi[2] - scene.lo[2]});
-  if (!(extent > 0) || !std::isfinite(extent)) extent = 1.0f;
-  const double scale = double((1u << 21) - 1) / double(extent);
-  std::vector<uint64_t> codes(nt);
   std::vector<uint32_t> order(nt);
-#pragma omp parallel for schedule(static)
-  for (long long i = 0; i < ntl; ++i) {
-    uint64_t q[3];
-    for (int d = 0; d < 3; ++d) {
-      double c = 0.5 * (double(boxes[i].lo[d]) + double(boxes[i].hi[d]));
-      double v = (c - scene.lo[d]) * scale;
-      v = std::min(std::max(v, 0.0), double((1u << 21) - 1));
-      q[d] = uint64_t(v);
-    }
-    codes[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
-    order[i] = uint32_t(i);
-  }
-
-  // 2. sort
-  radix_sort(codes, order);
-  std::vector<Box> sorted_boxes(nt);
-#pragma omp parallel for schedule(static)
-  for (long long i = 0; i < ntl; ++i) sorted_boxes[i] = boxes[order[i]];
-  std::vector<Box>().swap(boxes);
-
-  // 3. binary radix tree
   std::vector<BinNode> bin(2 * nt + 1);
-  TreeBuilder tb{codes, sorted_boxes, bin, {}, leaf_size};
   int32_t root = 0;
+  if (builder == 1) {
+    // 2-3. binned SAH splits over the triangles' boxes and centroids
+    std::vector<SahRef> refs(nt);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < ntl; ++i) {
+      refs[i].box = boxes[i];
+      for (int d = 0; d < 3; ++d) refs[i].c[d] = 0.5f * (boxes[i].lo[d] + boxes[i].hi[d]);
+      refs[i].id = uint32_t(i);
+    }
+    std::vector<Box>().swap(boxes);
+    SahBuilder sb{refs, bin, {}, leaf_size};
 #pragma omp parallel
 #pragma omp single
-  root = tb.build(0, (int32_t)nt);
-  bin.resize(tb.next.load());
+    root = sb.build(0, (int32_t)nt);
+    bin.resize(sb.next.load());
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < ntl; ++i) order[i] = refs[i].id;
+  } else {
+    float extent = std::max({scene.hi[0] - scene.lo[0], scene.hi[1] - scene.lo[1], scene.hi[2] - scene.lo[2]});
+    if (!(extent > 0) || !std::isfinite(extent)) extent = 1.0f;
+    const double scale = double((1u << 21) - 1) / double(extent);
+    std::vector<uint64_t> codes(nt);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < ntl; ++i) {
+      uint64_t q[3];
+      for (int d = 0; d < 3; ++d) {
+        double c = 0.5 * (double(boxes[i].lo[d]) + double(boxes[i].hi[d]));
+        double v = (c - scene.lo[d]) * scale;
+        v = std::min(std::max(v, 0.0), double((1u << 21) - 1));
+        q[d] = uint64_t(v);
+      }
+      codes[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+      order[i] = uint32_t(i);
+    }
+
+    // 2. sort
+    radix_sort(codes, order);
+    std::vector<Box> sorted_boxes(nt);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < ntl; ++i) sorted_boxes[i] = boxes[order[i]];
+    std::vector<Box>().swap(boxes);
+
+    // 3. binary radix tree
+    TreeBuilder tb{codes, sorted_boxes, bin, {}, leaf_size};
+#pragma omp parallel
+#pragma omp single
+    root = tb.build(0, (int32_t)nt);
+    bin.resize(tb.next.load());
+  }
 
   // 4. collapse to kBvhWidth-wide, breadth first
   std::vector<BvhNode> nodes;
@@ -295,6 +496,32 @@ bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf
   if ((kBvhWidth - 1) * depth + 1 > kStackSlots) {
     error = "BVH too deep for the traversal stack (depth " + std::to_string(depth) + ")";
     return false;
+  }
+  // Surface-area model of the wide tree: a ray through the root box enters a
+  // box with probability area(box) / area(root), so the expected wide nodes
+  // visited is the sum of the nodes' areas and the expected triangle tests the
+  // sum of leaf area x triangles, both over the root's area (double sums).
+  {
+    auto child_box = [](const BvhChild &c) {
+      Box b;
+      for (int d = 0; d < 3; ++d) { b.lo[d] = c.lo[d]; b.hi[d] = c.hi[d]; }
+      return b;
+    };
+    auto node_area = [&](const BvhNode &nd) {
+      Box b = empty_box();
+      for (int k = 0; k < kBvhWidth; ++k)
+        if (nd.c[k].count >= 0) grow(b, child_box(nd.c[k]));
+      return (double)half_area(b);
+    };
+    const double root_area = node_area(nodes[0]);
+    double visits = 0, tests = 0;
+    for (const BvhNode &nd : nodes) {
+      visits += node_area(nd);
+      for (int k = 0; k < kBvhWidth; ++k)
+        if (nd.c[k].count > 0) tests += (double)half_area(child_box(nd.c[k])) * nd.c[k].count;
+    }
+    out.sah_node_visits = root_area > 0 ? visits / root_area : 0;
+    out.sah_triangle_tests = root_area > 0 ? tests / root_area : 0;
   }
   out.nodes.swap(nodes);
   out.order.swap(order);

@@ -249,7 +249,9 @@ struct dvs_scene {
   std::vector<int32_t> rank_of_pixel;  // host inverse of pixel_of_rank
   size_t n_nodes = 0, n_tris = 0, n_vertices = 0;
   int depth = 0, leaf_size = 0;
+  int builder = 0;  // dvs_bvh_params.builder
   double build_seconds = 0;
+  double sah_node_visits = 0, sah_triangle_tests = 0;
   float coherent_span = 1.0f;  // 0.5 % of the scene's largest extent
   // camera render buffers
   cudaStream_t stream = nullptr;
@@ -453,6 +455,8 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   const bool leaf_given = params && params->leaf_size > 0;
   const int precision = params ? params->precision : 0;
   if (precision < 0 || precision > 3) return fail(DVS_ERR_INVALID, "invalid BVH precision flags (0..3)");
+  const int builder = params ? params->builder : 0;
+  if (builder != 0 && builder != 1) return fail(DVS_ERR_INVALID, "invalid BVH builder (0 Morton radix, 1 binned SAH)");
   const bool half_bounds = precision & DVS_BVH_HALF_BOUNDS, watertight = precision & DVS_BVH_WATERTIGHT;
   BvhBuild bvh;
   std::string err;
@@ -460,7 +464,7 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   int leaf = leaf_given ? params->leaf_size : 2;
   for (;; leaf *= 2) {
     err.clear();
-    built = build_bvh(vertices, n_vertices, indices, n_triangles, leaf, bvh, err);
+    built = build_bvh(vertices, n_vertices, indices, n_triangles, leaf, builder, bvh, err);
     if (built || leaf_given || leaf >= 8) break;
   }
   if (!built) return fail(DVS_ERR_INVALID, err);
@@ -522,6 +526,9 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   s->leaf_size = leaf;
   s->geometry_kind = precision;
   s->build_seconds = bvh.seconds;
+  s->builder = builder;
+  s->sah_node_visits = bvh.sah_node_visits;
+  s->sah_triangle_tests = bvh.sah_triangle_tests;
   {
     float lo[3] = {vertices[0], vertices[1], vertices[2]}, hi[3] = {vertices[0], vertices[1], vertices[2]};
     for (size_t i = 0; i < n_vertices; ++i)
@@ -635,6 +642,10 @@ int dvs_scene_view_create(const dvs_scene *base, const dvs_camera *camera, int32
   s->n_vertices = base->n_vertices;
   s->depth = base->depth;
   s->leaf_size = base->leaf_size;
+  s->builder = base->builder;
+  s->build_seconds = base->build_seconds;
+  s->sah_node_visits = base->sah_node_visits;
+  s->sah_triangle_tests = base->sah_triangle_tests;
   s->coherent_span = base->coherent_span;
   s->rank_of_pixel.assign(order.size(), 0);
   for (size_t r = 0; r < order.size(); ++r) s->rank_of_pixel[order[r]] = (int32_t)r;
@@ -666,6 +677,10 @@ int dvs_scene_info_get(const dvs_scene *s, dvs_scene_info *out) {
   out->build_seconds = s->build_seconds;
   out->leaf_size = s->leaf_size;
   out->precision = s->geometry_kind;
+  out->builder = s->builder;
+  out->reserved = 0;
+  out->sah_node_visits = s->sah_node_visits;
+  out->sah_triangle_tests = s->sah_triangle_tests;
   return DVS_OK;
 }
 
@@ -1004,7 +1019,7 @@ static int stage_batch(dvs_sensor *s, const dvs_optical_interval *ivs, size_t co
       cell.t0 = iv.t0 + step * dt;
       cell.t1 = step + 1 == steps ? iv.t1 : iv.t0 + (step + 1) * dt;
       cell.interval = (int32_t)i;
-      cell.pad = 0;
+      cell.dt = (float)(cell.t1 - cell.t0);
     }
   }
   std::memcpy(s->h_ivs, ivs, sizeof(dvs_optical_interval) * count);

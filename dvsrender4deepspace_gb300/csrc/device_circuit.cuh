@@ -124,19 +124,29 @@ struct PixelRegsF {
   double refractory_until;
   float threshold_pos, threshold_neg;
   bool reset_pending;
+  // false once refractory_until <= the start of a cell: the deadline then
+  // stays in the past for every later cell until an event sets a new one
+  bool refractory;
 };
 
 // Time inside the cell is an FP32 offset from the cell start (t0) and the
-// refractory deadline an FP32 offset too, so the no-event path has no FP64
-// arithmetic; absolute event times and deadlines are formed in FP64 only
-// when an event happens.
+// refractory deadline an FP32 offset too, formed from the FP64 deadline only
+// while the pixel is still refractory, so the no-event path has no FP64
+// arithmetic (GB300's FP64 pipe is narrow, and one lane that uses it costs
+// its warp the whole instruction); absolute event times and deadlines are
+// formed in FP64 only when an event happens.
 template <class Rng>
 __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, float rate, double t0, float dt,
                                  double *out_t, int8_t *out_p, int capacity, Rng &rng) {
   if (!(dt > 0)) return 0;
   const float charge = (float)p.charge_scale, leak = (float)p.reference_leak;
   int count = 0;
-  float off = 0.0f, ref_off = (float)(s.refractory_until - t0);
+  // a deadline in the past gives ref_off <= 0, which no offset in the cell is below
+  float off = 0.0f, ref_off = -1.0f;
+  if (s.refractory) {
+    ref_off = (float)(s.refractory_until - t0);
+    s.refractory = ref_off > 0.0f;
+  }
   float u = s.receptor_log;
   int passes = 0;
   while (off < dt) {
@@ -210,10 +220,47 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, float rate
     s.reference_log = u;
     s.refractory_until = t_event + p.refractory_time;
     ref_off = (float)(s.refractory_until - t0);
+    s.refractory = true;
     s.reset_pending = true;
   }
   s.receptor_log = u;
   return count;
+}
+
+// log of the Poisson pmf, k log(mu) - mu - log(k!), in FP32 without the
+// cancellation of large terms that the direct form suffers at large means.
+// Below k = 10 the direct form with lgammaf (the terms are small there).
+// From k = 10, Stirling's series log k! = (k + 1/2) log k - k + log(2 pi)/2
+// + 1/(12k) - 1/(360k^3) + 1/(1260k^5) (truncation error below 1e-10) turns
+// k log(mu) - mu - (k log k - k) into -mu h(x), x = (k - mu)/mu and
+// h(x) = (1 + x) log1p(x) - x, which is summed as its power series
+// sum_{n>=2} (-1)^n x^n / (n (n - 1)) for |x| < 1/4, where the closed form
+// would cancel.  Against FP64 lgamma the absolute error stays below 1e-5
+// wherever the pmf is above e^-25, for means from 10 to 1e6.
+__device__ __forceinline__ float poisson_log_pmf(float k, float mu) {
+  if (k < 10.0f) return k * logf(mu) - mu - lgammaf(k + 1.0f);
+  const float x = (k - mu) / mu;
+  float h;
+  if (fabsf(x) < 0.25f) {
+    float acc = 1.0f / 132.0f;  // n = 12
+    acc = fmaf(acc, x, -1.0f / 110.0f);
+    acc = fmaf(acc, x, 1.0f / 90.0f);
+    acc = fmaf(acc, x, -1.0f / 72.0f);
+    acc = fmaf(acc, x, 1.0f / 56.0f);
+    acc = fmaf(acc, x, -1.0f / 42.0f);
+    acc = fmaf(acc, x, 1.0f / 30.0f);
+    acc = fmaf(acc, x, -1.0f / 20.0f);
+    acc = fmaf(acc, x, 1.0f / 12.0f);
+    acc = fmaf(acc, x, -1.0f / 6.0f);
+    acc = fmaf(acc, x, 0.5f);  // n = 2
+    h = acc * x * x;
+  } else {
+    h = (1.0f + x) * log1pf(x) - x;
+  }
+  const float ik = 1.0f / k, ik2 = ik * ik;
+  const float series = ik * (1.0f / 12.0f - ik2 * (1.0f / 360.0f - ik2 * (1.0f / 1260.0f)));
+  const float half_log_2pi = 0.918938533f;  // log(2 pi) / 2
+  return -mu * h - 0.5f * logf(k) - half_log_2pi - series;
 }
 
 // Poisson draw for means of 10 and more by the transformed rejection method
@@ -222,10 +269,12 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, float rate
 // 12 (1993) 39-45 (algorithm PTRS).  A candidate k comes from a transformed
 // uniform U, a second uniform V accepts it at once inside the squeeze (about
 // 90 % of candidates at these means), and the rest are decided by the exact
-// test log(V * alpha / (a / us^2 + b)) <= k log(mu) - mu - log(k!), evaluated
-// in FP64 because it cancels large terms.  The constants are the paper's.
-// Every candidate takes two uniforms; after 64 rejected candidates (a
-// probability far below 1e-60) the draw falls back to the rounded normal.
+// test log(V * alpha / (a / us^2 + b)) <= log pmf(k), all in FP32 (the pmf
+// through poisson_log_pmf).  With one lane in ten taking the test nearly
+// every warp runs it, so it must not run on the GPU's narrow FP64 pipe.  The
+// constants are the paper's.  Every candidate takes two uniforms; after 64
+// rejected candidates (a probability far below 1e-60) the draw falls back to
+// the rounded normal.
 __device__ __forceinline__ float poisson_ptrs(curandStatePhilox4_32_10_t &st, float mu) {
   const float smu = sqrtf(mu);
   const float b = 0.931f + 2.53f * smu;
@@ -240,9 +289,8 @@ __device__ __forceinline__ float poisson_ptrs(curandStatePhilox4_32_10_t &st, fl
     const float k = floorf((2.0f * a / us + b) * U + mu + 0.43f);
     if (us >= 0.07f && V <= v_r) return k;
     if (k < 0.0f) continue;
-    const double lhs = log((double)V) + log((double)inv_alpha) - log((double)a / ((double)us * us) + (double)b);
-    const double rhs = -(double)mu + (double)k * log((double)mu) - lgamma((double)k + 1.0);
-    if (lhs <= rhs) return k;
+    const float lhs = logf(V) + logf(inv_alpha) - logf(a / (us * us) + b);
+    if (lhs <= poisson_log_pmf(k, mu)) return k;
   }
   return fmaxf(0.0f, floorf(mu + smu * curand_normal(&st) + 0.5f));
 }

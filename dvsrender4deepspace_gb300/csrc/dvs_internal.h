@@ -88,12 +88,16 @@ struct BvhBuild {
   std::vector<uint32_t> order;  // leaf order -> original triangle index
   int depth = 0;                // levels of wide nodes
   double seconds = 0;
+  // surface-area model of the wide tree: expected wide nodes visited and
+  // triangle tests of a ray through the root box
+  double sah_node_visits = 0, sah_triangle_tests = 0;
 };
 
-// Morton-ordered radix-split binary tree collapsed to an 8-wide tree.
+// Binary tree collapsed to an 8-wide tree; builder 0 splits Morton-ordered
+// ranges at their highest differing code bit, builder 1 by binned SAH.
 // Returns false with a message on invalid input.
 bool build_bvh(const float *vertices, size_t n_vertices, const uint32_t *indices, size_t n_triangles,
-               int leaf_size, BvhBuild &out, std::string &error);
+               int leaf_size, int builder, BvhBuild &out, std::string &error);
 
 // The precision-format copy of a built tree (same node indices).  Fails when a
 // leaf's first triangle or size does not fit the link, or when a decoded box

@@ -35,7 +35,7 @@ struct alignas(16) CellPose {
 struct alignas(8) Cell {
   double t0, t1;
   int32_t interval;
-  int32_t pad;
+  float dt;  // (float)(t1 - t0), rounded once on the host: the FP32 circuit's cell length
 };
 
 struct PixelParams {

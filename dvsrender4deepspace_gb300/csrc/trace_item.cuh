@@ -121,7 +121,7 @@ __device__ __forceinline__ void circuit_rank(int r, int n, const int32_t *rank_l
   } else {
     // precision mode: the state is held in FP32 registers for the chunk
     PixelRegsF s{(float)st.receptor_log[k], (float)st.reference_log[k], st.refractory_until[k],
-                 (float)st.threshold_pos[k], (float)st.threshold_neg[k], st.reset_pending[k] != 0};
+                 (float)st.threshold_pos[k], (float)st.threshold_neg[k], st.reset_pending[k] != 0, true};
     const int pixel = kPhilox ? st.pixel[k] : 0;
     const float e_rad = (float)photo.electrons_per_radiance, dark = (float)photo.dark_electrons;
     const float *chunk_f = photo.chunk_f32 ? reinterpret_cast<const float *>(radiance) : nullptr;
@@ -131,7 +131,7 @@ __device__ __forceinline__ void circuit_rank(int r, int n, const int32_t *rank_l
       const float rad = chunk_f ? chunk_f[o] : (float)radiance[o];
       if (!isfinite(rad)) { failed = kErrOptical; break; }
       float rate = rad * e_rad + dark;
-      const float dt = (float)(cell.t1 - cell.t0);
+      const float dt = cell.dt;
       int emitted;
       if (kPhilox) {
         curandStatePhilox4_32_10_t ph = philox_at(photo.seed, pixel, cell.t0);

@@ -89,10 +89,12 @@ class DeviceScene:
     (replaces BVHBuilder::build + DeviceScene)."""
 
     def __init__(self, vertices, normals, indices, camera, supersample, hapke=None, albedos=None, leaf_size=0,
-                 geometry=0):
+                 geometry=0, builder=0):
         """geometry: dvs_bvh_params.precision flags -- 0 the reference's (FP32
         child bounds, Moller-Trumbore), HALF_BOUNDS (FP16 child bounds
-        quantised outward), WATERTIGHT (watertight triangle test), or both."""
+        quantised outward), WATERTIGHT (watertight triangle test), or both.
+        builder: dvs_bvh_params.builder -- 0 Morton radix splits, 1 binned SAH
+        splits with the reference's criterion."""
         lib = _capi.load()
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
         n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
@@ -108,7 +110,7 @@ class DeviceScene:
         check(lib.dvs_scene_create(v.ctypes.data_as(fp), n.ctypes.data_as(fp), i.ctypes.data_as(C.POINTER(C.c_uint32)),
                                    a.ctypes.data_as(fp) if a is not None else None, v.shape[0], i.shape[0],
                                    C.byref(camera_struct(camera)), self.samples, C.byref(hapke_struct(self.hapke)),
-                                   C.byref(_capi.BvhParams(int(leaf_size), int(geometry))),
+                                   C.byref(_capi.BvhParams(int(leaf_size), int(geometry), int(builder))),
                                    C.byref(h)))
         self.handle = h
         self.width = int(camera["width"])

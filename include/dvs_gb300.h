@@ -121,7 +121,12 @@ typedef struct {
                                  triangles).  DVS_BVH_WATERTIGHT: the watertight FP32 triangle test
                                  (Woop et al. 2013) on stored vertices.  No counterpart in the
                                  reference. */
-  int32_t reserved[2];
+  int32_t builder;            /* split rule of the binary tree that is collapsed to 8-wide nodes:
+                                 0 = radix splits of 63-bit Morton codes (parallel, O(n log n));
+                                 1 = binned SAH splits with the reference's criterion
+                                 (src/bvh/bining.cpp:9-103: <= 32 bins per axis, cost area x count),
+                                 always split down to leaf_size */
+  int32_t reserved;
 } dvs_bvh_params;
 
 typedef struct {
@@ -131,6 +136,10 @@ typedef struct {
   double build_seconds;
   int32_t leaf_size;          /* triangles per leaf the tree was built with */
   int32_t precision;          /* dvs_bvh_params.precision flags of the tree */
+  int32_t builder;            /* dvs_bvh_params.builder of the tree */
+  int32_t reserved;
+  double sah_node_visits;     /* surface-area model of the 8-wide tree: expected nodes visited and */
+  double sah_triangle_tests;  /* triangle tests of a ray through the root box (sums of area ratios) */
 } dvs_scene_info;
 
 typedef struct {

@@ -37,13 +37,14 @@ class DeviceScene {
   DeviceScene(const std::vector<float> &vertices, const std::vector<float> &normals,
               const std::vector<uint32_t> &indices, const dvs_camera &camera, int supersample,
               const dvs_hapke &hapke, const std::vector<float> *albedos = nullptr, int leaf_size = 0,
-              int geometry = 0) {
+              int geometry = 0, int builder = 0) {
     if (vertices.size() % 3 || normals.size() != vertices.size() || indices.size() % 3 ||
         (albedos && albedos->size() * 3 != vertices.size()))
       throw std::invalid_argument("invalid indexed mesh/BVH/material dimensions");
     dvs_bvh_params params{};
     params.leaf_size = leaf_size;
     params.precision = geometry;  // DVS_BVH_HALF_BOUNDS | DVS_BVH_WATERTIGHT
+    params.builder = builder;     // 0 Morton radix splits, 1 binned SAH splits
     dvs_scene *s = nullptr;
     check(dvs_scene_create(vertices.data(), normals.data(), indices.data(), albedos ? albedos->data() : nullptr,
                            vertices.size() / 3, indices.size() / 3, &camera, supersample, &hapke, &params, &s));

@@ -41,10 +41,11 @@ static float add_rounded(float origin, uint16_t off, bool up) {
 }
 
 int main(int argc, char **argv) {
-  if (argc != 4) return 2;
+  if (argc != 4 && argc != 5) return 2;
   const unsigned seed = (unsigned)std::atoi(argv[1]);
   const int n = std::atoi(argv[2]);
   const double scale = std::atof(argv[3]);
+  const int builder = argc == 5 ? std::atoi(argv[4]) : 0;  // 0 Morton radix, 1 binned SAH
   std::mt19937 rng(seed);
   std::uniform_real_distribution<double> jitter(-0.3, 0.3), height(0.0, 1.0);
   std::vector<float> V;
@@ -64,7 +65,7 @@ int main(int argc, char **argv) {
   const size_t nt = I.size() / 3;
   BvhBuild bvh;
   std::string err;
-  if (!build_bvh(V.data(), V.size() / 3, I.data(), nt, 2, bvh, err)) {
+  if (!build_bvh(V.data(), V.size() / 3, I.data(), nt, 2, builder, bvh, err)) {
     std::printf("build failed: %s\n", err.c_str());
     return 1;
   }
@@ -126,6 +127,7 @@ int main(int argc, char **argv) {
   }
   for (size_t t = 0; t < nt; ++t)
     if (seen[t] != 1) { std::printf("triangle %zu in %d leaves\n", t, seen[t]); return 1; }
-  std::printf("nodes %zu depth %d leaves %zu max_slack %.3g\n", bvh.nodes.size(), bvh.depth, leaves, max_slack);
+  std::printf("nodes %zu depth %d leaves %zu max_slack %.3g sah_nodes %.6g sah_tris %.6g\n", bvh.nodes.size(),
+              bvh.depth, leaves, max_slack, bvh.sah_node_visits, bvh.sah_triangle_tests);
   return 0;
 }

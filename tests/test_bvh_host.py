@@ -24,13 +24,27 @@ def selftest(tmp_path_factory):
     return exe
 
 
+@pytest.mark.parametrize("builder", [0, 1])  # Morton radix splits, binned SAH splits
 @pytest.mark.parametrize("seed,n,scale,slack", [(1, 64, 1000.0, 2e-3),       # a 1 km tile
                                                 (2, 160, 40960.0, 2e-3),     # the 4096^2 terrain's extent
                                                 (3, 40, 300000.0, None)])    # offsets beyond 65504
-def test_quantised_bounds_enclose_the_fp32_tree(selftest, seed, n, scale, slack):
-    out = subprocess.run([selftest, str(seed), str(n), str(scale)], capture_output=True, text=True)
+def test_quantised_bounds_enclose_the_fp32_tree(selftest, seed, n, scale, slack, builder):
+    out = subprocess.run([selftest, str(seed), str(n), str(scale), str(builder)], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     fields = out.stdout.split()
     assert fields[0] == "nodes" and int(fields[1]) > 0 and int(fields[5]) > 0
     if slack is not None:
         assert float(fields[7]) < slack, out.stdout   # FP16 offsets widen a box by well under 0.2 % of its node
+
+
+def test_sah_splits_lower_the_surface_area_cost(selftest):
+    """On a jittered terrain grid the binned-SAH tree's surface-area model
+    (expected wide nodes plus triangle tests per ray through the root box) is
+    below the Morton tree's: the SAH splits minimise that cost level by level."""
+    got = {}
+    for builder in (0, 1):
+        out = subprocess.run([selftest, "5", "200", "10000.0", str(builder)], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout + out.stderr
+        f = out.stdout.split()
+        got[builder] = float(f[9]) + float(f[11])
+    assert got[1] < got[0], got

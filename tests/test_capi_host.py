@@ -82,6 +82,12 @@ def test_scene_create_rejects_invalid_arguments_on_host(lib):
     r = lib.dvs_scene_create(V.ctypes.data_as(fp), V.ctypes.data_as(fp), I.ctypes.data_as(C.POINTER(C.c_uint32)),
                              None, 3, 1, C.byref(cam), 1, C.byref(hap), None, C.byref(h))
     assert r == _capi.DVS_ERR_INVALID and b"nonfinite" in lib.dvs_last_error()
+    V[1, 0] = 1.0
+    for params in (_capi.BvhParams(0, 0, 7), _capi.BvhParams(0, 9, 0)):  # unknown builder, unknown flags
+        r = lib.dvs_scene_create(V.ctypes.data_as(fp), V.ctypes.data_as(fp),
+                                 I.ctypes.data_as(C.POINTER(C.c_uint32)), None, 3, 1, C.byref(cam), 1,
+                                 C.byref(hap), C.byref(params), C.byref(h))
+        assert r == _capi.DVS_ERR_INVALID and b"BVH" in lib.dvs_last_error()
 
 
 def test_cpp_facade_compiles_links_and_throws(lib, tmp_path):

@@ -116,18 +116,22 @@ def test_cam_terrain_matches_oracle(ss):
 
 def test_leaf_size_changes_the_tree_not_the_image():
     """Nearest hits and occlusion do not depend on how the tree is cut: the
-    default (2 triangles per leaf) and 1/8-triangle leaves render the same image
-    up to edge ties."""
+    default (2 triangles per leaf), 1/8-triangle leaves and the binned-SAH
+    tree render the same image up to edge ties."""
     pose = dict(position=(13.0, -7.0, 700.0), rotation=(0.0, 0.0, 0.0, 1.0),
                 light=trajectory.sun_direction(30, 40), intensity=1000)
     images = {}
     for leaf in (0, 1, 8):
         V, N, I, camera, hap, scene = terrain_scene(leaf=leaf)
         info = scene.info()
-        assert info["leaf_size"] == (leaf or 2)
+        assert info["leaf_size"] == (leaf or 2) and info["builder"] == 0
         images[leaf] = CamRayCaster(scene).render_state(pose)
-    for leaf in (1, 8):
-        for a, b in zip(images[0], images[leaf]):
+    sah = DeviceScene(V, N, I, camera, 2, hap, builder=1)
+    info = sah.info()
+    assert info["builder"] == 1 and info["sah_node_visits"] > 1 and info["sah_triangle_tests"] > 0
+    images["sah"] = CamRayCaster(sah).render_state(pose)
+    for key in (1, 8, "sah"):
+        for a, b in zip(images[0], images[key]):
             assert float(np.mean(rel_err(a, b) > RTOL)) < 1e-3
 
 
