@@ -287,7 +287,13 @@ __device__ __forceinline__ bool intersect_wt(const WtRay &w, float3 o, float3 v0
   const float ax = A.x - w.sx * az, ay = A.y - w.sy * az;
   const float bx = B.x - w.sx * bz, by = B.y - w.sy * bz;
   const float cx = C.x - w.sx * cz, cy = C.y - w.sy * cz;
-  float U = cx * by - cy * bx, V = ax * cy - ay * cx, W = bx * ay - by * ax;
+  float U = cx * by - cy * bx, V = ax * cy - ay * cx;
+  // A nonzero float edge function has the sign of the exact one (rounding
+  // keeps the order of the two products), and so does its FP64 recomputation:
+  // opposite nonzero signs of U and V are a miss whatever W is, decided
+  // before W is formed.
+  if ((U < 0.0f && V > 0.0f) || (U > 0.0f && V < 0.0f)) return false;
+  float W = bx * ay - by * ax;
   if (U == 0.0f || V == 0.0f || W == 0.0f) {
     U = (float)((double)cx * (double)by - (double)cy * (double)bx);
     V = (float)((double)ax * (double)cy - (double)ay * (double)cx);

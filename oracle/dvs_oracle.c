@@ -546,7 +546,10 @@ static int intersect_watertight(const wt_ray *w, rv3 o, rv3 v0, rv3 v1, rv3 v2, 
   const real ax = comp3(A, w->kx) - w->sx * az, ay = comp3(A, w->ky) - w->sy * az;
   const real bx = comp3(B, w->kx) - w->sx * bz, by = comp3(B, w->ky) - w->sy * bz;
   const real cx = comp3(C, w->kx) - w->sx * cz, cy = comp3(C, w->ky) - w->sy * cz;
-  real U = cx * by - cy * bx, V = ax * cy - ay * cx, W = bx * ay - by * ax;
+  real U = cx * by - cy * bx, V = ax * cy - ay * cx;
+  /* opposite nonzero signs of U and V: a miss decided before W, as the kernels do */
+  if ((U < R(0.0) && V > R(0.0)) || (U > R(0.0) && V < R(0.0))) return 0;
+  real W = bx * ay - by * ax;
   if (U == R(0.0) || V == R(0.0) || W == R(0.0)) {
     U = (real)((double)cx * (double)by - (double)cy * (double)bx);
     V = (real)((double)ax * (double)cy - (double)ay * (double)cx);
