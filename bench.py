@@ -75,15 +75,14 @@ PHYSIC = dict(threshold_pos=0.2, threshold_neg=0.2, refractory_time=200e-6, read
               photon_shot_noise=1, reset_thermal_noise=0, random_seed=114514, max_events_per_step=16,
               readout_queue_capacity=1000000)
 METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency vs plain path"
-# DRAM bytes (read + write) per pixel-cell of one trace_cells_kernel launch, by
-# workload and BVH format, measured with ncu's dram__bytes_read.sum and
-# dram__bytes_write.sum on one launch (precision: a 16-cell launch of the
-# FP16-bounds tree, a 4-cell launch of the FP32 one), scaled by the cells traced.
-TRACE_DRAM_BYTES_PER_PIXEL_CELL = {}
-# Warp instructions per traced ray (primary + shadow) of trace_cells_kernel, by
-# workload and BVH format: ncu smsp__inst_executed.sum of one launch divided
-# by the rays the sensor counted for it.
-TRACE_WARP_INSTRUCTIONS_PER_RAY = {}
+# ncu counters of one full-size trace_cells_kernel launch (one native batch),
+# by (workload, BVH format, cells per warp, rays per lane): warp instructions
+# (smsp__inst_executed.sum) per traced ray (primary + shadow, as the sensor
+# counted them), and DRAM bytes read + written (dram__bytes_read.sum +
+# dram__bytes_write.sum) per pixel-cell.  Radiance writes still held in L2
+# when the kernel ends are not in the DRAM count.
+TRACE_WARP_INSTRUCTIONS_PER_RAY = {("orbit", "reference", 32, 2): 82860353469 / 1768685229}
+TRACE_DRAM_BYTES_PER_PIXEL_CELL = {("orbit", "reference", 32, 2): (13664256 + 177929728) / (89960 * 640)}
 GB300_SMS = 152
 
 
@@ -500,7 +499,9 @@ def run_gb300(args):
     # per ray that ncu counted for this kernel and format, at the sampled clock
     rays_per_launch = rays / max(1, st["optics_launches"])
     issue = None
-    ipr = TRACE_WARP_INSTRUCTIONS_PER_RAY.get((args.workload, args.geometry))
+    shape = ((tuning["cells_per_warp"], tuning["rays_per_lane"]) if tuning else (args.cw or 32, args.rays or 2))
+    counted = (args.workload, args.geometry) + shape
+    ipr = TRACE_WARP_INSTRUCTIONS_PER_RAY.get(counted)
     sm_mhz = clocks.summary()["sm_mhz"]
     if ipr and optics_ms > 0 and sm_mhz:
         issue_peak = GB300_SMS * 4 * sm_mhz * 1e6
@@ -548,9 +549,8 @@ def run_gb300(args):
                       "events_total": st["events_ms"]},
         "roofline": {"bound": "hbm", "kernel": "trace_cells_kernel", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "traffic": (TRACE_DRAM_BYTES_PER_PIXEL_CELL[(args.workload, args.geometry)] * n_pix
-                                 * cells_per_launch
-                                 if (args.workload, args.geometry) in TRACE_DRAM_BYTES_PER_PIXEL_CELL else None),
+                     "traffic": (TRACE_DRAM_BYTES_PER_PIXEL_CELL[counted] * n_pix * cells_per_launch
+                                 if counted in TRACE_DRAM_BYTES_PER_PIXEL_CELL else None),
                      "algorithmic_bytes": alg_bytes,
                      "peak_source": "measured" if peaks else "fallback",
                      "note": "traversal is instruction-issue bound (roofline_issue); bytes = radiance written "

@@ -12,10 +12,10 @@ pixel's delivery times, so a cropped oracle could not reproduce them); light
 intensity 1000, the reference tests' value (the config's 1.0 is
 photon-starved and gives almost no events).
 
-bin/dvs runs the full sensor on the GPU.  The oracle runs two 16x12 crops of
-the same camera (the crop's sub-rays are the full camera's, bit for bit: the
-intrinsics are integers) through the app's own batches, with its margin
-classifier.  Every crop pixel's polarity sequence must equal the oracle's
+bin/dvs runs the full sensor on the GPU.  The oracle runs the two 16x12 crops
+of the same camera where the GPU's events are busiest (the crop's sub-rays
+are the full camera's, bit for bit: the intrinsics are integers) through the
+app's own batches, with its margin classifier.  Every crop pixel's polarity sequence must equal the oracle's
 unless the pixel is in a margin class, and non-margin timestamps agree
 within 1 us.
 """
@@ -42,7 +42,31 @@ PHYSIC = dict(threshold_pos=0.2, threshold_neg=0.2, threshold_std=0.0, threshold
               readout_latency=0.0, readout_queue_capacity=1000000, max_events_per_step=16, random_seed=114514)
 SCENE = dict(frame_count=50, fps=100.0, imu_fps=1000.0, cam_fps=100.0, time_resolution=1e-5, supersample_factor=1,
              blur_resolution=1e-3)
-CROPS = ((165, 124), (40, 30))  # (x0, y0) of 16 x 12 crops: the image centre and a corner region
+CROP_W, CROP_H = 16, 12
+
+
+def busiest_crops(ev, width, height, n=2):
+    """(x0, y0) of the n non-overlapping 16x12 windows (on a 4-pixel grid)
+    with the most pixels that have events.  A 1 km nadir pass at 50 m/s moves
+    the ground about seven pixels in 0.49 s, so events gather along crater
+    rims and shadow edges; fixed windows can hold none.  Every pixel of a
+    chosen window is compared, with or without events."""
+    active = np.zeros((height + 1, width + 1))
+    active[1:, 1:][ev["y"], ev["x"]] = 1
+    S = active.cumsum(0).cumsum(1)
+    cands = []
+    for y0 in range(0, height - CROP_H + 1, 4):
+        for x0 in range(0, width - CROP_W + 1, 4):
+            c = S[y0 + CROP_H, x0 + CROP_W] - S[y0, x0 + CROP_W] - S[y0 + CROP_H, x0] + S[y0, x0]
+            cands.append((c, x0, y0))
+    cands.sort(key=lambda c: -c[0])
+    chosen = []
+    for c, x0, y0 in cands:
+        if all(abs(x0 - a) >= CROP_W or abs(y0 - b) >= CROP_H for a, b in chosen):
+            chosen.append((x0, y0))
+        if len(chosen) == n:
+            break
+    return chosen
 
 
 def as_state(rec):
@@ -81,7 +105,7 @@ def test_small_config_through_bin_dvs_matches_the_oracle(tmp_path):
     o64 = O.OracleScene(V, N, I, CAMERA, 1, HAPKE, fp64=True)
     ivs = [oracle_intervals(b) for b in batches]
     total_pixels, total_margin, compared = 0, 0, 0
-    for x0, y0 in CROPS:
+    for x0, y0 in busiest_crops(gpu, CAMERA["width"], CAMERA["height"]):
         crop = dict(CAMERA, width=16, height=12, cx=CAMERA["cx"] - x0, cy=CAMERA["cy"] - y0)
         ors = O.OracleSensor(o64.with_camera(crop), cfg["physic"], margin=True)
         ors.initialize(as_state(state0), t0)
@@ -102,5 +126,5 @@ def test_small_config_through_bin_dvs_matches_the_oracle(tmp_path):
                 compared += 1
                 # events.bin stores float32 seconds (dvs_writer.hpp:44-55): 6e-8 s at 0.5 s
                 assert np.max(np.abs(g["t"].astype(np.float64) - o["timestamp"])) < 1e-6, (x, y)
-    assert compared > 20
-    assert total_margin < 0.2 * total_pixels
+    assert compared > 20, (compared, total_margin, total_pixels)
+    assert total_margin < 0.2 * total_pixels, (compared, total_margin, total_pixels)
