@@ -607,11 +607,13 @@ def run_serving(args):
 
     # warm-up: one small job per terrain through the server (first-use allocations, module load)
     warm = [j for j in stream() if j.camera["width"] == 64][:2]
-    serve.Server(scenes, 150 << 30).run(warm, realtime=False)
+    circuit = args.circuit
+    serve.Server(scenes, 150 << 30, circuit=circuit).run(warm, realtime=False)
     results = {}
     for mode, max_active, policy in (("served", 64, "srpt"), ("served_fair", 64, "fair"), ("plain", 1, "fair")):
         jobs = stream()
-        srv = serve.Server(scenes, 150 << 30, horizons_per_step=64, max_active=max_active, policy=policy)
+        srv = serve.Server(scenes, 150 << 30, horizons_per_step=64, max_active=max_active, policy=policy,
+                           circuit=circuit)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with ClockSampler(local) as clocks:
@@ -634,7 +636,8 @@ def run_serving(args):
                        "resolutions": ["64x48", "346x260", "640x480", "1280x720"],
                        "durations_s": [0.05 * args.serving_scale, 2.0 * args.serving_scale],
                        "terrain_grids": list(SERVING_GRIDS), "hbm_budget_gb": 150, "supersample": 1,
-                       "time_resolution": 1e-5, "circuit_step": PHYSIC["circuit_step"]},
+                       "time_resolution": 1e-5, "circuit_step": PHYSIC["circuit_step"],
+                       "circuit_precision": circuit},
             "served": results["served"], "served_fair": results["served_fair"], "plain": results["plain"],
             "p99_speedup_vs_plain": results["plain"]["p99_ms"] / results["served"]["p99_ms"],
             "throughput_vs_plain": results["served"]["events_per_s"] / max(1e-9, results["plain"]["events_per_s"]),
@@ -873,8 +876,8 @@ def main():
     w = WORKLOADS.get("orbit" if args.workload == "batching" else args.workload, {})
     if args.geometry is None:
         args.geometry = w.get("geometry", "reference")   # each workload's configured BVH format
-    if args.circuit is None:
-        args.circuit = w.get("circuit", "fp64")
+    if args.circuit is None:  # serving: the FP32 circuit with the counter-based noise stream
+        args.circuit = "fp32-philox" if args.workload == "serving" else w.get("circuit", "fp64")
     if args.impl == "reference":
         if args.workload in ("serving", "batching"):
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving or multi-sensor "

@@ -81,11 +81,13 @@ class Server:
     resident); hbm_budget: device bytes the admitted jobs may hold."""
 
     def __init__(self, scenes, hbm_budget, horizons_per_step=64, max_active=64, policy="srpt",
-                 fill_samples=1 << 26, circuit="fp32"):
-        """circuit: the jobs' pixel circuit -- "fp32" (precision mode: FP32
-        receptor arithmetic, FP64 times and root solves; the default, the
-        circuit being what bounds supersample-1 jobs), "fp32-philox" or the
-        reference's "fp64"."""
+                 fill_samples=1 << 26, circuit="fp32-philox"):
+        """circuit: the jobs' pixel circuit -- "fp32-philox" (the default:
+        FP32 receptor arithmetic, FP64 times and root solves, and the
+        counter-based Philox photon counts, whose no-event path has no FP64
+        instruction -- the circuit is what bounds supersample-1 jobs), "fp32"
+        (the same arithmetic with the reference's XORWOW stream, whose
+        curand_poisson runs in FP64) or the reference's "fp64"."""
         if policy not in ("srpt", "fair"):
             raise ValueError("policy must be srpt or fair")
         if circuit not in ("fp64", "fp32", "fp32-philox"):
