@@ -36,8 +36,8 @@ sys.path.insert(0, ROOT)
 # dvs_bvh_params.precision flags: 1 = FP16 child bounds, 2 = watertight triangle test
 GEOMETRY = {"reference": 0, "half": 1, "watertight": 2, "half+watertight": 3}
 # dvs_bvh_params.builder
-BUILDERS = {"morton": 0, "sah": 1}
-BUILDERS_TEXT = {0: "Morton radix splits", 1: "binned SAH splits"}
+BUILDERS = {"sah": 0, "morton": 1}
+BUILDERS_TEXT = {0: "binned SAH splits", 1: "Morton radix splits"}
 
 WORKLOADS = {
     # configs: precision (1280x720), small (346x260 DAVIS, plain method)
@@ -76,13 +76,13 @@ PHYSIC = dict(threshold_pos=0.2, threshold_neg=0.2, refractory_time=200e-6, read
               readout_queue_capacity=1000000)
 METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency vs plain path"
 # ncu counters of one full-size trace_cells_kernel launch (one native batch),
-# by (workload, BVH format, cells per warp, rays per lane): warp instructions
-# (smsp__inst_executed.sum) per traced ray (primary + shadow, as the sensor
-# counted them), and DRAM bytes read + written (dram__bytes_read.sum +
-# dram__bytes_write.sum) per pixel-cell.  Radiance writes still held in L2
-# when the kernel ends are not in the DRAM count.
-TRACE_WARP_INSTRUCTIONS_PER_RAY = {("orbit", "reference", 32, 2): 82860353469 / 1768685229}
-TRACE_DRAM_BYTES_PER_PIXEL_CELL = {("orbit", "reference", 32, 2): (13664256 + 177929728) / (89960 * 640)}
+# by (workload, BVH format, BVH builder, cells per warp, rays per lane): warp
+# instructions (smsp__inst_executed.sum) per traced ray (primary + shadow, as
+# the sensor counted them), and DRAM bytes read + written
+# (dram__bytes_read.sum + dram__bytes_write.sum) per pixel-cell.  Radiance
+# writes still held in L2 when the kernel ends are not in the DRAM count.
+TRACE_WARP_INSTRUCTIONS_PER_RAY = {("orbit", "reference", "morton", 32, 2): 82860353469 / 1768685229}
+TRACE_DRAM_BYTES_PER_PIXEL_CELL = {("orbit", "reference", "morton", 32, 2): (13664256 + 177929728) / (89960 * 640)}
 GB300_SMS = 152
 
 
@@ -267,8 +267,23 @@ def precision_errors(V, N, I, traj, w, scene, geometry, circuit, budget_pixels=2
                     "p99_rel": float(np.quantile(drel[hit], .99)), "above_1e-5": int((drel > 1e-5).sum()),
                     "non_margin_above_1e-5": int(((drel > 1e-5) & plain).sum()),
                     "misses_agree_non_margin": bool(np.all(((g_dep < 0) == (odep < 0)) | ~plain))}
-    # events: a 16x12 crop at the image centre, 0.5 ms light pulse (500 cells of 1 us)
+    # events: a 16x12 crop through a 0.5 ms light pulse (500 cells of 1 us), at the
+    # fully lit window nearest the image centre (with a low sun the centre can lie in
+    # shadow, where a pulse gives no events), else at the centre
+    lit = np.pad((img.reshape(cam["height"], cam["width"]) > 0).astype(np.int64), ((1, 0), (1, 0)))
+    S = lit.cumsum(0).cumsum(1)
     x0, y0 = cam["width"] // 2 - 8, cam["height"] // 2 - 6
+
+    def fully_lit(xx, yy):
+        return S[yy + 12, xx + 16] - S[yy, xx + 16] - S[yy + 12, xx] + S[yy, xx] == 16 * 12
+    best = (0, x0, y0) if fully_lit(x0, y0) else None
+    for yy in range(0, cam["height"] - 12 + 1, 4):
+        for xx in range(0, cam["width"] - 16 + 1, 4):
+            if best is None or (xx - x0) ** 2 + (yy - y0) ** 2 < best[0]:
+                if fully_lit(xx, yy):
+                    best = ((xx - x0) ** 2 + (yy - y0) ** 2, xx, yy)
+    if best is not None:
+        x0, y0 = best[1], best[2]
     crop = dict(cam, width=16, height=12, cx=cam["cx"] - x0, cy=cam["cy"] - y0)
     phys = dict(PHYSIC, photon_shot_noise=0, threshold_std=0, readout_bandwidth=0, readout_latency=0,
                 max_events_per_step=64)
@@ -500,7 +515,7 @@ def run_gb300(args):
     rays_per_launch = rays / max(1, st["optics_launches"])
     issue = None
     shape = ((tuning["cells_per_warp"], tuning["rays_per_lane"]) if tuning else (args.cw or 32, args.rays or 2))
-    counted = (args.workload, args.geometry) + shape
+    counted = (args.workload, args.geometry, args.builder) + shape
     ipr = TRACE_WARP_INSTRUCTIONS_PER_RAY.get(counted)
     sm_mhz = clocks.summary()["sm_mhz"]
     if ipr and optics_ms > 0 and sm_mhz:
@@ -855,8 +870,8 @@ def main():
     ap.add_argument("--serving-jobs", type=int, default=48)
     ap.add_argument("--serving-scale", type=float, default=0.01)
     ap.add_argument("--leaf", type=int, default=0)
-    ap.add_argument("--builder", default="morton", choices=sorted(BUILDERS),
-                    help="split rule of the BVH: Morton radix splits or binned SAH splits")
+    ap.add_argument("--builder", default="sah", choices=sorted(BUILDERS),
+                    help="split rule of the BVH: binned SAH splits (default) or Morton radix splits")
     ap.add_argument("--geometry", default=None, choices=sorted(GEOMETRY),
                     help="BVH format: FP32 or FP16 (half) child bounds; Moller-Trumbore or watertight triangles")
     ap.add_argument("--chunk", type=int, default=0)

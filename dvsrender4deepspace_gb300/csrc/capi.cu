@@ -456,7 +456,7 @@ int dvs_scene_create(const float *vertices, const float *normals, const uint32_t
   const int precision = params ? params->precision : 0;
   if (precision < 0 || precision > 3) return fail(DVS_ERR_INVALID, "invalid BVH precision flags (0..3)");
   const int builder = params ? params->builder : 0;
-  if (builder != 0 && builder != 1) return fail(DVS_ERR_INVALID, "invalid BVH builder (0 Morton radix, 1 binned SAH)");
+  if (builder != 0 && builder != 1) return fail(DVS_ERR_INVALID, "invalid BVH builder (0 binned SAH, 1 Morton radix)");
   const bool half_bounds = precision & DVS_BVH_HALF_BOUNDS, watertight = precision & DVS_BVH_WATERTIGHT;
   BvhBuild bvh;
   std::string err;

@@ -93,8 +93,8 @@ struct BvhBuild {
   double sah_node_visits = 0, sah_triangle_tests = 0;
 };
 
-// Binary tree collapsed to an 8-wide tree; builder 0 splits Morton-ordered
-// ranges at their highest differing code bit, builder 1 by binned SAH.
+// Binary tree collapsed to an 8-wide tree; builder 0 splits by binned SAH,
+// builder 1 splits Morton-ordered ranges at their highest differing code bit.
 // Returns false with a message on invalid input.
 bool build_bvh(const float *vertices, size_t n_vertices, const uint32_t *indices, size_t n_triangles,
                int leaf_size, int builder, BvhBuild &out, std::string &error);

