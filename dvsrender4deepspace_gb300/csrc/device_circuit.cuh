@@ -263,6 +263,20 @@ __device__ __forceinline__ float poisson_log_pmf(float k, float mu) {
   return -mu * h - 0.5f * logf(k) - half_log_2pi - series;
 }
 
+// A uniform draw in (0, 1] from the top 23 bits of one 32-bit Philox output:
+// the bits are the mantissa of a float in [1, 2), and 2 minus it lies in
+// [2^-23, 1].  Integer and FP32 operations only -- no integer-to-float
+// conversion instruction -- with the resolution of an FP32 uniform near 1.
+__device__ __forceinline__ float philox_uniform(curandStatePhilox4_32_10_t &st) {
+  return 2.0f - __uint_as_float(0x3f800000u | (curand(&st) >> 9));
+}
+// floor(x) for |x| < 2^23 by one addition rounded toward -inf: at 2^23 the
+// float spacing is 1, so x + 2^23 rounds down to the integer below it
+// (exact for every float in that range, negative ones included).
+__device__ __forceinline__ float floor_small(float x) {
+  return __fadd_rd(x, 8388608.0f) - 8388608.0f;
+}
+
 // Poisson draw for means of 10 and more by the transformed rejection method
 // with squeeze of W. Hormann, "The transformed rejection method for
 // generating Poisson random variables", Insurance: Mathematics and Economics
@@ -274,7 +288,8 @@ __device__ __forceinline__ float poisson_log_pmf(float k, float mu) {
 // every warp runs it, so it must not run on the GPU's narrow FP64 pipe.  The
 // constants are the paper's.  Every candidate takes two uniforms; after 64
 // rejected candidates (a probability far below 1e-60) the draw falls back to
-// the rounded normal.
+// the rounded normal.  Candidates are clamped to |k| < 2^23 before the
+// floor: means stop at 1e6, so a clamped candidate is rejected either way.
 __device__ __forceinline__ float poisson_ptrs(curandStatePhilox4_32_10_t &st, float mu) {
   const float smu = sqrtf(mu);
   const float b = 0.931f + 2.53f * smu;
@@ -282,11 +297,12 @@ __device__ __forceinline__ float poisson_ptrs(curandStatePhilox4_32_10_t &st, fl
   const float inv_alpha = 1.1239f + 1.1328f / (b - 3.4f);
   const float v_r = 0.9277f - 3.6224f / (b - 2.0f);
   for (int attempt = 0; attempt < 64; ++attempt) {
-    const float U = curand_uniform(&st) - 0.5f;  // (-1/2, 1/2]
-    const float V = curand_uniform(&st);         // (0, 1]
+    const float U = philox_uniform(st) - 0.5f;  // (-1/2, 1/2]
+    const float V = philox_uniform(st);         // (0, 1]
     const float us = 0.5f - fabsf(U);
     if (us < 0.013f && V > us) continue;  // outside the hat's usable part (also guards us == 0)
-    const float k = floorf((2.0f * a / us + b) * U + mu + 0.43f);
+    const float x = (2.0f * a / us + b) * U + mu + 0.43f;
+    const float k = floor_small(fminf(fmaxf(x, -8388607.0f), 8388607.0f));
     if (us >= 0.07f && V <= v_r) return k;
     if (k < 0.0f) continue;
     const float lhs = logf(V) + logf(inv_alpha) - logf(a / (us * us) + b);
@@ -306,17 +322,17 @@ __device__ __forceinline__ float poisson_electrons_philox(curandStatePhilox4_32_
   if (!(lambda > 0)) return 0;
   if (lambda > 1e6f) return fmaxf(0.0f, floorf(lambda + sqrtf(lambda) * curand_normal(&st) + 0.5f));
   if (lambda >= 10.0f) return poisson_ptrs(st, lambda);
-  const float u = curand_uniform(&st);  // (0, 1]
+  const float u = philox_uniform(st);  // (0, 1]
   float p = expf(-lambda), F = p;
-  int k = 0;
-  while (u > F && k < 512) {
-    ++k;
-    p *= lambda / (float)k;
+  float k = 0.0f;  // counted in float: no conversion per step
+  while (u > F && k < 512.0f) {
+    k += 1.0f;
+    p *= lambda / k;
     const float next = F + p;
     if (!(next > F)) break;  // the CDF stopped growing in float (tail mass below its last ulp)
     F = next;
   }
-  return (float)k;
+  return k;
 }
 // The pixel's Philox stream at a place fixed by the cell's start time: a
 // 64-bit mix (the SplitMix64 finalizer) of the bits of t0, aligned to 16
