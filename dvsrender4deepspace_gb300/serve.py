@@ -70,8 +70,11 @@ class _Active:
         self.job, self.scene, self.sensor, self.reserved = job, scene, sensor, reserved
         self.cursor = 0.0
         self.chunks = []
-        # horizons of the job, counted once: float-rounded horizon ends (as the
-        # reference app's float time_resolution) must not add a horizon at the end
+        # horizons of the job, counted once.  A job covers duration / time_resolution
+        # whole horizons; a ratio a rounding above an integer (a float time_resolution)
+        # adds none.  bin/dvs keeps the reference app's plain ceil, which then runs one
+        # more, very short horizon up to its end time (apps/main_dvs.cpp:82-84); served
+        # jobs have no such app counterpart, so they stop at the last whole horizon.
         self.total_h = max(1, math.ceil(job.duration / job.time_resolution - 1e-9))
         self.done_h = 0
 
