@@ -129,6 +129,66 @@ struct PixelRegsF {
   bool refractory;
 };
 
+// The FP32 forms of the parameters the no-event path reads, converted once per
+// chunk instead of per cell.
+struct PixelParamsF {
+  float charge, leak;
+  bool reset_noise;
+};
+__device__ __forceinline__ PixelParamsF pixel_params_f32(const PixelParams &p) {
+  return PixelParamsF{(float)p.charge_scale, (float)p.reference_leak, p.reset_noise_std > 0};
+}
+
+// The FP64 parts of advance_pixel_f32 are separate, non-inlined functions:
+// inlined, the compiler hoisted parts of them (promotions of the FP32 state,
+// FP64 compares) into the no-event path, where they ran on every cell --
+// 30-44 FP64 instructions per warp and cell, on a GPU whose FP64 rate is a
+// small fraction of its FP32 rate.  Called only where the arithmetic needs
+// them (an event, a refractory reset, a nonzero leak); same operations, same
+// results.
+template <class Rng>
+__device__ __noinline__ float reset_noise_draw(double stddev, Rng &rng) {
+  return (float)(stddev * curand_normal_double(&rng));
+}
+// The leak extremum (FP64): the time at which the leaking reference stops
+// approaching the receptor, as a new segment end if it comes first.
+__device__ __noinline__ float leak_segment_end(const PixelParams &p, float rate, float u, float boundary) {
+  const double rate_d = rate, x = exp((double)u), target = rate_d + p.charge_scale * p.reference_leak;
+  if (x > target && target > rate_d) {
+    double extremum;
+    if (rate_d > 0) extremum = -p.charge_scale / rate_d * log((1.0 / target - 1.0 / rate_d) / (1.0 / x - 1.0 / rate_d));
+    else extremum = p.charge_scale * (1.0 / target - 1.0 / x);
+    if (extremum > 1e-15 && extremum < (double)boundary) return (float)extremum;
+  }
+  return boundary;
+}
+// The crossing time in FP64 from the FP32 state, as an offset into the segment,
+// and the receptor log at that time (FP32).
+struct Crossing {
+  double hi;
+  float u;
+};
+__device__ __noinline__ Crossing crossing_f64(const PixelParams &p, float rate, float u, float ref, float level,
+                                              float boundary, bool immediate, int polarity) {
+  const double rate_d = rate, ud = u, refd = ref, leveld = level, bnd = boundary;
+  double lo = 0, hi = bnd;
+  if (immediate) hi = 0;
+  else if (p.reference_leak == 0) {
+    const double target_inverse = exp(-(refd + leveld)), initial_inverse = exp(-ud);
+    if (rate_d > 0) {
+      const double stationary_inverse = 1.0 / rate_d;
+      hi = -p.charge_scale / rate_d * log1p((target_inverse - initial_inverse) / (initial_inverse - stationary_inverse));
+    } else hi = p.charge_scale * (target_inverse - initial_inverse);
+    hi = fmin(bnd, fmax(0.0, hi));
+  } else
+    for (int j = 0; j < 48; ++j) {
+      const double mid = (lo + hi) * .5;
+      const double cm = receptor_log_at(ud, rate_d, mid, p.charge_scale) - refd + p.reference_leak * mid;
+      if (polarity ? cm >= leveld : cm <= leveld) hi = mid; else lo = mid;
+    }
+  return Crossing{hi, (float)receptor_log_at(ud, rate_d, hi, p.charge_scale)};
+}
+
 // Time inside the cell is an FP32 offset from the cell start (t0) and the
 // refractory deadline an FP32 offset too, formed from the FP64 deadline only
 // while the pixel is still refractory, so the no-event path has no FP64
@@ -136,10 +196,10 @@ struct PixelRegsF {
 // its warp the whole instruction); absolute event times and deadlines are
 // formed in FP64 only when an event happens.
 template <class Rng>
-__device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, float rate, double t0, float dt,
-                                 double *out_t, int8_t *out_p, int capacity, Rng &rng) {
+__device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, const PixelParamsF &pf, float rate, double t0,
+                                 float dt, double *out_t, int8_t *out_p, int capacity, Rng &rng) {
   if (!(dt > 0)) return 0;
-  const float charge = (float)p.charge_scale, leak = (float)p.reference_leak;
+  const float charge = pf.charge, leak = pf.leak;
   int count = 0;
   // a deadline in the past gives ref_off <= 0, which no offset in the cell is below
   float off = 0.0f, ref_off = -1.0f;
@@ -158,26 +218,18 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, float rate
       s.reference_log = u;
       if (off < dt || off == ref_off) {
         if (off >= ref_off && s.reset_pending) {
-          if (p.reset_noise_std > 0) s.reference_log += (float)(p.reset_noise_std * curand_normal_double(&rng));
+          if (pf.reset_noise) s.reference_log += reset_noise_draw(p.reset_noise_std, rng);
           s.reset_pending = false;
         }
       }
       if (off >= dt) break;
     } else if (s.reset_pending) {
-      if (p.reset_noise_std > 0) s.reference_log += (float)(p.reset_noise_std * curand_normal_double(&rng));
+      if (pf.reset_noise) s.reference_log += reset_noise_draw(p.reset_noise_std, rng);
       s.reset_pending = false;
     }
     const float remaining = dt - off;
     float boundary = remaining;
-    if (leak > 0) {  // leak extremum in FP64 (it places the segment end)
-      const double rate_d = rate, x = exp((double)u), target = rate_d + p.charge_scale * p.reference_leak;
-      if (x > target && target > rate_d) {
-        double extremum;
-        if (rate_d > 0) extremum = -p.charge_scale / rate_d * log((1.0 / target - 1.0 / rate_d) / (1.0 / x - 1.0 / rate_d));
-        else extremum = p.charge_scale * (1.0 / target - 1.0 / x);
-        if (extremum > 1e-15 && extremum < (double)boundary) boundary = (float)extremum;
-      }
-    }
+    if (leak > 0) boundary = leak_segment_end(p, rate, u, boundary);  // FP64: it places the segment end
     const float c0 = u - s.reference_log;
     const float ub = receptor_log_at_f(u, rate, boundary, charge);
     const float cb = ub - s.reference_log + leak * boundary;
@@ -194,24 +246,10 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, float rate
       continue;
     }
     if (count == capacity) return -1;
-    // crossing time in FP64 from the FP32 state
-    const double rate_d = rate, ud = u, refd = s.reference_log, leveld = level, bnd = boundary;
-    double lo = 0, hi = bnd;
-    if (c0 >= s.threshold_pos || c0 <= -s.threshold_neg) hi = 0;
-    else if (p.reference_leak == 0) {
-      const double target_inverse = exp(-(refd + leveld)), initial_inverse = exp(-ud);
-      if (rate_d > 0) {
-        const double stationary_inverse = 1.0 / rate_d;
-        hi = -p.charge_scale / rate_d * log1p((target_inverse - initial_inverse) / (initial_inverse - stationary_inverse));
-      } else hi = p.charge_scale * (target_inverse - initial_inverse);
-      hi = fmin(bnd, fmax(0.0, hi));
-    } else
-      for (int j = 0; j < 48; ++j) {
-        const double mid = (lo + hi) * .5;
-        const double cm = receptor_log_at(ud, rate_d, mid, p.charge_scale) - refd + p.reference_leak * mid;
-        if (polarity ? cm >= leveld : cm <= leveld) hi = mid; else lo = mid;
-      }
-    u = (float)receptor_log_at(ud, rate_d, hi, p.charge_scale);
+    const Crossing x = crossing_f64(p, rate, u, s.reference_log, level, boundary,
+                                    c0 >= s.threshold_pos || c0 <= -s.threshold_neg, polarity);
+    const double hi = x.hi;
+    u = x.u;
     const double t_event = t0 + (double)off + hi;
     off = fminf(dt, off + (float)hi);
     out_t[count] = t_event;

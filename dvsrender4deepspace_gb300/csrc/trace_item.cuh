@@ -124,6 +124,7 @@ __device__ __forceinline__ void circuit_rank(int r, int n, const int32_t *rank_l
                  (float)st.threshold_pos[k], (float)st.threshold_neg[k], st.reset_pending[k] != 0, true};
     const int pixel = kPhilox ? st.pixel[k] : 0;
     const float e_rad = (float)photo.electrons_per_radiance, dark = (float)photo.dark_electrons;
+    const PixelParamsF pf = pixel_params_f32(p);
     const float *chunk_f = photo.chunk_f32 ? reinterpret_cast<const float *>(radiance) : nullptr;
     for (int c = 0; c < nc; ++c) {
       const Cell cell = cells[c0 + c];
@@ -136,10 +137,10 @@ __device__ __forceinline__ void circuit_rank(int r, int n, const int32_t *rank_l
       if (kPhilox) {
         curandStatePhilox4_32_10_t ph = philox_at(photo.seed, pixel, cell.t0);
         if (photo.shot_noise) rate = poisson_electrons_philox(ph, rate * dt) / dt;
-        emitted = advance_pixel_f32(s, p, rate, cell.t0, dt, my_t + cnt, my_p + cnt, max_events - cnt, ph);
+        emitted = advance_pixel_f32(s, p, pf, rate, cell.t0, dt, my_t + cnt, my_p + cnt, max_events - cnt, ph);
       } else {
         if (photo.shot_noise) rate = (float)poisson_electrons(rng, (double)(rate * dt)) / dt;
-        emitted = advance_pixel_f32(s, p, rate, cell.t0, dt, my_t + cnt, my_p + cnt, max_events - cnt, rng);
+        emitted = advance_pixel_f32(s, p, pf, rate, cell.t0, dt, my_t + cnt, my_p + cnt, max_events - cnt, rng);
       }
       if (emitted == -1) { failed = kErrCapacity; break; }
       if (emitted == -2) { failed = kErrStalled; break; }
