@@ -356,10 +356,80 @@ struct SahBuilder {
   }
 };
 
+// ---- 8-wide collapse by slot budgets (collapse 1) -----------------------------------
+// D(b, j), j = 1..8: the least surface-area cost of covering binary subtree b
+// with at most j children of one wide node.  A binary leaf as a child costs
+// kTriCost x area x triangles; an inner node as one child is a wide node of its
+// own, kNodeCost x area + S(b, 8); with j >= 2 slots the subtree may instead be
+// split between its two children, S(b, j) = min over k of D(left, k) +
+// D(right, j - k).  The wide node made from inner node b takes the children of
+// S(b, 8).  Both builders number a parent before its children, so one pass in
+// decreasing index fills the tables.  (Areas are the binary boxes' half areas;
+// the ratio to the root's area is the probability a ray enters the box.)
+constexpr float kNodeCost = 1.0f, kTriCost = 1.0f;
+struct SlotPlan {
+  std::vector<float> d;       // D(b, j) at 8 * b + j - 1
+  std::vector<uint8_t> pick;  // for j >= 2: 0 = b itself as one child, k = k slots to the left
+  std::vector<uint8_t> wide;  // k of S(b, 8), the split the wide node made from b uses
+  void emit(const std::vector<BinNode> &bin, int32_t b, int j, int32_t *kids, int &nk) const {
+    const int k = (bin[b].count > 0 || j == 1) ? 0 : pick[8 * (size_t)b + j - 1];
+    if (k == 0) {
+      kids[nk++] = b;
+      return;
+    }
+    emit(bin, bin[b].left, k, kids, nk);
+    emit(bin, bin[b].right, j - k, kids, nk);
+  }
+  void children(const std::vector<BinNode> &bin, int32_t b, int32_t *kids, int &nk) const {
+    const int k = wide[b];
+    emit(bin, bin[b].left, k, kids, nk);
+    emit(bin, bin[b].right, kBvhWidth - k, kids, nk);
+  }
+};
+SlotPlan plan_slots(const std::vector<BinNode> &bin, int32_t root) {
+  SlotPlan p;
+  const size_t n = bin.size();
+  p.d.assign(8 * n, 0.0f);
+  p.pick.assign(8 * n, 0);
+  p.wide.assign(n, 1);
+  for (size_t i = n; i-- > (size_t)root;) {
+    const BinNode &b = bin[i];
+    float *d = &p.d[8 * i];
+    if (b.count > 0) {
+      const float leaf = kTriCost * b.area * (float)b.count;
+      for (int j = 0; j < 8; ++j) d[j] = leaf;
+      continue;
+    }
+    const float *dl = &p.d[8 * (size_t)b.left], *dr = &p.d[8 * (size_t)b.right];
+    float s[9];  // S(b, j), j = 2..8
+    uint8_t sk[9];
+    for (int j = 2; j <= 8; ++j) {
+      s[j] = std::numeric_limits<float>::infinity();
+      sk[j] = 1;
+      for (int k = 1; k < j; ++k) {
+        const float c = dl[k - 1] + dr[j - k - 1];
+        if (c < s[j]) { s[j] = c; sk[j] = (uint8_t)k; }
+      }
+    }
+    p.wide[i] = sk[8];
+    d[0] = kNodeCost * b.area + s[8];
+    for (int j = 2; j <= 8; ++j) {
+      if (s[j] < d[0]) {
+        d[j - 1] = s[j];
+        p.pick[8 * i + j - 1] = sk[j];
+      } else {
+        d[j - 1] = d[0];
+        p.pick[8 * i + j - 1] = 0;
+      }
+    }
+  }
+  return p;
+}
+
 }  // namespace
 
 bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf_size, int builder, BvhBuild &out,
-               std::string &error) {
+               std::string &error, int collapse) {
   const auto t_start = std::chrono::steady_clock::now();
   if (nt == 0 || nv == 0) { error = "empty mesh"; return false; }
   if (nt > (size_t(1) << 28)) { error = "mesh exceeds 2^28 triangles"; return false; }
@@ -444,6 +514,7 @@ bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf
   }
 
   // 4. collapse to kBvhWidth-wide, breadth first
+  const SlotPlan plan = collapse == 1 ? plan_slots(bin, root) : SlotPlan{};
   std::vector<BvhNode> nodes;
   nodes.reserve(bin.size() / (kBvhWidth - 1) + 2);
   std::vector<int32_t> queue;  // binary node per wide node
@@ -457,6 +528,8 @@ bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf
     int nk = 0;
     if (bin[b].count > 0) {
       kids[nk++] = b;  // a leaf root: one leaf child
+    } else if (collapse == 1) {
+      plan.children(bin, b, kids, nk);
     } else {
       kids[nk++] = bin[b].left;
       kids[nk++] = bin[b].right;

@@ -97,7 +97,7 @@ struct BvhBuild {
 // builder 1 splits Morton-ordered ranges at their highest differing code bit.
 // Returns false with a message on invalid input.
 bool build_bvh(const float *vertices, size_t n_vertices, const uint32_t *indices, size_t n_triangles,
-               int leaf_size, int builder, BvhBuild &out, std::string &error);
+               int leaf_size, int builder, BvhBuild &out, std::string &error, int collapse = 0);
 
 // The precision-format copy of a built tree (same node indices).  Fails when a
 // leaf's first triangle or size does not fit the link, or when a decoded box

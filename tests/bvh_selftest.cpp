@@ -41,11 +41,12 @@ static float add_rounded(float origin, uint16_t off, bool up) {
 }
 
 int main(int argc, char **argv) {
-  if (argc != 4 && argc != 5) return 2;
+  if (argc < 4 || argc > 6) return 2;
   const unsigned seed = (unsigned)std::atoi(argv[1]);
   const int n = std::atoi(argv[2]);
   const double scale = std::atof(argv[3]);
-  const int builder = argc == 5 ? std::atoi(argv[4]) : 0;  // 0 binned SAH, 1 Morton radix
+  const int builder = argc >= 5 ? std::atoi(argv[4]) : 0;   // 0 binned SAH, 1 Morton radix
+  const int collapse = argc == 6 ? std::atoi(argv[5]) : 0;  // 0 greedy, 1 slot budgets
   std::mt19937 rng(seed);
   std::uniform_real_distribution<double> jitter(-0.3, 0.3), height(0.0, 1.0);
   std::vector<float> V;
@@ -65,7 +66,7 @@ int main(int argc, char **argv) {
   const size_t nt = I.size() / 3;
   BvhBuild bvh;
   std::string err;
-  if (!build_bvh(V.data(), V.size() / 3, I.data(), nt, 2, builder, bvh, err)) {
+  if (!build_bvh(V.data(), V.size() / 3, I.data(), nt, 2, builder, bvh, err, collapse)) {
     std::printf("build failed: %s\n", err.c_str());
     return 1;
   }
