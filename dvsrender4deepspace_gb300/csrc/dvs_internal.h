@@ -95,9 +95,11 @@ struct BvhBuild {
 
 // Binary tree collapsed to an 8-wide tree; builder 0 splits by binned SAH,
 // builder 1 splits Morton-ordered ranges at their highest differing code bit.
-// Returns false with a message on invalid input.
+// collapse 1 (the default) chooses the wide nodes by surface-area cost over
+// slot budgets, collapse 0 opens the largest-area child greedily.  Returns
+// false with a message on invalid input.
 bool build_bvh(const float *vertices, size_t n_vertices, const uint32_t *indices, size_t n_triangles,
-               int leaf_size, int builder, BvhBuild &out, std::string &error, int collapse = 0);
+               int leaf_size, int builder, BvhBuild &out, std::string &error, int collapse = 1);
 
 // The precision-format copy of a built tree (same node indices).  Fails when a
 // leaf's first triangle or size does not fit the link, or when a decoded box

@@ -46,7 +46,7 @@ int main(int argc, char **argv) {
   const int n = std::atoi(argv[2]);
   const double scale = std::atof(argv[3]);
   const int builder = argc >= 5 ? std::atoi(argv[4]) : 0;   // 0 binned SAH, 1 Morton radix
-  const int collapse = argc == 6 ? std::atoi(argv[5]) : 0;  // 0 greedy, 1 slot budgets
+  const int collapse = argc == 6 ? std::atoi(argv[5]) : 1;  // 1 slot budgets (default), 0 greedy
   std::mt19937 rng(seed);
   std::uniform_real_distribution<double> jitter(-0.3, 0.3), height(0.0, 1.0);
   std::vector<float> V;

@@ -24,12 +24,14 @@ def selftest(tmp_path_factory):
     return exe
 
 
+@pytest.mark.parametrize("collapse", [1, 0])  # slot budgets (default), greedy largest-area
 @pytest.mark.parametrize("builder", [0, 1])  # binned SAH splits, Morton radix splits
 @pytest.mark.parametrize("seed,n,scale,slack", [(1, 64, 1000.0, 2e-3),       # a 1 km tile
                                                 (2, 160, 40960.0, 2e-3),     # the 4096^2 terrain's extent
                                                 (3, 40, 300000.0, None)])    # offsets beyond 65504
-def test_quantised_bounds_enclose_the_fp32_tree(selftest, seed, n, scale, slack, builder):
-    out = subprocess.run([selftest, str(seed), str(n), str(scale), str(builder)], capture_output=True, text=True)
+def test_quantised_bounds_enclose_the_fp32_tree(selftest, seed, n, scale, slack, builder, collapse):
+    out = subprocess.run([selftest, str(seed), str(n), str(scale), str(builder), str(collapse)], capture_output=True,
+                         text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     fields = out.stdout.split()
     assert fields[0] == "nodes" and int(fields[1]) > 0 and int(fields[5]) > 0
@@ -48,3 +50,21 @@ def test_sah_splits_lower_the_surface_area_cost(selftest):
         f = out.stdout.split()
         got[builder] = float(f[9]) + float(f[11])
     assert got[0] < got[1], got  # builder 0: SAH
+
+
+def test_slot_budget_collapse_lowers_the_node_cost(selftest):
+    """The slot-budget collapse minimises the wide nodes' total area (the
+    surface-area model's node visits) over every way of grouping the binary
+    tree into nodes of at most 8 children; the greedy largest-area collapse is
+    one of those groupings, so it can only cost as much or more.  Leaves, and so
+    the triangle tests, are the same."""
+    for builder in (0, 1):
+        got = {}
+        for collapse in (0, 1):
+            out = subprocess.run([selftest, "7", "300", "20000.0", str(builder), str(collapse)], capture_output=True,
+                                 text=True)
+            assert out.returncode == 0, out.stdout + out.stderr
+            f = out.stdout.split()
+            got[collapse] = (float(f[9]), float(f[11]), int(f[5]))
+        assert got[1][0] <= got[0][0] * (1 + 1e-6) and got[1][2] == got[0][2], got
+        assert abs(got[1][1] - got[0][1]) <= 1e-9 * got[0][1], got
