@@ -82,16 +82,10 @@ METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency v
 # (dram__bytes_read.sum + dram__bytes_write.sum) per pixel-cell.  Radiance
 # writes still held in L2 when the kernel ends are not in the DRAM count.
 TRACE_WARP_INSTRUCTIONS_PER_RAY = {
-    ("orbit", "reference", "morton", 32, 2): 82860353469 / 1768685229,
-    ("orbit", "reference", "sah", 32, 2): 82092603783 / 1768685229,
-    ("precision", "half+watertight", "morton", 16, 2): 1680561156231 / 29471262018,
-    ("precision", "half+watertight", "sah", 32, 2): 1499392428478 / 29471262019,
+    ("precision", "half+watertight", "sah", 32, 2): 1500654289593 / 29471262019,
 }
 TRACE_DRAM_BYTES_PER_PIXEL_CELL = {
-    ("precision", "half+watertight", "sah", 32, 2): (70099456 + 221486592) / (921600 * 64),
-    ("orbit", "reference", "morton", 32, 2): (13664256 + 177929728) / (89960 * 640),
-    ("orbit", "reference", "sah", 32, 2): (15953408 + 179276800) / (89960 * 640),
-    ("precision", "half+watertight", "morton", 16, 2): (71625984 + 221396224) / (921600 * 64),
+    ("precision", "half+watertight", "sah", 32, 2): (67016192 + 221377024) / (921600 * 64),
 }
 GB300_SMS = 152
 
