@@ -832,7 +832,8 @@ def run_batching(args):
                        "horizons_per_step": H, "time_resolution": dt, "circuit_precision": args.circuit,
                        "geometry": args.geometry, "parallelism": "dp%d (independent batches)" % world,
                        "l2": "inputs larger than L2 (radiance chunks %.1f GB)"
-                             % (len(members) * H * 10 * w["camera"]["width"] * w["camera"]["height"] * 8 / 1e9)},
+                             % (len(members) * H * 10 * w["camera"]["width"] * w["camera"]["height"]
+                                * (4 if args.circuit.startswith("fp32") else 8) / 1e9)},
             # per active member-step: its intervals and their circuit cells (24 B each) in, its
             # events (24 B each on the device side) and status words out
             "e2e": {"value": b_rays / b_wall / 1e6, "unit": "Mrays/s",
