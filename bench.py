@@ -83,9 +83,11 @@ METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency v
 # writes still held in L2 when the kernel ends are not in the DRAM count.
 TRACE_WARP_INSTRUCTIONS_PER_RAY = {
     ("precision", "half+watertight", "sah", 32, 2): 1500654289593 / 29471262019,
+    ("orbit", "reference", "sah", 32, 2): 82134327371 / 1768685229,
 }
 TRACE_DRAM_BYTES_PER_PIXEL_CELL = {
     ("precision", "half+watertight", "sah", 32, 2): (67016192 + 221377024) / (921600 * 64),
+    ("orbit", "reference", "sah", 32, 2): (15039232 + 179304192) / (89960 * 640),
 }
 GB300_SMS = 152
 
