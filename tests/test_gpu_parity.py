@@ -276,12 +276,44 @@ def cell_count(t0, t1, circuit_step):
     return math.ceil((t1 - t0) / float(np.float32(circuit_step)))
 
 
-@pytest.mark.parametrize("shot", [0, 1])
-def test_sensor_batch_invariance(shot):
-    scene, phys = plane_sensor(photon_shot_noise=shot)
+@pytest.mark.parametrize("circuit", ["fp64", "fp32"])
+def test_sensor_with_reference_leak_against_the_fp64_oracle(circuit):
+    """A leaking reference (reset_leakage_a > 0, pixel_model.hpp:46-59): the
+    segment ends at the leak extremum and the crossing time comes from the
+    48-step bisection, both FP64, out of line in the FP32 circuit.  A 64x48
+    crop of the DAVIS camera through the interior pulse against the FP64 oracle:
+    identical polarity sequences outside the margin classes, timestamps within
+    1 us."""
+    V, N, I = plane_mesh()
+    crop = dict(DAVIS, width=64, height=48, cx=DAVIS["cx"] - 141, cy=DAVIS["cy"] - 106)
+    scene = DeviceScene(V, N, I, crop, 1, DAVIS_HAPKE)
+    phys = davis_physic(threshold_std=0, photon_shot_noise=0, max_events_per_step=64, readout_bandwidth=0,
+                        readout_latency=0, random_seed=42, reset_leakage_a=1.3e-14)  # reference leak ~20 /s
+    start, end = dict(POSE, intensity_rate=8e6), dict(POSE, intensity_rate=-8e6)
+    ivs = [(POSE, POSE, 0, 0.001), (start, end, 0.001, 0.003)]
+    s = EventSensor(scene, phys, circuit_precision=circuit)
+    s.initialize(POSE, 0)
+    ev = s.process_many(ivs)
+    ors = O.OracleSensor(O.OracleScene(V, N, I, crop, 1, DAVIS_HAPKE, fp64=True), phys, margin=True)
+    ors.initialize(POSE, 0)
+    oev = ors.process(ivs)
+    assert len(oev) > 1000
+    report = compare_event_streams(ev, oev, ors.margins(), crop["width"])
+    assert report["unclassified_mismatches"] == 0, report
+    assert report["max_timestamp_error_s"] < 1e-6, report
+
+
+@pytest.mark.parametrize("circuit", ["fp64", "fp32", "fp32-philox"])
+@pytest.mark.parametrize("shot,reset", [(0, 0), (1, 0), (1, 1)])
+def test_sensor_batch_invariance(shot, reset, circuit):
+    """Batching cannot change the events, with photon shot noise and kTC reset
+    noise (reset_thermal_noise, drawn after each refractory period; out of line
+    in the FP32 circuits) on or off, for every circuit and noise stream."""
+    scene, phys = plane_sensor(photon_shot_noise=shot, reset_thermal_noise=reset)
     bright = dict(POSE, intensity=2000)
     ivs = [(POSE, POSE, 0, 0.001), (bright, bright, 0.001, 0.002), (POSE, POSE, 0.002, 0.003)]
-    grouped, separate = EventSensor(scene, phys), EventSensor(scene, phys)
+    grouped = EventSensor(scene, phys, circuit_precision=circuit)
+    separate = EventSensor(scene, phys, circuit_precision=circuit)
     grouped.initialize(POSE, 0)
     separate.initialize(POSE, 0)
     individual = np.concatenate([separate.process(iv) for iv in ivs])
