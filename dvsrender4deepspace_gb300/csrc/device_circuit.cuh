@@ -209,6 +209,13 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, const Pixe
   }
   float u = s.receptor_log;
   int passes = 0;
+  // With a constant rate the receptor moves monotonically toward it, so once
+  // it has reached the leak target (the extremum) it stays past it for the
+  // rest of the cell: there is at most one extremum split per cell.  The
+  // FP32 state at the split can round to a hair before the target, and
+  // recomputing the extremum from it would give ever shorter splits that an
+  // FP32 offset cannot even add; so after one split it is not looked for again.
+  bool past_extremum = false;
   while (off < dt) {
     if (++passes > 4096) return -2;  // bounded: see kErrStalled
     if (off < ref_off) {
@@ -229,7 +236,7 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, const Pixe
     }
     const float remaining = dt - off;
     float boundary = remaining;
-    if (leak > 0) boundary = leak_segment_end(p, rate, u, boundary);  // FP64: it places the segment end
+    if (leak > 0 && !past_extremum) boundary = leak_segment_end(p, rate, u, boundary);  // FP64: places the end
     const float c0 = u - s.reference_log;
     const float ub = receptor_log_at_f(u, rate, boundary, charge);
     const float cb = ub - s.reference_log + leak * boundary;
@@ -242,7 +249,8 @@ __device__ int advance_pixel_f32(PixelRegsF &s, const PixelParams &p, const Pixe
     if (polarity < 0) {
       u = ub;
       s.reference_log -= leak * boundary;
-      off = boundary == remaining ? dt : off + boundary;
+      if (boundary == remaining) off = dt;
+      else { off += boundary; past_extremum = true; }
       continue;
     }
     if (count == capacity) return -1;
