@@ -667,6 +667,138 @@ def run_serving(args):
     return 0
 
 
+READOUT_KERNELS_PER_SUBMIT = 1 + 12 * 3 + 3 + 3  # keys, 12 x (histogram, scan, scatter), FIFO, release
+
+
+def readout_events(rng, n, t):
+    """One batch of the readout workload: n events of a 1280x720 sensor within
+    64 us from t, uniform over pixels, polarities and times."""
+    from dvsrender4deepspace_gb300._capi import EVENT_DTYPE
+    ev = np.zeros(n, EVENT_DTYPE)
+    ev["timestamp"] = t + rng.uniform(0.0, 64e-6, n)
+    ev["x"] = rng.integers(0, 1280, n)
+    ev["y"] = rng.integers(0, 720, n)
+    ev["polarity"] = rng.integers(0, 2, n)
+    return ev
+
+
+def run_readout(args, n_events=1 << 22):
+    """Readout workload: the device FIFO (dvs_device_readout_*) alone on batches
+    of 4,194,304 events of a 1280x720 sensor within 64 us each, through an
+    unbounded bus (1e12 s^-1, no latency) so that every batch takes the
+    parallel path (radix sort by (t, y, x), max-plus scan, occupancy, release);
+    the configs' 5e6 s^-1 bus would saturate at that density and take the
+    serial drop path.  `value` is events per second of device time (CUDA
+    events around the submit's kernels); `e2e` the same through the host call
+    with the events in host memory (upload, kernels, download of the delivered
+    events).  The reference arm times the oracle's serial FIFO (stable sort
+    and queue, the reference's event_readout.cpp) on one batch."""
+    import torch
+    from dvsrender4deepspace_gb300.build import build
+    from dvsrender4deepspace_gb300.raycast import EventReadout
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    build()
+    rng = np.random.default_rng(5)
+    batches = [readout_events(rng, n_events, 1.0 + 64e-6 * b) for b in range(args.warmup + args.steps)]
+    r = EventReadout(1e12, 0.0, 1 << 24, device=True, max_batch=n_events)
+    dev_ms, wall = [], 0.0
+    for b, ev in enumerate(batches):
+        if b == args.warmup:
+            clocks = ClockSampler(local).__enter__()
+            torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = r.submit(ev, 1.0 + 64e-6 * (b + 1))
+        dt = time.perf_counter() - t0
+        if len(out) != n_events:
+            raise RuntimeError("device readout delivered %d of %d events" % (len(out), n_events))
+        if b >= args.warmup:
+            dev_ms.append(r.last_ms())
+            wall += dt
+    clocks.__exit__()
+    ms = sum(dev_ms) / len(dev_ms)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    alg = n_events * 2 * 24.0
+    cb = None
+    if not args.no_cpu_baseline:
+        cb = readout_cpu_baseline(batches[:1])
+    n = args.steps
+    line = {"metric": METRIC, "value": n_events / (ms / 1e3), "unit": "events/s", "n_gpus": 1, "steps": n,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "readout", "events_per_batch": n_events, "width": 1280, "height": 720,
+                       "batch_window_s": 64e-6, "bandwidth": 1e12, "latency": 0.0, "capacity": 1 << 24,
+                       "l2": "inputs larger than L2: each batch's events are 100.7 MB on the device, "
+                             "its sort buffers 3 x 67 MB"},
+            "e2e": {"value": n_events * n / wall, "unit": "events/s", "h2d_bytes_per_step": n_events * 24 + 16,
+                    "d2h_bytes_per_step": n_events * batches[0].dtype.itemsize},
+            "roofline": {"bound": "hbm", "kernel": "device readout (radix sort, max-plus scan, release)",
+                         "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / (ms / 1e3) / 1e9 / peak, "traffic": None, "algorithmic_bytes": alg,
+                         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+            "gpu_launches": READOUT_KERNELS_PER_SUBMIT * n, "clocks": clocks.summary(), "cpu_baseline": cb}
+    print(json.dumps(line))
+    return 0
+
+
+def run_readout_reference(args, n_events=1 << 22):
+    """The readout workload's reference arm: the oracle's serial FIFO (the
+    reference's event_readout.cpp restated) on the host, one batch per step."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    rng = np.random.default_rng(5)
+    res = []
+    for b in range(args.warmup + args.steps):
+        cb = readout_cpu_baseline([readout_events(rng, n_events, 1.0 + 64e-6 * b)], first=b)
+        if b >= args.warmup:
+            res.append(cb)
+    value = statistics.median(r["value"] for r in res)
+    cbl = dict(res[-1], value=value)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n_events / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "readout", "events_per_batch": n_events, "width": 1280, "height": 720,
+                       "batch_window_s": 64e-6, "bandwidth": 1e12, "latency": 0.0, "capacity": 1 << 24},
+            "cpu_baseline": cbl,
+            "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def readout_cpu_baseline(batches, first=0):
+    """The oracle's serial FIFO (the reference's event_readout.cpp: stable sort
+    by (t, y, x), then the queue) on the host, one thread."""
+    import ctypes as C
+    from oracle import oracle as O
+    lib = O.load(False)
+    s, n = 0.0, 0
+    for b, ev in enumerate(batches):
+        oev = np.zeros(len(ev), O.EVENT_DTYPE)
+        for f in O.EVENT_DTYPE.names:
+            oev[f] = ev[f]
+        out = np.zeros(len(ev), O.EVENT_DTYPE)
+        got = C.c_size_t()
+        r = lib.oracle_readout_create(1e12, 0.0, 1 << 24)
+        t0 = time.perf_counter()
+        lib.oracle_readout_submit(r, oev.ctypes.data, len(oev), 1.0 + 64e-6 * (first + b + 1), out.ctypes.data,
+                                  len(out), C.byref(got))
+        s += time.perf_counter() - t0
+        lib.oracle_readout_destroy(r)
+        n += len(ev)
+        if got.value != len(ev):
+            raise RuntimeError("oracle readout delivered %d of %d events" % (got.value, len(ev)))
+    return {"value": n / s, "unit": "events/s", "cores": 1, "kind": "port",
+            "sample": "%d events (one batch), %.1f s of CPU work" % (n, s)}
+
+
 def batching_members(n, seed, light, intensity):
     """The batching config's trajectories: constant-altitude arcs with altitude
     U(0.5, 5) km, speed U(10, 200) m/s, heading U(0, 360) deg, yaw rate
@@ -867,7 +999,8 @@ def main():
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="precision", choices=sorted(WORKLOADS) + ["serving", "batching"])
+    ap.add_argument("--workload", default="precision",
+                    choices=sorted(WORKLOADS) + ["serving", "batching", "readout"])
     ap.add_argument("--batch-members", type=int, default=64)
     ap.add_argument("--batch-horizons", type=int, default=16, help="horizons per member per batching step")
     ap.add_argument("--batch-precision-members", type=int, default=4,
@@ -905,7 +1038,11 @@ def main():
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving or multi-sensor "
                                                                   "batching layer"}))
             return 0
+        if args.workload == "readout":
+            return run_readout_reference(args)
         return run_reference(args)
+    if args.workload == "readout":
+        return run_readout(args)
     if args.workload == "serving":
         return run_serving(args)
     if args.workload == "batching":

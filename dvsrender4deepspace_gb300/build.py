@@ -8,6 +8,7 @@ every expression rounds as written.
 
     python -m dvsrender4deepspace_gb300.build        (or build() from Python)
 """
+import fcntl
 import os
 import shutil
 import subprocess
@@ -59,10 +60,20 @@ def up_to_date():
 
 
 def build(force=False, verbose=False):
-    """Compile the library unless it is newer than every source."""
+    """Compile the library unless it is newer than every source.  Processes
+    that find it stale at the same time (parallel test workers) build it one
+    at a time: the others wait on a lock file and find it fresh."""
     if not force and up_to_date():
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
+    with open(os.path.join(OUT_DIR, "build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not force and up_to_date():
+            return LIB
+        return _build(verbose)
+
+
+def _build(verbose):
     inc = ["-I", CSRC, "-I", APPS, "-I", os.path.join(ROOT, "include")]
     xhost = ",".join(HOST_FLAGS)
     cmds = []

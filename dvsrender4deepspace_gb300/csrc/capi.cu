@@ -146,10 +146,11 @@ struct DeviceReadout {
     };
     const size_t o_kt0 = take(8 * max_batch), o_kt1 = take(8 * max_batch), o_yx0 = take(4 * max_batch),
                  o_yx1 = take(4 * max_batch), o_i0 = take(4 * max_batch), o_i1 = take(4 * max_batch),
-                 o_hist = take(4 * 256 * (size_t)max_grid), o_ring = take(sizeof(DevEvent) * ring),
-                 o_bmax = take(8 * (size_t)max_grid), o_comp = take(8 * max_batch), o_del = take(8 * max_batch),
+                 o_hist = take(4 * 256 * (size_t)max_grid), o_dtot = take(4 * 256), o_vary = take(8 * 2),
+                 o_ring = take(sizeof(DevEvent) * ring), o_bmax = take(8 * (size_t)max_grid),
+                 o_comp = take(8 * max_batch), o_del = take(8 * max_batch),
                  o_out = take(sizeof(DevEvent) * (ring + max_batch)), o_u64 = take(8 * 5), o_avail = take(8),
-                 o_i32 = take(4 * 5), o_plan = take(8 * 3);
+                 o_i32 = take(4 * 3), o_plan = take(8 * 3);
     cudaError_t e = cudaMalloc(&arena, off);
     if (e != cudaSuccess) return e;
     bytes = off;
@@ -161,12 +162,12 @@ struct DeviceReadout {
     sort.idx[0] = reinterpret_cast<unsigned *>(b + o_i0);
     sort.idx[1] = reinterpret_cast<unsigned *>(b + o_i1);
     sort.hist = reinterpret_cast<unsigned *>(b + o_hist);
+    sort.digit_total = reinterpret_cast<unsigned *>(b + o_dtot);
+    sort.varying = reinterpret_cast<unsigned long long *>(b + o_vary);
     int32_t *i32 = reinterpret_cast<int32_t *>(b + o_i32);
-    sort.cur = i32;
-    sort.skip = i32 + 1;
-    fifo.overflow = i32 + 2;
-    fifo.status = i32 + 3;
-    fifo.out_count = i32 + 4;
+    fifo.overflow = i32;
+    fifo.status = i32 + 1;
+    fifo.out_count = i32 + 2;
     unsigned long long *u64 = reinterpret_cast<unsigned long long *>(b + o_u64);
     fifo.head = u64;
     fifo.tail = u64 + 1;
@@ -179,7 +180,7 @@ struct DeviceReadout {
     fifo.capacity = capacity;
     fifo.step = bandwidth > 0 ? 1.0 / bandwidth : 0.0;
     fifo.latency = latency;
-    fifo.block_max = reinterpret_cast<double *>(b + o_bmax);
+    fifo.block_max = reinterpret_cast<unsigned long long *>(b + o_bmax);
     fifo.completion = reinterpret_cast<double *>(b + o_comp);
     fifo.delivery = reinterpret_cast<double *>(b + o_del);
     fifo.plan = reinterpret_cast<long long *>(b + o_plan);
@@ -225,8 +226,8 @@ struct DeviceReadout {
     grid = (int)std::min<size_t>(608, std::max<size_t>(1, (events + 4095) / 4096));
   }
   size_t bytes = 0;  // device memory held
-  // kernels of one submit: keys, 12 radix passes of 4, the scan's 3, commit, release, advance
-  int launches() const { return 1 + 12 * 4 + (fifo.step > 0 ? 3 : 0) + 3; }
+  // kernels of one submit: keys, 12 radix passes of 3, the scan's 3, commit, release, advance
+  int launches() const { return readout_submit_launches(fifo.step > 0); }
 };
 
 // ---- handles --------------------------------------------------------------------

@@ -70,14 +70,16 @@ struct alignas(8) DevEvent {
 
 // Device readout (readout.cu).  Sort buffers for up to max_batch events:
 // keys (order-preserving bits of t, then y<<16|x) and source indices, double
-// buffered; cur selects the buffer that holds the current order, skip marks
-// a radix pass that moves nothing; hist: 256 x grid per-block digit counts.
+// buffered; which buffer holds the current order follows from `varying` (the
+// radix passes whose digit differs between events move the keys, the others
+// do nothing).
 struct ReadoutSort {
   unsigned long long *kt[2];
   unsigned *kyx[2];
   unsigned *idx[2];
-  int32_t *cur, *skip;
-  unsigned *hist;
+  unsigned long long *varying;  // [0]: OR over the batch of (time key ^ the first event's), [1]: the same for (y, x)
+  unsigned *hist;               // per pass: counts per digit and sort block (digit-major, 256 x grid), scanned in place
+  unsigned *digit_total;        // per pass: keys per digit (256)
 };
 // FIFO state and scratch.  ring: pending delivered events, ring_size a power
 // of two; head/tail: monotone positions of the pending entries; plan: the
@@ -88,7 +90,8 @@ struct ReadoutFifo {
   unsigned long long *head, *tail, *peak, *peak_batch, *dropped;
   double *available;
   double step, latency;  // 1 / bandwidth (0: no FIFO delay), latency
-  double *block_max, *completion, *delivery;
+  unsigned long long *block_max;  // per sort block: the order-preserving key of max_k (t_k - k/B)
+  double *completion, *delivery;
   int32_t *overflow, *status, *out_count;
   long long *plan;
   DevEvent *out;         // released events of the last submit or drain
@@ -101,6 +104,8 @@ struct ReadoutFifo {
 cudaError_t launch_readout_submit(const DevEvent *events, const int32_t *count, ReadoutSort s, ReadoutFifo f,
                                   const double *now, int grid, cudaStream_t st);
 cudaError_t launch_readout_drain(ReadoutFifo f, int grid, cudaStream_t st);
+// Kernels one launch_readout_submit enqueues (delayed: a bandwidth > 0 FIFO).
+int readout_submit_launches(bool delayed);
 
 // Error word bits (host maps them to DVS_ERR_* with capacity first, as
 // event_sensor.cu:300-301 tests code 1 before any other code).
