@@ -89,6 +89,10 @@ TRACE_DRAM_BYTES_PER_PIXEL_CELL = {
     ("precision", "half+watertight", "sah", 32, 2): (67016192 + 221377024) / (921600 * 64),
     ("orbit", "reference", "sah", 32, 2): (15039232 + 179304192) / (89960 * 640),
 }
+# ncu DRAM counters (dram__bytes_read.sum + dram__bytes_write.sum) of the 44
+# launches of one device-readout batch of 4,194,304 events (the readout
+# workload's batch), per event: the sort's passes, the FIFO scan and the release.
+READOUT_DRAM_BYTES_PER_EVENT = (1489862912 + 310624256) / 4194304
 GB300_SMS = 152
 
 
@@ -120,7 +124,8 @@ def readout_roofline(peak, n_events=1 << 22, batches=4):
     return {"bound": "hbm", "kernel": "device readout (radix sort, max-plus scan, release)",
             "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s", "frac": alg / (ms / 1e3) / 1e9 / peak,
             "ms_per_batch": ms, "events_per_batch": n_events, "events_per_s": n_events / (ms / 1e3),
-            "algorithmic_bytes": alg}
+            "algorithmic_bytes": alg, "traffic": READOUT_DRAM_BYTES_PER_EVENT * n_events,
+            "traffic_gbs": READOUT_DRAM_BYTES_PER_EVENT * n_events / (ms / 1e3) / 1e9}
 
 
 def dist_env():
@@ -667,7 +672,7 @@ def run_serving(args):
     return 0
 
 
-READOUT_KERNELS_PER_SUBMIT = 1 + 12 * 3 + 3 + 3  # keys, 12 x (histogram, scan, scatter), FIFO, release
+READOUT_KERNELS_PER_SUBMIT = 2 + 12 * 3 + 3 + 3  # keys, packing, 12 x (histogram, scan, scatter), FIFO, release
 
 
 def readout_events(rng, n, t):
@@ -741,7 +746,9 @@ def run_readout(args, n_events=1 << 22):
                     "d2h_bytes_per_step": n_events * batches[0].dtype.itemsize},
             "roofline": {"bound": "hbm", "kernel": "device readout (radix sort, max-plus scan, release)",
                          "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": alg / (ms / 1e3) / 1e9 / peak, "traffic": None, "algorithmic_bytes": alg,
+                         "frac": alg / (ms / 1e3) / 1e9 / peak, "traffic": READOUT_DRAM_BYTES_PER_EVENT * n_events,
+                         "traffic_gbs": READOUT_DRAM_BYTES_PER_EVENT * n_events / (ms / 1e3) / 1e9,
+                         "algorithmic_bytes": alg,
                          "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
             "gpu_launches": READOUT_KERNELS_PER_SUBMIT * n, "clocks": clocks.summary(), "cpu_baseline": cb}
     print(json.dumps(line))

@@ -146,7 +146,7 @@ struct DeviceReadout {
     };
     const size_t o_kt0 = take(8 * max_batch), o_kt1 = take(8 * max_batch), o_yx0 = take(4 * max_batch),
                  o_yx1 = take(4 * max_batch), o_i0 = take(4 * max_batch), o_i1 = take(4 * max_batch),
-                 o_hist = take(4 * 256 * (size_t)max_grid), o_dtot = take(4 * 256), o_vary = take(8 * 2),
+                 o_hist = take(4 * 256 * (size_t)max_grid), o_dtot = take(4 * 256), o_vary = take(8 * 3),
                  o_ring = take(sizeof(DevEvent) * ring), o_bmax = take(8 * (size_t)max_grid),
                  o_comp = take(8 * max_batch), o_del = take(8 * max_batch),
                  o_out = take(sizeof(DevEvent) * (ring + max_batch)), o_u64 = take(8 * 5), o_avail = take(8),
@@ -226,7 +226,7 @@ struct DeviceReadout {
     grid = (int)std::min<size_t>(608, std::max<size_t>(1, (events + 4095) / 4096));
   }
   size_t bytes = 0;  // device memory held
-  // kernels of one submit: keys, 12 radix passes of 3, the scan's 3, commit, release, advance
+  // kernels of one submit: keys, packing, 12 radix passes of 3, the scan's 3, commit, release, advance
   int launches() const { return readout_submit_launches(fifo.step > 0); }
 };
 

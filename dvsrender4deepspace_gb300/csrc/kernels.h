@@ -77,7 +77,8 @@ struct ReadoutSort {
   unsigned long long *kt[2];
   unsigned *kyx[2];
   unsigned *idx[2];
-  unsigned long long *varying;  // [0]: OR over the batch of (time key ^ the first event's), [1]: the same for (y, x)
+  unsigned long long *varying;  // [0]: OR over the batch of (time key ^ the first event's), [1]: the same for
+                                // (y, x), [2]: the first event's time key
   unsigned *hist;               // per pass: counts per digit and sort block (digit-major, 256 x grid), scanned in place
   unsigned *digit_total;        // per pass: keys per digit (256)
 };

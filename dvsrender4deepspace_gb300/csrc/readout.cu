@@ -4,12 +4,15 @@
 //   1. Order: a stable LSD radix sort of the batch by (t, y, x) -- 8-bit
 //      digits over the 32-bit (y, x) key, then over the 64 order-preserving
 //      bits of t.  The key kernel ORs every key against the first event's, so
-//      a digit that is the same for every event (the high bytes of t within a
-//      batch, the high byte of y) is known before its pass: such a pass does
-//      nothing at all, and every kernel derives from the same mask which of
-//      the two key buffers its pass reads.  Per active pass: a digit histogram
-//      per block, one block per digit scanning that digit's counts over the
-//      blocks, and a stable scatter whose blocks add the digits' totals.
+//      the bits that vary within the batch are known before any pass.  Bits
+//      that never vary decide nothing: when the varying ranges of t, y and x
+//      fit 64 bits (a 64 us batch of a 1280x720 sensor: 38 + 10 + 11), they
+//      are packed into one key and the (y, x) key is not moved at all; a
+//      digit that is the same for every key makes its pass do nothing; and
+//      every kernel derives from the same words which of the two key buffers
+//      its pass reads.  Per active pass: a digit histogram per block, one
+//      block per digit scanning that digit's counts over the blocks, and a
+//      stable scatter whose blocks add the digits' totals.
 //   2. Completions: with bandwidth B the FIFO's serial recurrence
 //      c_k = max(c_{k-1}, t_k) + 1/B (c_{-1} = the carried availability A)
 //      equals the max-plus scan c_k = (k+1)/B + max(A, max_{j<=k} (t_j - j/B)):
@@ -58,22 +61,59 @@ __device__ __forceinline__ unsigned yx_key(const DevEvent &e) {
 __device__ __forceinline__ unsigned long long *kt_of(const ReadoutSort &s, int b) { return b ? s.kt[1] : s.kt[0]; }
 __device__ __forceinline__ unsigned *kyx_of(const ReadoutSort &s, int b) { return b ? s.kyx[1] : s.kyx[0]; }
 __device__ __forceinline__ unsigned *idx_of(const ReadoutSort &s, int b) { return b ? s.idx[1] : s.idx[0]; }
-// Bit p set: pass p's digit differs between events (passes 0-3: bytes of the
-// (y, x) key, 4-11: bytes of the time key).
-__device__ __forceinline__ unsigned pass_mask(const ReadoutSort &s) {
+// The sort key of a batch.  Bits that are the same for every event of the
+// batch decide no comparison, so dropping them keeps the (t, y, x) order:
+// when the varying ranges of the time key (its low bt bits: all higher bits
+// are the first event's), of y (low by bits) and of x (low bx bits) fit 64
+// bits together, the batch sorts on one packed key t' << (by + bx) | y' << bx
+// | x' in the time-key buffers (passes 4-11, the (y, x) buffers unused);
+// otherwise on the time key and the (y, x) key (passes 0-3 over (y, x), 4-11
+// over t).  Every kernel derives the same layout from `varying`.
+__device__ __forceinline__ int bits_of(unsigned long long v) { return v ? 64 - __clzll((long long)v) : 0; }
+__device__ __forceinline__ unsigned long long low_mask(int b) { return b >= 64 ? ~0ull : (1ull << b) - 1ull; }
+struct KeyLayout {
+  bool packed;
+  int xbits, shift;              // packed: bits of x', and of y' and x' together
+  unsigned long long tmask;      // packed: the varying range of the time key
+  unsigned long long thigh;      // packed: the time key's bits above it (the first event's)
+  unsigned xmask, ymask;
+  unsigned long long vary_t;     // varying bits of the time-key buffers' keys (packed: of the packed key)
+  unsigned long long vary_yx;    // varying bits of the (y, x) keys (0 when packed)
+  unsigned mask;                 // bit p: pass p's digit differs between events
+};
+__device__ __forceinline__ unsigned long long pack_key(const KeyLayout &L, unsigned long long kt, unsigned kyx) {
+  return ((kt & L.tmask) << L.shift) | ((unsigned long long)((kyx >> 16) & L.ymask) << L.xbits) | (kyx & L.xmask);
+}
+__device__ __forceinline__ KeyLayout key_layout(const ReadoutSort &s) {
   const unsigned long long vt = s.varying[0], vyx = s.varying[1];
+  const int bt = bits_of(vt), bx = bits_of(vyx & 0xffffull), by = bits_of(vyx >> 16);
+  KeyLayout L;
+  L.packed = bt + bx + by <= 64;
+  L.xbits = bx;
+  L.shift = bx + by;
+  L.tmask = low_mask(bt);
+  L.thigh = s.varying[2] & ~L.tmask;
+  L.xmask = (unsigned)low_mask(bx);
+  L.ymask = (unsigned)low_mask(by);
+  L.vary_t = L.packed ? pack_key(L, vt, (unsigned)vyx) : vt;
+  L.vary_yx = L.packed ? 0ull : vyx;
   unsigned m = 0;
 #pragma unroll
   for (int p = 0; p < 4; ++p)
-    if ((vyx >> (8 * p)) & 0xffull) m |= 1u << p;
+    if ((L.vary_yx >> (8 * p)) & 0xffull) m |= 1u << p;
 #pragma unroll
   for (int p = 0; p < 8; ++p)
-    if ((vt >> (8 * p)) & 0xffull) m |= 1u << (4 + p);
-  return m;
+    if ((L.vary_t >> (8 * p)) & 0xffull) m |= 1u << (4 + p);
+  L.mask = m;
+  return L;
+}
+// The time key of a sorted key.
+__device__ __forceinline__ unsigned long long time_key_of(const KeyLayout &L, unsigned long long k) {
+  return L.packed ? L.thigh | ((k >> L.shift) & L.tmask) : k;
 }
 // The key buffer pass p reads: each active pass before it moved the keys once.
 __device__ __forceinline__ int buffer_before(unsigned mask, int pass) { return __popc(mask & ((1u << pass) - 1u)) & 1; }
-__device__ __forceinline__ int sorted_buffer(const ReadoutSort &s) { return __popc(pass_mask(s)) & 1; }
+__device__ __forceinline__ int sorted_buffer(const KeyLayout &L) { return __popc(L.mask) & 1; }
 __device__ __forceinline__ unsigned digit_of(int pass, unsigned long long kt, unsigned kyx) {
   return pass < 4 ? (kyx >> (8 * pass)) & 0xffu : (unsigned)(kt >> (8 * (pass - 4))) & 0xffu;
 }
@@ -109,8 +149,9 @@ __device__ __forceinline__ long long first_after(const double *a, long long k, d
 }
 
 // ---- sort ---------------------------------------------------------------------------
-// Keys of the batch in arrival order, and the OR of every key against the
-// first event's (*varying, zeroed before the launch).  256 threads.
+// Keys of the batch in arrival order, the OR of every key against the first
+// event's (varying[0..1], zeroed before the launch) and the first event's time
+// key (varying[2]).  256 threads.
 __global__ void __launch_bounds__(256) ro_keys_kernel(const DevEvent *events, const int32_t *count, ReadoutSort s) {
   __shared__ unsigned long long red[256 / 32][2];
   const int n = *count;
@@ -138,6 +179,7 @@ __global__ void __launch_bounds__(256) ro_keys_kernel(const DevEvent *events, co
     red[warp][1] = yx;
   }
   __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) s.varying[2] = kt0;
   if (threadIdx.x == 0) {
     unsigned long long a = 0, b = 0;
     for (int w = 0; w < 256 / 32; ++w) {
@@ -149,12 +191,21 @@ __global__ void __launch_bounds__(256) ro_keys_kernel(const DevEvent *events, co
   }
 }
 
+// Packed layout: the packed key replaces the time key, in place.
+__global__ void __launch_bounds__(256) ro_pack_kernel(const int32_t *count, ReadoutSort s) {
+  const KeyLayout L = key_layout(s);
+  if (!L.packed) return;  // grid-uniform
+  const int n = *count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    s.kt[0][i] = pack_key(L, s.kt[0][i], s.kyx[0][i]);
+}
+
 // A pass whose digit takes few values (at most 3 varying bits: <= 8 values,
 // e.g. the high byte of y) counts with lanes of the same digit adding once
 // (match_any), so they do not serialize on one shared counter; other passes
 // count with one shared atomic per key.
-__device__ __forceinline__ bool few_digit_values(const ReadoutSort &s, int pass) {
-  const unsigned long long v = pass < 4 ? s.varying[1] >> (8 * pass) : s.varying[0] >> (8 * (pass - 4));
+__device__ __forceinline__ bool few_digit_values(const KeyLayout &L, int pass) {
+  const unsigned long long v = pass < 4 ? L.vary_yx >> (8 * pass) : L.vary_t >> (8 * (pass - 4));
   return __popcll(v & 0xffull) <= 3;
 }
 // Adds one key of digit d (live) to h; called by every lane of the warp.
@@ -186,22 +237,28 @@ __device__ __forceinline__ unsigned block_exclusive_scan_256(unsigned v, unsigne
 // Per block: the histogram of the pass's digit over its tile, digit-major
 // (hist[d * grid + b]).
 __global__ void __launch_bounds__(kSortThreads) ro_hist_kernel(int pass, const int32_t *count, ReadoutSort s) {
+  constexpr int kPer = 4;  // keys per thread and round: their loads are in flight together
   __shared__ unsigned h[kDigits];
-  const unsigned mask = pass_mask(s);
-  if (!((mask >> pass) & 1u)) return;  // grid-uniform: the digit is every key's
-  const int n = *count, cur = buffer_before(mask, pass);
-  const bool aggregate = few_digit_values(s, pass);
+  const KeyLayout L = key_layout(s);
+  if (!((L.mask >> pass) & 1u)) return;  // grid-uniform: the digit is every key's
+  const int n = *count, cur = buffer_before(L.mask, pass);
+  const bool aggregate = few_digit_values(L, pass);
   const unsigned long long *kt = kt_of(s, cur);
   const unsigned *kyx = kyx_of(s, cur);
   h[threadIdx.x] = 0;
   __syncthreads();
   int begin, end;
   tile_of(n, blockIdx.x, begin, end);
-  for (int r0 = begin; r0 < end; r0 += kSortThreads) {  // block-uniform rounds: every lane reaches the match
-    const int i = r0 + (int)threadIdx.x;
-    unsigned d = kFull;
-    if (i < end) d = pass < 4 ? (kyx[i] >> (8 * pass)) & 0xffu : (unsigned)(kt[i] >> (8 * (pass - 4))) & 0xffu;
-    count_digit(h, d, i < end, aggregate);
+  for (int r0 = begin; r0 < end; r0 += kPer * kSortThreads) {  // block-uniform rounds: every lane reaches the match
+    unsigned d[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int i = r0 + j * kSortThreads + (int)threadIdx.x;
+      d[j] = kFull;
+      if (i < end) d[j] = pass < 4 ? (kyx[i] >> (8 * pass)) & 0xffu : (unsigned)(kt[i] >> (8 * (pass - 4))) & 0xffu;
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) count_digit(h, d[j], d[j] != kFull, aggregate);
   }
   __syncthreads();
   s.hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
@@ -212,7 +269,7 @@ __global__ void __launch_bounds__(kSortThreads) ro_hist_kernel(int pass, const i
 // digit's total.
 __global__ void __launch_bounds__(kScanThreads) ro_scan_kernel(int pass, int grid, ReadoutSort s) {
   __shared__ unsigned warp_sum[kScanThreads / 32];
-  if (!((pass_mask(s) >> pass) & 1u)) return;  // grid-uniform
+  if (!((key_layout(s).mask >> pass) & 1u)) return;  // grid-uniform
   const int b = threadIdx.x, lane = b & 31, warp = b >> 5;
   unsigned *row = s.hist + (size_t)blockIdx.x * grid;
   const unsigned v = b < grid ? row[b] : 0u;
@@ -255,10 +312,10 @@ __global__ void __launch_bounds__(kSortThreads) ro_scatter_kernel(int pass, cons
   __shared__ unsigned warp_count[2][kWarps][kDigits];
   __shared__ unsigned long long skt[kTileKeys];
   __shared__ unsigned skyx[kTileKeys], sidx[kTileKeys];
-  const unsigned mask = pass_mask(s);
-  if (!((mask >> pass) & 1u)) return;  // grid-uniform
-  const int n = *count, cur = buffer_before(mask, pass);
-  const bool aggregate = few_digit_values(s, pass);
+  const KeyLayout L = key_layout(s);
+  if (!((L.mask >> pass) & 1u)) return;  // grid-uniform
+  const int n = *count, cur = buffer_before(L.mask, pass);
+  const bool aggregate = few_digit_values(L, pass), yx = !L.packed;  // packed: no (y, x) keys to move
   const unsigned long long *kt_in = kt_of(s, cur);
   const unsigned *kyx_in = kyx_of(s, cur), *idx_in = idx_of(s, cur);
   unsigned long long *kt_out = kt_of(s, 1 - cur);
@@ -280,7 +337,7 @@ __global__ void __launch_bounds__(kSortThreads) ro_scatter_kernel(int pass, cons
       dg[j] = kFull;  // no key
       if (q < tn) {
         k_t[j] = kt_in[c0 + q];
-        k_yx[j] = kyx_in[c0 + q];
+        if (yx) k_yx[j] = kyx_in[c0 + q];
         k_i[j] = idx_in[c0 + q];
         dg[j] = digit_of(pass, k_t[j], k_yx[j]);
       }
@@ -310,7 +367,7 @@ __global__ void __launch_bounds__(kSortThreads) ro_scatter_kernel(int pass, cons
         for (int w = 0; w < warp; ++w) before += warp_count[buf][w][d];
         const unsigned local = toff[d] + run[d] + before + rank_in_warp;
         skt[local] = k_t[j];
-        skyx[local] = k_yx[j];
+        if (yx) skyx[local] = k_yx[j];
         sidx[local] = k_i[j];
       }
       unsigned quarter_total = 0;
@@ -328,11 +385,11 @@ __global__ void __launch_bounds__(kSortThreads) ro_scatter_kernel(int pass, cons
       const int q = j * kSortThreads + t;
       if (q < tn) {
         const unsigned long long a = skt[q];
-        const unsigned b = skyx[q];
+        const unsigned b = yx ? skyx[q] : 0u;
         const unsigned d = digit_of(pass, a, b);
         const unsigned g = base[d] + (unsigned)q - toff[d];
         kt_out[g] = a;
-        kyx_out[g] = b;
+        if (yx) kyx_out[g] = b;
         idx_out[g] = sidx[q];
       }
     }
@@ -362,20 +419,21 @@ __device__ __forceinline__ unsigned long long warp_max_key(unsigned long long v)
   for (int off = 16; off > 0; off >>= 1) v = u64_max(v, __shfl_xor_sync(kFull, v, off));
   return v;
 }
-// Key of u_k = t_k - k/B, t_k from the sorted time key.
-__device__ __forceinline__ unsigned long long slack_key(unsigned long long kt, int k, double step) {
-  return time_key(key_time(kt) - (double)k * step);
+// Key of u_k = t_k - k/B, t_k from the sorted key.
+__device__ __forceinline__ unsigned long long slack_key(const KeyLayout &L, unsigned long long key, int k, double step) {
+  return time_key(key_time(time_key_of(L, key)) - (double)k * step);
 }
 
 // Per block: the maximum of u_k over its tile.
 __global__ void __launch_bounds__(256) ro_fifo_max_kernel(const int32_t *count, ReadoutSort s, ReadoutFifo f) {
   __shared__ unsigned long long red[256 / 32];
-  const int n = *count, cur = sorted_buffer(s);
+  const KeyLayout L = key_layout(s);
+  const int n = *count, cur = sorted_buffer(L);
   const unsigned long long *kt = kt_of(s, cur);
   int begin, end;
   tile_of(n, blockIdx.x, begin, end);
   unsigned long long m = 0;
-  for (int k = begin + threadIdx.x; k < end; k += blockDim.x) m = u64_max(m, slack_key(kt[k], k, f.step));
+  for (int k = begin + threadIdx.x; k < end; k += blockDim.x) m = u64_max(m, slack_key(L, kt[k], k, f.step));
   m = warp_max_key(m);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
@@ -392,7 +450,8 @@ __global__ void __launch_bounds__(256) ro_fifo_scan_kernel(const int32_t *count,
   constexpr int kWarps = 256 / 32;
   __shared__ unsigned long long wmax[kWarps];
   __shared__ unsigned long long carry_in;
-  const int n = *count, cur = sorted_buffer(s);
+  const KeyLayout L = key_layout(s);
+  const int n = *count, cur = sorted_buffer(L);
   const unsigned long long *kt = kt_of(s, cur);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int begin, end;
@@ -412,7 +471,7 @@ __global__ void __launch_bounds__(256) ro_fifo_scan_kernel(const int32_t *count,
   for (int r0 = begin; r0 < end; r0 += blockDim.x) {  // block-uniform rounds
     const int k = r0 + (int)threadIdx.x;
     const bool live = k < end;
-    unsigned long long incl = live ? slack_key(kt[k], k, f.step) : 0ull;
+    unsigned long long incl = live ? slack_key(L, kt[k], k, f.step) : 0ull;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {  // inclusive prefix maximum within the warp
       const unsigned long long v = __shfl_up_sync(kFull, incl, off);
@@ -437,14 +496,15 @@ __global__ void __launch_bounds__(256) ro_fifo_scan_kernel(const int32_t *count,
 __global__ void __launch_bounds__(256) ro_fifo_occupancy_kernel(const int32_t *count, ReadoutSort s, ReadoutFifo f) {
   __shared__ unsigned red_peak[256 / 32];
   __shared__ int red_over[256 / 32];
-  const int n = *count, cur = sorted_buffer(s);
+  const KeyLayout L = key_layout(s);
+  const int n = *count, cur = sorted_buffer(L);
   const unsigned long long *kt = kt_of(s, cur);
   const unsigned long long head = *f.head, tail = *f.tail;
   // occupancy + 1 <= ring entries (< 2^25) + batch events (< 2^31): fits 32 bits
   unsigned peak = 0;
   int over = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const double t = key_time(kt[k]);
+    const double t = key_time(time_key_of(L, kt[k]));
     const long long lo = first_after(f.delivery, k, t);  // earlier arrivals still queued at t: [lo, k)
     const long long occ = carried_after(f, head, tail, t) + (k - lo);
     over |= occ >= (long long)f.capacity;
@@ -482,7 +542,8 @@ __global__ void ro_fifo_commit_kernel(const DevEvent *events, const int32_t *cou
     *f.out_count = 0;
     return;
   }
-  const int n = *count, cur = sorted_buffer(s);
+  const KeyLayout L = key_layout(s);
+  const int n = *count, cur = sorted_buffer(L);
   unsigned long long head = *f.head, tail = *f.tail;
   if (f.step <= 0) {
     f.plan[0] = 0;
@@ -496,7 +557,7 @@ __global__ void ro_fifo_commit_kernel(const DevEvent *events, const int32_t *cou
     // time; deliveries only grow along the queue and an event is delivered
     // after its own arrival, so both releases are prefixes at the threshold
     // max(now, last arrival).
-    const double until = n > 0 ? fmax(now, key_time(kt_of(s, cur)[n - 1])) : now;
+    const double until = n > 0 ? fmax(now, key_time(time_key_of(L, kt_of(s, cur)[n - 1]))) : now;
     const long long lo = first_after(f.delivery, n, until);
     const long long carried_out = (long long)(tail - head) - carried_after(f, head, tail, until);
     if ((long long)(tail - head) - carried_out + (n - lo) > (long long)f.ring_size) {
@@ -549,7 +610,7 @@ __global__ void ro_fifo_commit_kernel(const DevEvent *events, const int32_t *cou
 __global__ void ro_fifo_release_kernel(const DevEvent *events, ReadoutSort s, ReadoutFifo f) {
   const long long carried_out = f.plan[0], batch_out = f.plan[1], accepted = f.plan[2];
   if (carried_out < 0) return;
-  const int cur = sorted_buffer(s);
+  const int cur = sorted_buffer(key_layout(s));
   const unsigned long long head = *f.head, tail = *f.tail;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < carried_out + accepted; i += stride) {
@@ -585,14 +646,15 @@ __global__ void ro_drain_commit_kernel(ReadoutFifo f) {
 
 }  // namespace
 
-int readout_submit_launches(bool delayed) { return 1 + kPasses * 3 + (delayed ? 3 : 0) + 3; }
+int readout_submit_launches(bool delayed) { return 2 + kPasses * 3 + (delayed ? 3 : 0) + 3; }
 
 cudaError_t launch_readout_submit(const DevEvent *events, const int32_t *count, ReadoutSort s, ReadoutFifo f,
                                   const double *now, int grid, cudaStream_t st) {
   if (grid < 1 || grid > kScanThreads) return cudaErrorInvalidValue;
-  cudaError_t e = cudaMemsetAsync(s.varying, 0, 2 * sizeof(unsigned long long), st);
+  cudaError_t e = cudaMemsetAsync(s.varying, 0, 3 * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   ro_keys_kernel<<<grid, 256, 0, st>>>(events, count, s);
+  ro_pack_kernel<<<grid, 256, 0, st>>>(count, s);
   for (int pass = 0; pass < kPasses; ++pass) {
     ro_hist_kernel<<<grid, kSortThreads, 0, st>>>(pass, count, s);
     ro_scan_kernel<<<kDigits, kScanThreads, 0, st>>>(pass, grid, s);

@@ -86,6 +86,32 @@ def test_device_readout_equals_the_host_fifo(bandwidth, latency, capacity, ties)
         assert host.dropped() > 0
 
 
+@pytest.mark.parametrize("bandwidth,latency,capacity", [
+    (0.0, 0.0, 1000),                # no FIFO delay
+    (1e12, 0.0, 1 << 24),            # unbounded bus: the parallel path, nothing pending
+    (5e9, 18e-9, 1_000_000),         # busy bus, no drops: completions carried across batches
+    (5e8, 1e-6, 20_000),             # saturated bus with drops (serial pass)
+])
+def test_device_readout_packed_keys_equal_the_host_fifo(bandwidth, latency, capacity):
+    """Batches of one 64 us window of a 1280x720 sensor at t ~ 1 s (the
+    readout workload's shape): the varying bits of t, y and x fit one 64-bit
+    key, so the device sorts on the packed key (the wide batches of the test
+    above take the two-key sort)."""
+    rng = np.random.default_rng(23)
+    dev = EventReadout(bandwidth, latency, capacity, device=True, max_batch=300_000)
+    host = EventReadout(bandwidth, latency, capacity)
+    t = 1.0
+    for batch in range(5):
+        n = int(rng.integers(1, 250_000)) if batch != 2 else 1
+        ev = random_events(rng, n, t, t + 64e-6, ties=batch == 3 and bandwidth == 0)  # ties: (y, x) decides
+        t += 64e-6
+        same_stream(dev.submit(ev, t), host.submit(ev, t), bandwidth > 0)
+        assert dev.dropped() == host.dropped() and dev.peak_queue() == host.peak_queue()
+    same_stream(dev.drain(), host.drain(), bandwidth > 0)
+    if capacity == 20_000:
+        assert host.dropped() > 0
+
+
 def test_device_readout_refuses_oversized_batches():
     r = EventReadout(1e6, 0.0, 100, device=True, max_batch=16)
     with pytest.raises(ValueError):
