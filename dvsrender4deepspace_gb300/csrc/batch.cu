@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(128, kRays == 2 ? DVS_TRACE_PAIR_MIN_BLOCKS : 
     trace_jobs_kernel(const __grid_constant__ TraceJobs P) {
   __shared__ int s_code[kWarpsPerBlock][kStackSlots];
   __shared__ float s_t[kWarpsPerBlock][kStackSlots];
-  __shared__ double s_cos4[kWarpsPerBlock][kCos4Table];
+  __shared__ SubraySample s_subrays[kWarpsPerBlock][kSubrayTable];
   __shared__ long long s_first[kMaxBatchJobs];
   __shared__ long long s_base;
   for (int j = threadIdx.x; j < P.n_jobs; j += blockDim.x) s_first[j] = P.jobs[j].first_item;
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(128, kRays == 2 ? DVS_TRACE_PAIR_MIN_BLOCKS : 
       const TraceJob &J = P.jobs[j];
       trace_cells_item<kRadiance, kRays, kGeo>(J.view, J.n_pix, nullptr, J.poses, J.c0, J.nc, J.cw_log2,
                                                J.radiance, nullptr, J.counters, item - s_first[j], s_code[wib],
-                                               s_t[wib], s_cos4[wib]);
+                                               s_t[wib], s_subrays[wib]);
     }
   }
 }

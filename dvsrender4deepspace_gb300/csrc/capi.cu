@@ -1559,16 +1559,20 @@ int dvs_sensor_set_tuning(dvs_sensor *s, int32_t cells_per_warp, int32_t rays_pe
 }  // extern "C"
 
 // Second stage of the autotuner: the circuit-step chunk.  The optics ->
-// circuit pipeline of every pixel over the first (up to 64) cells of the
-// staged batch, with the chosen packet shape, for chunks of 1, 1/2, 1/4 and
-// 1/8 of them (at least 4 cells), each run from the same shadow copy of the
-// circuit state; the real state, RNG and time are untouched.  Keeps the
-// current chunk unless another is >= 3 % faster.
+// circuit pipeline of every pixel over the first cells of the staged batch --
+// as many as the batch's default chunk, at least 64 (or the whole batch) --
+// with the chosen packet shape, for chunks of 1, 1/2, 1/4 and 1/8 of them (at
+// least 4 cells), each run from the same shadow copy of the circuit state;
+// the real state, RNG and time are untouched.  Keeps the default chunk unless
+// another is >= 3 % faster.  (A trial of at most 64 cells could not see that a
+// small sensor's whole 640-cell batch in one launch beats ten 64-cell launches:
+// one launch keeps a block's consecutive packets on the same pixel.)
 static int autotune_chunk(dvs_sensor *s, size_t n_cells, dvs_tuning *out) {
   const int n = s->pixels();
-  const int ncs = (int)std::min<size_t>(n_cells, 64);
   size_t def_chunk;
   int cw_log2;
+  chunk_shape(s, n_cells, (size_t)n, def_chunk, cw_log2);
+  const int ncs = (int)std::min<size_t>(n_cells, std::max<size_t>(64, def_chunk));
   chunk_shape(s, (size_t)ncs, (size_t)n, def_chunk, cw_log2);
   std::vector<int> cands;
   for (int c = ncs; c >= 4 && cands.size() < 4; c /= 2) cands.push_back(c);

@@ -727,6 +727,15 @@ enum SampleMode : int { kRadiance = 0, kRadianceDepth = 1, kDepthOnly = 2 };
 __device__ __forceinline__ double cos4_of(float px, float py) {
   return 1.0 / ((1.0 + px * px + py * py) * (1.0 + px * px + py * py));
 }
+// One sub-ray of a pixel: its image-plane coordinates and FP64 cos^4, the
+// same values subray_x/subray_y/cos4_of give.  A warp whose lanes all sample
+// one pixel forms them once per sub-ray in shared memory instead of once per
+// lane and ray (an integer division by the sub-ray count and four IEEE
+// divisions per ray).
+struct SubraySample {
+  double cos4;
+  float px, py;
+};
 __device__ __forceinline__ float subray_x(const SceneView &S, int px_i, int sx) {
   return (px_i + (sx + .5f) / S.samples - .5f - S.cx) / S.fx;
 }
@@ -735,12 +744,11 @@ __device__ __forceinline__ float subray_y(const SceneView &S, int py_i, int sy) 
 }
 
 // sample_pixel (device_optics.cuh:73-94) for one lane of a converged warp.
-// cos4_table: when every lane of the warp samples the same pixel, the FP64
-// cos^4 of each sub-ray is computed once per warp (shared memory) instead of
-// once per lane; otherwise nullptr.
+// subrays: when every lane of the warp samples the same pixel, its sub-rays'
+// coordinates and cos^4, formed once per warp (shared memory); otherwise nullptr.
 template <int kMode, int kGeo = kGeoReference>
 __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool active, const CellPose &pose,
-                                           int *stack_code, float *stack_t, const double *cos4_table) {
+                                           int *stack_code, float *stack_t, const SubraySample *subrays) {
   PixelSample out{0.0, -1.0f, true, 0u, 0u};
   double depth = 0;
   int valid_depth = 0;
@@ -752,8 +760,8 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
   const float3 lnorm = normalize(light);  // as in sample_pixel_group
   for (int sy = 0; sy < ss; ++sy)
     for (int sx = 0; sx < ss; ++sx) {
-      const float px = subray_x(S, px_i, sx);
-      const float py = subray_y(S, py_i, sy);
+      const float px = subrays ? subrays[sy * ss + sx].px : subray_x(S, px_i, sx);
+      const float py = subrays ? subrays[sy * ss + sx].py : subray_y(S, py_i, sy);
       const float3 ray = normalize(rotate_ray(pose, f3(px, -py, -1)));
       const HitRecord hit = trace_nearest_packet<kGeo>(S, origin, ray, active && out.valid, stack_code, stack_t);
       if (active && out.valid) ++out.primary;
@@ -790,7 +798,7 @@ __device__ PixelSample sample_pixel_packet(const SceneView &S, int pixel, bool a
           if (lit) ++out.shadow;
           const bool occ = trace_shadow_packet<kGeo>(S, sorigin, light, lit, hit.tri, stack_code, stack_t);
           if (lit && !occ) {
-            const double cos4 = cos4_table ? cos4_table[sy * ss + sx] : cos4_of(px, py);
+            const double cos4 = subrays ? subrays[sy * ss + sx].cos4 : cos4_of(px, py);
             // hapke_directional_reflectance (hapke.hpp:153-157)
             const float3 n = normalize(normal), l = lnorm, v = normalize(-ray);
             const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo, r0, S.hapke, hc);
@@ -1094,7 +1102,7 @@ __device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], 
 // the ray counts are those of the one-ray loop.
 template <int kMode, int R, int kGeo = kGeoReference>
 __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool active, const CellPose &pose,
-                                          int *stack_code, float *stack_t, const double *cos4_table) {
+                                          int *stack_code, float *stack_t, const SubraySample *subrays) {
   PixelSample out{0.0, -1.0f, true, 0u, 0u};
   double depth = 0;
   int valid_depth = 0;
@@ -1112,9 +1120,14 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
     bool live[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const int sx = (j + r) % ss, sy = (j + r) / ss;
-      px[r] = subray_x(S, px_i, sx);
-      py[r] = subray_y(S, py_i, sy);
+      if (subrays) {
+        px[r] = subrays[j + r].px;
+        py[r] = subrays[j + r].py;
+      } else {
+        const int sx = (j + r) % ss, sy = (j + r) / ss;
+        px[r] = subray_x(S, px_i, sx);
+        py[r] = subray_y(S, py_i, sy);
+      }
       ray[r] = normalize(rotate_ray(pose, f3(px[r], -py[r], -1)));
       org[r] = origin;
       live[r] = active && out.valid;
@@ -1171,7 +1184,7 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
         for (int r = 0; r < R; ++r) {
           if (lit[r]) ++out.shadow;
           if (lit[r] && !occ[r]) {
-            const double cos4 = cos4_table ? cos4_table[j + r] : cos4_of(px[r], py[r]);
+            const double cos4 = subrays ? subrays[j + r].cos4 : cos4_of(px[r], py[r]);
             const float3 n = normalize(normal[r]), l = lnorm, v = normalize(-ray[r]);
             const float n_h = hapke_reflectance(dot(n, l), dot(n, v), dot(l, v), albedo[r], r0[r], S.hapke, hc);
             out.radiance += fmaxf(0, n_h * pose.intensity) * cos4;

@@ -73,11 +73,11 @@ __global__ void __launch_bounds__(128, kRays == 4   ? DVS_TRACE_QUAD_MIN_BLOCKS
                        int cw_log2, double *radiance, float *depth_out, unsigned long long *counters) {
   __shared__ int s_code[kWarpsPerBlock][kStackSlots];
   __shared__ float s_t[kWarpsPerBlock][kStackSlots];
-  __shared__ double s_cos4[kWarpsPerBlock][kCos4Table];
+  __shared__ SubraySample s_subrays[kWarpsPerBlock][kSubrayTable];
   const int wib = threadIdx.x >> 5;
   const long long warp = (long long)(blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   trace_cells_item<kMode, kRays, kGeo>(S, n_pix, rank_list, poses, c0, nc, cw_log2, radiance, depth_out, counters,
-                                       warp, s_code[wib], s_t[wib], s_cos4[wib]);
+                                       warp, s_code[wib], s_t[wib], s_subrays[wib]);
 }
 
 // Few poses per pixel: one warp per (pixel, pose), lanes carrying the

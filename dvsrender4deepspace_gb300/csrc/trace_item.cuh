@@ -15,7 +15,7 @@ constexpr int kWarpsPerBlock = 4;  // all ray kernels launch 128 threads
 #ifndef DVS_TRACE_MIN_BLOCKS
 #define DVS_TRACE_MIN_BLOCKS 5
 #endif
-constexpr int kCos4Table = 256;    // sub-rays per pixel with a shared cos^4 table (ss <= 16)
+constexpr int kSubrayTable = 256;  // sub-rays per pixel with a shared sub-ray table (ss <= 16)
 
 // Element o of a radiance chunk: double, or float when the chunk feeds an
 // FP32 circuit (which uses the value as a float: the same bits, half the bytes).
@@ -41,7 +41,8 @@ template <int kMode, int kRays, int kGeo>
 __device__ __forceinline__ void trace_cells_item(const SceneView &S, int n_pix, const int32_t *rank_list,
                                                  const CellPose *poses, int c0, int nc, int cw_log2,
                                                  double *radiance, float *depth_out, unsigned long long *counters,
-                                                 long long warp, int *stack_code, float *stack_t, double *cos4) {
+                                                 long long warp, int *stack_code, float *stack_t,
+                                                 SubraySample *subrays) {
   // n_pix pixels: all Morton ranks, or the ranks listed in rank_list
   const int lane = threadIdx.x & 31;
   const int cw = 1 << cw_log2, ppw = 32 >> cw_log2;
@@ -55,18 +56,20 @@ __device__ __forceinline__ void trace_cells_item(const SceneView &S, int n_pix, 
   const int pixel = rank < n_pix ? __ldg(S.pixel_of_rank + (rank_list ? rank_list[rank] : rank)) : 0;
   const CellPose pose = poses[c0 + (active ? cell : 0)];
   const int ss2 = S.samples * S.samples;
-  // one pixel per warp: its sub-rays' FP64 cos^4 once per warp
-  const bool shared_cos4 = kMode != kDepthOnly && cw_log2 == 5 && ss2 <= kCos4Table;
-  if (shared_cos4) {
-    for (int j = lane; j < ss2; j += 32)
-      cos4[j] = cos4_of(subray_x(S, pixel % S.width, j % S.samples), subray_y(S, pixel / S.width, j / S.samples));
+  // one pixel per warp: its sub-rays' coordinates and FP64 cos^4 once per warp
+  const bool shared_subrays = kMode != kDepthOnly && cw_log2 == 5 && ss2 <= kSubrayTable;
+  if (shared_subrays) {
+    for (int j = lane; j < ss2; j += 32) {
+      const float x = subray_x(S, pixel % S.width, j % S.samples), y = subray_y(S, pixel / S.width, j / S.samples);
+      subrays[j] = SubraySample{cos4_of(x, y), x, y};
+    }
     __syncwarp();
   }
   const PixelSample s =
       kRays > 1 ? sample_pixel_group<kMode, kRays, kGeo>(S, pixel, active, pose, stack_code, stack_t,
-                                                         shared_cos4 ? cos4 : nullptr)
+                                                         shared_subrays ? subrays : nullptr)
                 : sample_pixel_packet<kMode, kGeo>(S, pixel, active, pose, stack_code, stack_t,
-                                                   shared_cos4 ? cos4 : nullptr);
+                                                   shared_subrays ? subrays : nullptr);
   if (active) {
     const size_t o = (size_t)cell * n_pix + rank;
     store_radiance(S, radiance, o, s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll));
@@ -77,7 +80,7 @@ __device__ __forceinline__ void trace_cells_item(const SceneView &S, int n_pix, 
     atomicAdd(counters + kCntPrimary, (unsigned long long)prim);
     atomicAdd(counters + kCntShadow, (unsigned long long)shad);
   }
-  if (shared_cos4) __syncwarp();  // the table is rewritten by the warp's next item
+  if (shared_subrays) __syncwarp();  // the table is rewritten by the warp's next item
 }
 
 // One pixel of a circuit launch (generate_pixels' circuit half,

@@ -367,16 +367,17 @@ typedef struct {
   int32_t chunk_candidates, chunk_cells;  /* chunk sizes timed, cells of the timed pipeline */
   double chunk_best_ms, chunk_default_ms; /* optics + circuit time of the chosen and of the previous chunk */
 } dvs_tuning;
-/* Autotuner, two stages, both on a prefix (up to 64 circuit cells) of the next
- * batch (the intervals dvs_sensor_process/enqueue will be given next):
- *  1. packet shape: the trace over a patch of up to 32768 pixels from the
- *     middle of the image, for each shape (cells per warp 4..32 x 1, 2 or 4
- *     sub-rays per lane);
+/* Autotuner, two stages, both on a prefix of the next batch (the intervals
+ * dvs_sensor_process/enqueue will be given next):
+ *  1. packet shape: the trace of up to 64 circuit cells over a patch of up
+ *     to 32768 pixels from the middle of the image, for each shape (cells per
+ *     warp 4..32 x 1, 2 or 4 sub-rays per lane);
  *  2. circuit-step chunking: the whole optics -> circuit pipeline of every
- *     pixel with the chosen shape, for chunks of 1, 1/2, 1/4 and 1/8 of the
- *     prefix (at least 4 cells), on a shadow copy of the circuit state --
+ *     pixel with the chosen shape over as many cells as the batch's default
+ *     chunk (at least 64, at most the batch), for chunks of 1, 1/2, 1/4 and
+ *     1/8 of them (at least 4 cells), on a shadow copy of the circuit state --
  *     smaller chunks keep the radiance of a launch in L2 for the circuit,
- *     larger ones launch less.
+ *     larger ones launch less and keep a block's packets on one pixel.
  * Each stage keeps the current setting unless another is >= 3 % faster.  No
  * circuit state, RNG or time changes; not allowed while an enqueued batch
  * awaits collect. */

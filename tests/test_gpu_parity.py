@@ -538,9 +538,10 @@ def test_packet_shape_and_autotuner_do_not_change_events():
         if tuned:
             assert tuned["rays_per_lane"] in (1, 2, 4) and tuned["cells_per_warp"] in (4, 8, 16, 32)
             assert tuned["candidates"] >= 4 and tuned["best_ms"] > 0
-            # second stage: the circuit-step chunk over the first 64 cells (64, 32, 16, 8)
-            assert tuned["chunk_cells"] == 64 and tuned["chunk_candidates"] == 4
-            assert tuned["cells_per_chunk"] in (8, 16, 32, 64) and tuned["chunk_best_ms"] > 0
+            # second stage: the circuit-step chunk over the batch's default chunk -- here 2048 cells
+            # (the 512 MB radiance bound at 64x48 pixels) of the 4000-cell batch: 2048, 1024, 512, 256
+            assert tuned["chunk_cells"] == 2048 and tuned["chunk_candidates"] == 4
+            assert tuned["cells_per_chunk"] in (256, 512, 1024, 2048) and tuned["chunk_best_ms"] > 0
     s = EventSensor(scene, phys)
     with pytest.raises(ValueError):
         s.set_tuning(3, 2)
