@@ -82,12 +82,12 @@ METRIC = "DVS events/s and Mrays/s at 1280x720 on 1 GB300; serving p99 latency v
 # (dram__bytes_read.sum + dram__bytes_write.sum) per pixel-cell.  Radiance
 # writes still held in L2 when the kernel ends are not in the DRAM count.
 TRACE_WARP_INSTRUCTIONS_PER_RAY = {
-    ("precision", "half+watertight", "sah", 32, 2): 1500654289593 / 29471262019,
-    ("orbit", "reference", "sah", 32, 2): 82134327371 / 1768685229,
+    ("precision", "half+watertight", "sah", 32, 2): 1466157173123 / 29471262019,
+    ("orbit", "reference", "sah", 32, 2): 79970172908 / 1768685229,
 }
 TRACE_DRAM_BYTES_PER_PIXEL_CELL = {
-    ("precision", "half+watertight", "sah", 32, 2): (67016192 + 221377024) / (921600 * 64),
-    ("orbit", "reference", "sah", 32, 2): (15039232 + 179304192) / (89960 * 640),
+    ("precision", "half+watertight", "sah", 32, 2): (66908416 + 219526144) / (921600 * 64),
+    ("orbit", "reference", "sah", 32, 2): (14630400 + 178991360) / (89960 * 640),
 }
 # ncu DRAM counters (dram__bytes_read.sum + dram__bytes_write.sum) of the 44
 # launches of one device-readout batch of 4,194,304 events (the readout
