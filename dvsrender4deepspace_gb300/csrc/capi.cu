@@ -2182,9 +2182,15 @@ int device_readout_fetch(dvs_device_readout *r) {
     r->ready.clear();
     r->head = 0;
   }
+  // host conversions of large batches run on all host threads (independent elements)
+  const size_t base = r->ready.size();
+  r->ready.resize(base + (size_t)std::max<int32_t>(released, 0));
+  HostEvent *dst = r->ready.data() + base;
+  const DevEvent *src = r->h_out;
+#pragma omp parallel for schedule(static) if (released > 65536)
   for (int32_t i = 0; i < released; ++i) {
-    const DevEvent &e = r->h_out[i];
-    r->ready.push_back(HostEvent{e.t, e.x, e.y, e.polarity, e.depth});
+    const DevEvent &e = src[i];
+    dst[i] = HostEvent{e.t, e.x, e.y, e.polarity, e.depth};
   }
   return DVS_OK;
 }
@@ -2243,7 +2249,8 @@ int dvs_device_readout_submit(dvs_device_readout *r, const dvs_event *events, si
   if (n > r->dro.max_batch) return fail(DVS_ERR_INVALID, "more events than the readout's batch size");
   if (!std::isfinite(now)) return fail(DVS_ERR_INVALID, "invalid readout time");
   CUDA_TRY(cudaSetDevice(r->device), "select device");
-  for (size_t i = 0; i < n; ++i) {
+#pragma omp parallel for schedule(static) if (n > 65536)
+  for (long long i = 0; i < (long long)n; ++i) {
     DevEvent d{};
     d.t = events[i].timestamp;
     d.depth = events[i].depth;
@@ -2283,8 +2290,10 @@ int dvs_device_readout_read(dvs_device_readout *r, dvs_event *out, size_t capaci
   if (!r || !n_out) return fail(DVS_ERR_INVALID, "null argument");
   const size_t m = std::min(capacity, r->ready.size() - r->head);
   if (m && !out) return fail(DVS_ERR_INVALID, "null output buffer");
-  for (size_t i = 0; i < m; ++i) {
-    const HostEvent &e = r->ready[r->head + i];
+  const HostEvent *src = r->ready.data() + r->head;
+#pragma omp parallel for schedule(static) if (m > 65536)
+  for (long long i = 0; i < (long long)m; ++i) {
+    const HostEvent &e = src[i];
     out[i].timestamp = e.t;
     out[i].x = e.x;
     out[i].y = e.y;

@@ -325,7 +325,7 @@ class EventReadout:
         out = np.zeros(max(n, 1), EVENT_DTYPE)
         got = C.c_size_t()
         check(self._call("read", out.ctypes.data, len(out), C.byref(got)))
-        return out[: got.value].copy()
+        return out if got.value == len(out) else out[: got.value].copy()
 
     def submit(self, events, now):
         ev = np.ascontiguousarray(events, EVENT_DTYPE) if len(events) else np.zeros(0, EVENT_DTYPE)
