@@ -1026,11 +1026,23 @@ __device__ void trace_nearest_packet_r(const SceneView &S, const float3 (&o)[R],
     for (int r = 0; r < R; ++r) h[r].hit = -1;
 }
 
+// The direction terms of a lane's shadow rays (all toward the same light):
+// formed once per pixel sample loop, not once per shadow packet.
+struct ShadowDir {
+  float3 idir;
+  WtRay wr;
+};
+template <int kGeo>
+__device__ __forceinline__ ShadowDir shadow_dir(float3 light) {
+  return ShadowDir{inverse_direction(light), wt_ray<kGeo>(light)};
+}
+
 template <int R, int kGeo>
-__device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], float3 light, const bool (&active)[R],
-                                      const int (&self)[R], int *stack_code, float *stack_t, bool (&occluded)[R]) {
-  const float3 idir1 = inverse_direction(light);
-  const WtRay wr = wt_ray<kGeo>(light);
+__device__ void trace_shadow_packet_r(const SceneView &S, const float3 (&o)[R], float3 light, const ShadowDir &sd,
+                                      const bool (&active)[R], const int (&self)[R], int *stack_code, float *stack_t,
+                                      bool (&occluded)[R]) {
+  const float3 idir1 = sd.idir;
+  const WtRay wr = sd.wr;
   float3 d[R], idir[R], op[R];
   bool alive[R];
   float reach[R];
@@ -1114,6 +1126,7 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
   // hapke_directional_reflectance normalizes the light for every shaded ray
   // (hapke.hpp:153-157); it is the same vector for all of this lane's rays
   const float3 lnorm = normalize(light);
+  const ShadowDir sdir = shadow_dir<kGeo>(light);
   for (int j = 0; j < n_sub; j += R) {
     float px[R], py[R];
     float3 ray[R], org[R];
@@ -1179,7 +1192,7 @@ __device__ PixelSample sample_pixel_group(const SceneView &S, int pixel, bool ac
       for (int r = 0; r < R; ++r) any_lit = any_lit || lit[r];
       if (__any_sync(kFull, any_lit)) {
         bool occ[R];
-        trace_shadow_packet_r<R, kGeo>(S, sorigin, light, lit, self, stack_code, stack_t, occ);
+        trace_shadow_packet_r<R, kGeo>(S, sorigin, light, sdir, lit, self, stack_code, stack_t, occ);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           if (lit[r]) ++out.shadow;
@@ -1219,6 +1232,7 @@ __device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const
   const int px_i = pixel % S.width, py_i = pixel / S.width;
   const HapkeConst hc = hapke_const(S.hapke);
   const float3 lnorm = normalize(light);  // as in sample_pixel_group
+  const ShadowDir sdir = shadow_dir<kGeo>(light);
   bool valid = true;
   for (int g = 0; g < n_sub; g += 32 * R) {
     float px[R], py[R];
@@ -1271,7 +1285,7 @@ __device__ PixelSample sample_pixel_subrays(const SceneView &S, int pixel, const
     double term[R] = {0.0, 0.0};
     if (kMode != kDepthOnly && __any_sync(kFull, lit[0] || lit[1])) {
       bool occ[R];
-      trace_shadow_packet_r<R, kGeo>(S, sorigin, light, lit, self, stack_code, stack_t, occ);
+      trace_shadow_packet_r<R, kGeo>(S, sorigin, light, sdir, lit, self, stack_code, stack_t, occ);
 #pragma unroll
       for (int r = 0; r < R; ++r)
         if (lit[r] && !occ[r]) {

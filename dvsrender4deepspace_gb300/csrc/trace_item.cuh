@@ -56,20 +56,26 @@ __device__ __forceinline__ void trace_cells_item(const SceneView &S, int n_pix, 
   const int pixel = rank < n_pix ? __ldg(S.pixel_of_rank + (rank_list ? rank_list[rank] : rank)) : 0;
   const CellPose pose = poses[c0 + (active ? cell : 0)];
   const int ss2 = S.samples * S.samples;
-  // one pixel per warp: its sub-rays' coordinates and FP64 cos^4 once per warp
-  const bool shared_subrays = kMode != kDepthOnly && cw_log2 == 5 && ss2 <= kSubrayTable;
+  // the warp's ppw pixels: their sub-rays' coordinates and FP64 cos^4 once per
+  // warp (entry p * ss2 + j: sub-ray j of the pixel in lanes p * cw ...)
+  const int table = ppw * ss2;
+  const bool shared_subrays = kMode != kDepthOnly && table <= kSubrayTable;
   if (shared_subrays) {
-    for (int j = lane; j < ss2; j += 32) {
-      const float x = subray_x(S, pixel % S.width, j % S.samples), y = subray_y(S, pixel / S.width, j / S.samples);
-      subrays[j] = SubraySample{cos4_of(x, y), x, y};
+    for (int q0 = 0; q0 < table; q0 += 32) {  // warp-uniform: every lane takes part in the shuffle
+      const int q = q0 + lane, p = min(q / ss2, ppw - 1);
+      const int pix = __shfl_sync(kFull, pixel, p << cw_log2);
+      if (q < table) {
+        const int j = q - p * ss2;
+        const float x = subray_x(S, pix % S.width, j % S.samples), y = subray_y(S, pix / S.width, j / S.samples);
+        subrays[q] = SubraySample{cos4_of(x, y), x, y};
+      }
     }
     __syncwarp();
   }
+  const SubraySample *mine = shared_subrays ? subrays + (lane >> cw_log2) * ss2 : nullptr;
   const PixelSample s =
-      kRays > 1 ? sample_pixel_group<kMode, kRays, kGeo>(S, pixel, active, pose, stack_code, stack_t,
-                                                         shared_subrays ? subrays : nullptr)
-                : sample_pixel_packet<kMode, kGeo>(S, pixel, active, pose, stack_code, stack_t,
-                                                   shared_subrays ? subrays : nullptr);
+      kRays > 1 ? sample_pixel_group<kMode, kRays, kGeo>(S, pixel, active, pose, stack_code, stack_t, mine)
+                : sample_pixel_packet<kMode, kGeo>(S, pixel, active, pose, stack_code, stack_t, mine);
   if (active) {
     const size_t o = (size_t)cell * n_pix + rank;
     store_radiance(S, radiance, o, s.valid ? s.radiance : __longlong_as_double(0x7ff8000000000000ll));
