@@ -242,23 +242,28 @@ struct SahBuilder {
     }
   }
 
+  // Per axis and bin: the union of the triangles' boxes, the bounds of their
+  // centroids, and their count.  A split's two sides are unions of bins, so
+  // the children's boxes and centroid bounds come from the bins: the same
+  // minima and maxima a scan of the children's triangles would give, without
+  // the scan.
   struct Bins {
     Box box[3][kSahBins];
+    Box cent[3][kSahBins];
     int32_t count[3][kSahBins];
     void clear() {
       for (int d = 0; d < 3; ++d)
         for (int j = 0; j < kSahBins; ++j) {
-          box[d][j] = empty_box();
+          box[d][j] = cent[d][j] = empty_box();
           count[d][j] = 0;
         }
     }
   };
 
-  int32_t build(int32_t b, int32_t e) {
+  // Range [b, e) with its box and its centroids' bounds.
+  int32_t build(int32_t b, int32_t e, Box range, Box cent) {
     const int32_t id = next.fetch_add(1);
     const int32_t n = e - b;
-    Box range, cent;
-    bounds(b, e, range, cent);
     if (n <= leaf_size) {
       BinNode &leaf = nodes[id];
       leaf.box = range;
@@ -282,12 +287,16 @@ struct SahBuilder {
       {
         Bins &p = part[k];
         p.clear();
-        for (int32_t i = chunk_begin(b, n, k, chunks), ie = chunk_begin(b, n, k + 1, chunks); i < ie; ++i)
+        for (int32_t i = chunk_begin(b, n, k, chunks), ie = chunk_begin(b, n, k + 1, chunks); i < ie; ++i) {
+          const SahRef &ref = refs[i];
+          const Box point{{ref.c[0], ref.c[1], ref.c[2]}, {ref.c[0], ref.c[1], ref.c[2]}};
           for (int d = 0; d < 3; ++d) {
-            const int j = bin_of(refs[i].c[d], cent.lo[d], scale[d], nb);
-            grow(p.box[d][j], refs[i].box);
+            const int j = bin_of(ref.c[d], cent.lo[d], scale[d], nb);
+            grow(p.box[d][j], ref.box);
+            grow(p.cent[d][j], point);
             ++p.count[d][j];
           }
+        }
       }
     }
 #pragma omp taskwait
@@ -296,6 +305,7 @@ struct SahBuilder {
       for (int d = 0; d < 3; ++d)
         for (int j = 0; j < nb; ++j) {
           grow(bins.box[d][j], part[k].box[d][j]);
+          grow(bins.cent[d][j], part[k].cent[d][j]);
           bins.count[d][j] += part[k].count[d][j];
         }
     // sweep every boundary of every axis
@@ -327,6 +337,7 @@ struct SahBuilder {
       }
     }
     int32_t m;
+    Box lrange, lcent, rrange, rcent;
     if (best_d >= 0) {
       // the same bin_of as the binning pass, so the split has the swept counts
       const int d = best_d;
@@ -334,19 +345,26 @@ struct SahBuilder {
       m = (int32_t)(std::partition(refs.begin() + b, refs.begin() + e,
                                    [&](const SahRef &r) { return bin_of(r.c[d], lo, sc, nb) < best_j; }) -
                     refs.begin());
+      lrange = lcent = rrange = rcent = empty_box();
+      for (int j = 0; j < nb; ++j) {
+        grow(j < best_j ? lrange : rrange, bins.box[d][j]);
+        grow(j < best_j ? lcent : rcent, bins.cent[d][j]);
+      }
     } else {
       m = b + n / 2;  // every centroid in one bin on every axis
+      bounds(b, m, lrange, lcent);
+      bounds(m, e, rrange, rcent);
     }
     int32_t l, r;
     if (n > 32768) {
-#pragma omp task shared(l)
-      l = build(b, m);
-#pragma omp task shared(r)
-      r = build(m, e);
+#pragma omp task shared(l, lrange, lcent)
+      l = build(b, m, lrange, lcent);
+#pragma omp task shared(r, rrange, rcent)
+      r = build(m, e, rrange, rcent);
 #pragma omp taskwait
     } else {
-      l = build(b, m);
-      r = build(m, e);
+      l = build(b, m, lrange, lcent);
+      r = build(m, e, rrange, rcent);
     }
     BinNode &nn = nodes[id];
     nn.box = range;
@@ -366,8 +384,8 @@ struct SahBuilder {
 // own, kNodeCost x area + S(b, 8); with j >= 2 slots the subtree may instead be
 // split between its two children, S(b, j) = min over k of D(left, k) +
 // D(right, j - k).  The wide node made from inner node b takes the children of
-// S(b, 8).  Both builders number a parent before its children, so one pass in
-// decreasing index fills the tables.  (Areas are the binary boxes' half areas;
+// S(b, 8).  A node's tables need its children's: they are filled in post
+// order, the subtrees of the top levels as parallel tasks.  (Areas are the binary boxes' half areas;
 // the ratio to the root's area is the probability a ray enters the box.)
 constexpr float kNodeCost = 1.0f, kTriCost = 1.0f;
 struct SlotPlan {
@@ -389,43 +407,64 @@ struct SlotPlan {
     emit(bin, bin[b].right, kBvhWidth - k, kids, nk);
   }
 };
+// D(i, .) of one node from its children's (already filled).
+void plan_node(const std::vector<BinNode> &bin, SlotPlan &p, size_t i) {
+  const BinNode &b = bin[i];
+  float *d = &p.d[8 * i];
+  if (b.count > 0) {
+    const float leaf = kTriCost * b.area * (float)b.count;
+    for (int j = 0; j < 8; ++j) d[j] = leaf;
+    return;
+  }
+  const float *dl = &p.d[8 * (size_t)b.left], *dr = &p.d[8 * (size_t)b.right];
+  float s[9];  // S(b, j), j = 2..8
+  uint8_t sk[9];
+  for (int j = 2; j <= 8; ++j) {
+    s[j] = std::numeric_limits<float>::infinity();
+    sk[j] = 1;
+    for (int k = 1; k < j; ++k) {
+      const float c = dl[k - 1] + dr[j - k - 1];
+      if (c < s[j]) { s[j] = c; sk[j] = (uint8_t)k; }
+    }
+  }
+  p.wide[i] = sk[8];
+  d[0] = kNodeCost * b.area + s[8];
+  for (int j = 2; j <= 8; ++j) {
+    if (s[j] < d[0]) {
+      d[j - 1] = s[j];
+      p.pick[8 * i + j - 1] = sk[j];
+    } else {
+      d[j - 1] = d[0];
+      p.pick[8 * i + j - 1] = 0;
+    }
+  }
+}
+// Children before their parent; the top levels' subtrees as parallel tasks.
+void plan_subtree(const std::vector<BinNode> &bin, SlotPlan &p, int32_t i, int depth) {
+  const BinNode &b = bin[i];
+  if (b.count == 0) {
+    if (depth < 12) {
+#pragma omp task shared(bin, p)
+      plan_subtree(bin, p, b.left, depth + 1);
+#pragma omp task shared(bin, p)
+      plan_subtree(bin, p, b.right, depth + 1);
+#pragma omp taskwait
+    } else {
+      plan_subtree(bin, p, b.left, depth + 1);
+      plan_subtree(bin, p, b.right, depth + 1);
+    }
+  }
+  plan_node(bin, p, (size_t)i);
+}
 SlotPlan plan_slots(const std::vector<BinNode> &bin, int32_t root) {
   SlotPlan p;
   const size_t n = bin.size();
   p.d.assign(8 * n, 0.0f);
   p.pick.assign(8 * n, 0);
   p.wide.assign(n, 1);
-  for (size_t i = n; i-- > (size_t)root;) {
-    const BinNode &b = bin[i];
-    float *d = &p.d[8 * i];
-    if (b.count > 0) {
-      const float leaf = kTriCost * b.area * (float)b.count;
-      for (int j = 0; j < 8; ++j) d[j] = leaf;
-      continue;
-    }
-    const float *dl = &p.d[8 * (size_t)b.left], *dr = &p.d[8 * (size_t)b.right];
-    float s[9];  // S(b, j), j = 2..8
-    uint8_t sk[9];
-    for (int j = 2; j <= 8; ++j) {
-      s[j] = std::numeric_limits<float>::infinity();
-      sk[j] = 1;
-      for (int k = 1; k < j; ++k) {
-        const float c = dl[k - 1] + dr[j - k - 1];
-        if (c < s[j]) { s[j] = c; sk[j] = (uint8_t)k; }
-      }
-    }
-    p.wide[i] = sk[8];
-    d[0] = kNodeCost * b.area + s[8];
-    for (int j = 2; j <= 8; ++j) {
-      if (s[j] < d[0]) {
-        d[j - 1] = s[j];
-        p.pick[8 * i + j - 1] = sk[j];
-      } else {
-        d[j - 1] = d[0];
-        p.pick[8 * i + j - 1] = 0;
-      }
-    }
-  }
+#pragma omp parallel
+#pragma omp single
+  plan_subtree(bin, p, root, 0);
   return p;
 }
 
@@ -479,7 +518,11 @@ bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf
     SahBuilder sb{refs, bin, {}, leaf_size};
 #pragma omp parallel
 #pragma omp single
-    root = sb.build(0, (int32_t)nt);
+    {
+      Box range, cent;
+      sb.bounds(0, (int32_t)nt, range, cent);
+      root = sb.build(0, (int32_t)nt, range, cent);
+    }
     bin.resize(sb.next.load());
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < ntl; ++i) order[i] = refs[i].id;
@@ -516,60 +559,81 @@ bool build_bvh(const float *V, size_t nv, const uint32_t *I, size_t nt, int leaf
     bin.resize(tb.next.load());
   }
 
-  // 4. collapse to kBvhWidth-wide, breadth first
+  // 4. collapse to kBvhWidth-wide, breadth first: level by level, each level's
+  // wide nodes in parallel; a prefix sum of their inner children numbers the
+  // next level in the order a serial breadth-first queue would
   const SlotPlan plan = collapse == 1 ? plan_slots(bin, root) : SlotPlan{};
   std::vector<BvhNode> nodes;
   nodes.reserve(bin.size() / (kBvhWidth - 1) + 2);
-  std::vector<int32_t> queue;  // binary node per wide node
-  std::vector<int32_t> level;
-  queue.push_back(root);
-  level.push_back(1);
-  int depth = 1;
-  for (size_t qi = 0; qi < queue.size(); ++qi) {
-    const int32_t b = queue[qi];
-    int32_t kids[kBvhWidth];
-    int nk = 0;
-    if (bin[b].count > 0) {
-      kids[nk++] = b;  // a leaf root: one leaf child
-    } else if (collapse == 1) {
-      plan.children(bin, b, kids, nk);
-    } else {
-      kids[nk++] = bin[b].left;
-      kids[nk++] = bin[b].right;
-      while (nk < kBvhWidth) {
-        int best = -1;
-        float best_area = -1;
-        for (int k = 0; k < nk; ++k)
-          if (bin[kids[k]].count == 0 && bin[kids[k]].area > best_area) { best = k; best_area = bin[kids[k]].area; }
-        if (best < 0) break;
-        const int32_t open = kids[best];
-        kids[best] = bin[open].left;
-        kids[nk++] = bin[open].right;
-      }
-    }
-    BvhNode node;
-    std::memset(&node, 0, sizeof(node));
-    for (int k = 0; k < kBvhWidth; ++k) {
-      BvhChild &out_child = node.c[k];
-      if (k >= nk) {
-        out_child.child = -1;
-        out_child.count = -1;
-        continue;
-      }
-      const BinNode &c = bin[kids[k]];
-      for (int d = 0; d < 3; ++d) { out_child.lo[d] = c.box.lo[d]; out_child.hi[d] = c.box.hi[d]; }
-      if (c.count > 0) {
-        out_child.child = c.start;
-        out_child.count = c.count;
+  std::vector<int32_t> level{root};  // binary node per wide node of the level
+  int depth = 0;
+  while (!level.empty()) {
+    ++depth;
+    const long long m = (long long)level.size();
+    const size_t base = nodes.size();
+    nodes.resize(base + (size_t)m);
+    std::vector<int32_t> kids_of((size_t)m * kBvhWidth);
+    std::vector<int> nk_of((size_t)m);
+    std::vector<long long> inner_at((size_t)m + 1, 0);  // inner children before wide node q of the level
+#pragma omp parallel for schedule(static) if (m > 4096)
+    for (long long q = 0; q < m; ++q) {
+      const int32_t b = level[q];
+      int32_t *kids = &kids_of[(size_t)q * kBvhWidth];
+      int nk = 0;
+      if (bin[b].count > 0) {
+        kids[nk++] = b;  // a leaf root: one leaf child
+      } else if (collapse == 1) {
+        plan.children(bin, b, kids, nk);
       } else {
-        out_child.child = (int32_t)queue.size();
-        out_child.count = 0;
-        queue.push_back(kids[k]);
-        level.push_back(level[qi] + 1);
-        depth = std::max(depth, level[qi] + 1);
+        kids[nk++] = bin[b].left;
+        kids[nk++] = bin[b].right;
+        while (nk < kBvhWidth) {
+          int best = -1;
+          float best_area = -1;
+          for (int k = 0; k < nk; ++k)
+            if (bin[kids[k]].count == 0 && bin[kids[k]].area > best_area) { best = k; best_area = bin[kids[k]].area; }
+          if (best < 0) break;
+          const int32_t open = kids[best];
+          kids[best] = bin[open].left;
+          kids[nk++] = bin[open].right;
+        }
       }
+      nk_of[q] = nk;
+      int inner = 0;
+      for (int k = 0; k < nk; ++k) inner += bin[kids[k]].count > 0 ? 0 : 1;
+      inner_at[q + 1] = inner;
     }
-    nodes.push_back(node);
+    for (long long q = 0; q < m; ++q) inner_at[q + 1] += inner_at[q];
+    const size_t next_base = base + (size_t)m;
+    std::vector<int32_t> next((size_t)inner_at[m]);
+#pragma omp parallel for schedule(static) if (m > 4096)
+    for (long long q = 0; q < m; ++q) {
+      const int32_t *kids = &kids_of[(size_t)q * kBvhWidth];
+      const int nk = nk_of[q];
+      long long slot = inner_at[q];
+      BvhNode node;
+      std::memset(&node, 0, sizeof(node));
+      for (int k = 0; k < kBvhWidth; ++k) {
+        BvhChild &out_child = node.c[k];
+        if (k >= nk) {
+          out_child.child = -1;
+          out_child.count = -1;
+          continue;
+        }
+        const BinNode &c = bin[kids[k]];
+        for (int d = 0; d < 3; ++d) { out_child.lo[d] = c.box.lo[d]; out_child.hi[d] = c.box.hi[d]; }
+        if (c.count > 0) {
+          out_child.child = c.start;
+          out_child.count = c.count;
+        } else {
+          out_child.child = (int32_t)(next_base + (size_t)slot);
+          out_child.count = 0;
+          next[(size_t)slot++] = kids[k];
+        }
+      }
+      nodes[base + (size_t)q] = node;
+    }
+    level.swap(next);
   }
   if ((kBvhWidth - 1) * depth + 1 > kStackSlots) {
     error = "BVH too deep for the traversal stack (depth " + std::to_string(depth) + ")";
