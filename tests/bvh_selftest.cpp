@@ -128,7 +128,17 @@ int main(int argc, char **argv) {
   }
   for (size_t t = 0; t < nt; ++t)
     if (seen[t] != 1) { std::printf("triangle %zu in %d leaves\n", t, seen[t]); return 1; }
-  std::printf("nodes %zu depth %d leaves %zu max_slack %.3g sah_nodes %.6g sah_tris %.6g\n", bvh.nodes.size(),
-              bvh.depth, leaves, max_slack, bvh.sah_node_visits, bvh.sah_triangle_tests);
+  // FNV-1a over the wide nodes, the triangle order and the depth: the tree's identity
+  uint64_t hash = 1469598103934665603ull;
+  auto mix = [&hash](const void *p, size_t bytes) {
+    const unsigned char *c = static_cast<const unsigned char *>(p);
+    for (size_t i = 0; i < bytes; ++i) hash = (hash ^ c[i]) * 1099511628211ull;
+  };
+  mix(bvh.nodes.data(), sizeof(BvhNode) * bvh.nodes.size());
+  mix(bvh.order.data(), sizeof(uint32_t) * bvh.order.size());
+  mix(&bvh.depth, sizeof bvh.depth);
+  std::printf("nodes %zu depth %d leaves %zu max_slack %.3g sah_nodes %.6g sah_tris %.6g hash %016llx\n",
+              bvh.nodes.size(), bvh.depth, leaves, max_slack, bvh.sah_node_visits, bvh.sah_triangle_tests,
+              (unsigned long long)hash);
   return 0;
 }

@@ -68,3 +68,21 @@ def test_slot_budget_collapse_lowers_the_node_cost(selftest):
             got[collapse] = (float(f[9]), float(f[11]), int(f[5]))
         assert got[1][0] <= got[0][0] * (1 + 1e-6) and got[1][2] == got[0][2], got
         assert abs(got[1][1] - got[0][1]) <= 1e-9 * got[0][1], got
+
+
+@pytest.mark.parametrize("builder,collapse", [(0, 1), (0, 0), (1, 1)])
+def test_tree_is_the_same_at_every_thread_count(selftest, builder, collapse):
+    """The builder runs in parallel (chunked binning, subtree tasks, the slot
+    tables as post-order tasks, each level's wide nodes at once); the tree it
+    returns -- node bytes, triangle order, depth -- is the same with one thread
+    as with several.  2.1 M triangles reach every parallel path."""
+    hashes = set()
+    for threads in ("1", "3", "8"):
+        env = dict(os.environ, OMP_NUM_THREADS=threads)
+        out = subprocess.run([selftest, "9", "1024", "10240.0", str(builder), str(collapse)], capture_output=True,
+                             text=True, env=env)
+        assert out.returncode == 0, out.stdout + out.stderr
+        f = out.stdout.split()
+        assert f[12] == "hash", out.stdout
+        hashes.add(f[13])
+    assert len(hashes) == 1, hashes
