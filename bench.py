@@ -742,8 +742,10 @@ def run_readout(args, n_events=1 << 22):
                        "batch_window_s": 64e-6, "bandwidth": 1e12, "latency": 0.0, "capacity": 1 << 24,
                        "l2": "inputs larger than L2: each batch's events are 100.7 MB on the device, "
                              "its sort buffers 3 x 67 MB"},
+            # per batch: the events as 24-byte device records plus the count and time in; the
+            # released events as 24-byte device records plus four status words (24 B) out
             "e2e": {"value": n_events * n / wall, "unit": "events/s", "h2d_bytes_per_step": n_events * 24 + 16,
-                    "d2h_bytes_per_step": n_events * batches[0].dtype.itemsize},
+                    "d2h_bytes_per_step": n_events * 24 + 24},
             "roofline": {"bound": "hbm", "kernel": "device readout (radix sort, max-plus scan, release)",
                          "achieved": alg / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": alg / (ms / 1e3) / 1e9 / peak, "traffic": READOUT_DRAM_BYTES_PER_EVENT * n_events,
